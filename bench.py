@@ -1,0 +1,324 @@
+"""VMC step throughput of the GB300 path (one JSON line on stdout).
+
+Workload: transverse-field Ising 10x10 periodic (J=1, h=3), ConvNetAutoregressive2D
+depth 10, 32 channels (weight-normalised), 4096 exact samples per step from the
+persistent sampler, local energy over the 101 connected configurations of each
+sample, adjoint gradient, Adam -- the full VMC step of the BF16 tensor-core path.
+The same step on the plain FP32 CUDA-core path of the same code is timed beside
+it. Synthetic, seeded: random-init weights, Philox samples.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU restatement of the reference algorithm (the
+reference is TensorFlow 1.x and cannot run here) on the host cores, on a
+bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+import torch
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SHAPE = (10, 10)
+DEPTH = 10
+CHANNELS = 32
+BATCH = 4096
+H_FIELD = 3.0
+METRIC = "VMC steps/s & samples/s, BF16+adjoint vs plain FP32 on GPU at matched energy"
+WORKLOAD = "TFIM 10x10 PBC J=1 h=3; ConvNetAutoregressive2D depth 10 F32 (weight norm); 4096 samples/step; " \
+           "full VMC step: exact AR sampling + local energy (101 conn/sample) + adjoint gradient + Adam"
+
+
+def flops_per_sample_forward(shape, depth, f):
+    """Dense conv FLOPs of one forward (2 * MACs/site * sites), zero-padded
+    taps included: the reference's per-unit figure."""
+    n_cc = 2 * depth - 2
+    first = 9 * f + 3 * f + 2 * f * (f // 2) + 9 * f * f
+    rest = 22 * f * f
+    head = 4 * f
+    return 2 * (first + (n_cc - 1) * rest + head) * shape[0] * shape[1]
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--fp32-steps", type=int, default=2)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_init(n):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend=backend)
+        if torch.cuda.is_available():
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self):
+        self.proc = None
+        self.path = os.path.join(ROOT, "_work", "bench_clocks.csv")
+
+    def start(self):
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-i", str(torch.cuda.current_device()), "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+        if self.proc is None:
+            return out
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if sm:
+            out = {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                   "samples": len(sm)}
+        return out
+
+
+# ------------------------------------------------------------------ CPU arm
+def cpu_vmc_sample(batch, seed, threads):
+    """One VMC step of the reference algorithm restated on the CPU (oracle),
+    for `batch` samples: fast AR sampling, local energy over all connections,
+    autograd gradient. Returns seconds."""
+    from oracle import ar2d, operators
+    from oracle.fast_sampler import FastSamplerCPU
+    torch.set_num_threads(threads)
+    params = ar2d.init_params(SHAPE, DEPTH, CHANNELS, True, seed=0)
+    p32 = ar2d.params_to(params, torch.float32)
+    t0 = time.perf_counter()
+    spins = FastSamplerCPU(params, SHAPE, DEPTH, True, dtype=torch.float32).sample(batch, seed=seed, offset=0)
+    conn, mel, use = operators.ising_find_conn(spins, h=H_FIELD, pbc=True)
+    with torch.no_grad():
+        flat = torch.as_tensor(conn.reshape((-1,) + SHAPE).astype(np.int8))
+        re, im = ar2d.log_psi(p32, flat, DEPTH, True)
+    lv = (re.double().numpy() + 1j * im.double().numpy()).reshape(conn.shape[0], batch)
+    local = (mel * np.exp(lv - lv[0])).sum(axis=0)
+    y = np.conj(local - local.mean()) / batch
+    ar2d.weighted_gradient(p32, spins, DEPTH, True, 2 * y.real / batch, -2 * y.imag / batch, dtype=torch.float32)
+    return time.perf_counter() - t0
+
+
+def reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    batch = 16
+    for i in range(args.warmup):
+        cpu_vmc_sample(batch, 100 + i, threads)
+    times = [cpu_vmc_sample(batch, i, threads) for i in range(args.steps)]
+    t = float(np.mean(times))
+    value = batch / t
+    line = {"metric": METRIC, "value": value, "unit": "samples/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "cpu_sample": f"{batch} samples per step"},
+            "cpu_baseline": {"value": value, "unit": "samples/s", "cores": threads, "kind": "port",
+                             "sample": f"{batch} of the 4096 samples of one VMC step per timed step (oracle "
+                                       "restatement: fast AR sampler, all 101 connections, autograd)"},
+            "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ GPU arm
+def build_problem(precision, seed_offset):
+    from flowket_gb300.machines import ConvNetAutoregressive2D
+    from flowket_gb300.operators import Ising
+    from flowket_gb300.optimization import VariationalMonteCarlo
+    from flowket_gb300.optimizers import Adam
+    from flowket_gb300.samplers import FastAutoregressiveSampler
+    m = ConvNetAutoregressive2D(SHAPE, DEPTH, CHANNELS, weights_normalization=True, precision=precision, seed=0)
+    vmc = VariationalMonteCarlo(m, Ising(h=H_FIELD, hilbert_state_shape=SHAPE, pbc=True),
+                                FastAutoregressiveSampler(m, BATCH, seed=1234 + seed_offset))
+    return m, vmc, Adam(m, lr=1e-3)
+
+
+def timed_steps(vmc, opt, k):
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    fwd_ms, rows = 0.0, 0
+    torch.cuda.synchronize()
+    start.record()
+    for _ in range(k):
+        vmc.step(opt, sync=False)
+        fwd_ms_i, rows_i = vmc.energy_observable.last_forward
+        rows += rows_i
+    stop.record()
+    torch.cuda.synchronize()
+    for ev in vmc.energy_observable.forward_events:
+        fwd_ms += ev[0].elapsed_time(ev[1])
+    vmc.energy_observable.forward_events.clear()
+    vmc.finish_step()
+    return start.elapsed_time(stop), fwd_ms, rows
+
+
+def ours_arm(args, rank, world):
+    from flowket_gb300 import _lib
+    lib = _lib.load()
+    m, vmc, opt = build_problem("bf16", rank)
+    obs = vmc.energy_observable
+    obs.record_forward = True
+    for _ in range(args.warmup):
+        vmc.step(opt)
+    obs.forward_events.clear()
+    clocks = Clocks()
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks.start()
+    l0 = lib.fk_kernel_launches()
+    total_ms, fwd_ms, rows = timed_steps(vmc, opt, args.steps)
+    launches = lib.fk_kernel_launches() - l0
+    clk = clocks.stop()
+    barrier(world)
+    total_ms = max_over_ranks(total_ms, world)
+    ms_per_step = total_ms / args.steps
+    samples_per_s = world * BATCH * args.steps / (total_ms / 1e3)
+    energy_bf16 = vmc.current_energy.real
+
+    # e2e: the public API with the host owning the parameters (pinned) and the
+    # reference's host-side outputs (samples, local energies, energy stats).
+    host_params = torch.empty(m.num_params, dtype=torch.float32, pin_memory=True)
+    host_params.copy_(m.params)
+    host_spins = torch.empty((BATCH,) + SHAPE, dtype=torch.int8, pin_memory=True)
+    host_local = torch.empty((BATCH, 2), dtype=torch.float64, pin_memory=True)
+    host_stats = torch.empty(3, dtype=torch.float64, pin_memory=True)
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        m.params.copy_(host_params, non_blocking=True)
+        m.params_updated()
+        stats = vmc.step(opt, sync=False)
+        host_params.copy_(m.params, non_blocking=True)
+        host_spins.copy_(vmc.current_batch, non_blocking=True)
+        host_local.copy_(vmc._local, non_blocking=True)
+        host_stats.copy_(stats, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+    e2e = {"value": world * BATCH * args.steps / e2e_s, "unit": "samples/s",
+           "h2d_bytes_per_step": m.num_params * 4,
+           "d2h_bytes_per_step": m.num_params * 4 + BATCH * SHAPE[0] * SHAPE[1] + BATCH * 16 + 24}
+
+    # plain FP32 path of the same code
+    fp32 = None
+    if args.fp32_steps > 0:
+        m32, vmc32, opt32 = build_problem("fp32", rank)
+        vmc32.energy_observable.record_forward = True
+        vmc32.step(opt32)
+        vmc32.energy_observable.forward_events.clear()
+        t32, _, _ = timed_steps(vmc32, opt32, args.fp32_steps)
+        fp32 = {"samples_per_s": BATCH / (t32 / args.fp32_steps / 1e3), "ms_per_step": t32 / args.fp32_steps,
+                "energy": vmc32.current_energy.real, "steps": args.fp32_steps}
+
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = peaks.get("bf16_tflops_sustained") or 1700.0
+    fps = flops_per_sample_forward(SHAPE, DEPTH, CHANNELS)
+    achieved = rows * fps / (fwd_ms / 1e3) / 1e12 if fwd_ms > 0 else None
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        traffic = json.load(open(tpath)).get("ar2d_forward_bytes_per_config")
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": samples_per_s, "unit": "samples/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+                "vmc_steps_per_s": 1e3 / ms_per_step, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "bf16", "data": "synthetic (seeded init, Philox samples)",
+                "config": {"workload": WORKLOAD, "batch_per_gpu": BATCH, "lattice": list(SHAPE), "depth": DEPTH,
+                           "channels": CHANNELS, "parallelism": f"replicas x{world}",
+                           "l2": "inputs larger than L2 (activation workspaces of several GB per step)"},
+                "energy_bf16": energy_bf16, "fp32_path": fp32,
+                "bf16_over_fp32": (samples_per_s / world) / fp32["samples_per_s"] if fp32 else None,
+                "stage_ms": vmc.times,
+                "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                             "frac": achieved / peak if achieved else None,
+                             "traffic": traffic,
+                             "kernel": "AR2D conv ops (V/H/C) of the local-energy forward",
+                             "flops_per_config": fps, "configs_timed": rows},
+                "clocks": clk, "gpu_launches": launches, "e2e": e2e}
+        if not args.no_cpu_baseline:
+            threads = os.cpu_count() or 1
+            n = 8
+            cpu_vmc_sample(2, 7, threads)
+            t = cpu_vmc_sample(n, 0, threads)
+            line["cpu_baseline"] = {"value": n / t, "unit": "samples/s", "cores": threads, "kind": "port",
+                                    "sample": f"{n} samples of one VMC step (oracle restatement on the host: "
+                                              "fast AR sampler, 101 connections each, autograd gradient)"}
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world = dist_init(args.gpus)
+    if args.impl == "reference":
+        reference_arm(args, rank, world)
+    else:
+        ours_arm(args, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

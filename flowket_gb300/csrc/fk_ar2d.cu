@@ -1,0 +1,1007 @@
+// ConvNetAutoregressive2D forward pass, exact sampler and weight packing.
+//
+// Network (machines/conv_net_autoregressive_2D.py:24-74), per causal conv i:
+//   V op  : Vp = conv3x3(V_i) [taps rows -2..0, cols -1..1] + b_v
+//           V_{i+1} = relu(Vp [+ residual]);  RV = relu(Vp)
+//           U = relu(W_y RV + b_y)  -> Cat[r+1, c][F/2:F]   (DownShift, :44-45)
+//   H op  : T = relu(conv1x3(H_i) [cols -2..0] + b_h)
+//           Z = relu(W_x T + b_x)   -> Cat[r, c+s][0:F/2]   (RightShift s=1 on the
+//                                                            final conv, :41-43)
+//   C op  : Hp = conv3x3(Cat) [rows -2..0, cols -2..0] + b_c
+//           H_{i+1} = relu(Hp [+ residual]); on the final conv the 1x1 head
+//           W_o relu(Hp) + b_o gives the four outputs (Re0, Re1, Im0, Im1).
+// Boundary values of the shifted tensors are relu(bias) (a shifted-in zero
+// through the 1x1 conv + relu), written by the ops at r == 0 / c == 0.
+//
+// Every op is executed per (tile of 128 samples, pixel) by one CTA of 128
+// threads (thread = sample). Two engines compute the GEMMs:
+//   * FP32 CUDA cores (the plain FP32 path): thread-local accumulators;
+//   * BF16 tcgen05: taps and weight slices arrive by bulk copies (TMA) into
+//     shared memory, one thread issues tcgen05.mma (M=128, N=F, K=16 steps)
+//     into TMEM, the epilogue reads TMEM with tcgen05.ld; the chained 1x1 is
+//     a second MMA on the epilogue's bf16 output staged in shared memory.
+// Both engines share the epilogue, so the two precisions run the same code
+// path apart from the GEMMs.
+#include "fk_ar2d.cuh"
+
+#include <math.h>
+#include <string.h>
+
+namespace fk {
+
+// ============================================================== layout (host)
+int build_layout(const fk_ar2d_desc* d, NetLayout* L) {
+  if (!d) {
+    set_error("fk_ar2d: NULL descriptor");
+    return FK_ERR_ARG;
+  }
+  if (d->height < 1 || d->width < 1 || d->height * d->width > 4096 || d->depth < 2 || d->depth > 20 ||
+      !(d->channels == 16 || d->channels == 32 || d->channels == 64) ||
+      !(d->precision == FK_PRECISION_FP32 || d->precision == FK_PRECISION_BF16)) {
+    set_error("fk_ar2d: unsupported shape (H=%d W=%d depth=%d channels=%d precision=%d); "
+              "supported: depth 2..20, channels 16/32/64",
+              d->height, d->width, d->depth, d->channels, d->precision);
+    return FK_ERR_ARG;
+  }
+  memset(L, 0, sizeof(*L));
+  L->H = d->height;
+  L->W = d->width;
+  L->P = d->height * d->width;
+  L->depth = d->depth;
+  L->F = d->channels;
+  L->wn = d->weights_normalization ? 1 : 0;
+  L->precision = d->precision;
+  L->n_cc = 2 * d->depth - 2;
+  const int F = L->F;
+  int64_t p = 0, w = 0;
+  auto add = [&](int kh, int kw, int cin, int cout, bool wn) {
+    ConvDesc& c = L->conv[L->n_convs++];
+    c.kh = kh;
+    c.kw = kw;
+    c.cin = cin;
+    c.cout = cout;
+    c.K = kh * kw * cin;
+    c.Kpad = (c.K + 15) / 16 * 16;
+    c.Npad = cout < 16 ? 16 : (cout + 15) / 16 * 16;
+    c.p_kernel = p;
+    p += (int64_t)c.K * cout;
+    c.p_bias = p;
+    p += cout;
+    c.p_g = -1;
+    if (wn) {
+      c.p_g = p;
+      p += cout;
+    }
+    c.w_off = w;
+    if (L->precision == FK_PRECISION_BF16) {
+      w += ((int64_t)c.Kpad * c.Npad * 2 + 255) / 256 * 256;
+    }
+    c.w32_off = w;
+    w += ((int64_t)c.K * cout * 4 + 255) / 256 * 256;
+    c.b_off = w;
+    w += ((int64_t)c.Npad * 4 + 255) / 256 * 256;
+  };
+  for (int i = 0; i < L->n_cc; ++i) {
+    int cin = i == 0 ? 1 : F;
+    add(3, 3, cin, F, L->wn);      // v
+    add(1, 3, cin, F, L->wn);      // h
+    add(1, 1, F, F / 2, L->wn);    // x
+    add(1, 1, F, F / 2, L->wn);    // y
+    add(3, 3, F, F, L->wn);        // c
+  }
+  add(1, 1, F, 4, false);          // out head
+  L->num_params = p;
+  L->packed_bytes = w;
+  return FK_OK;
+}
+
+static inline int64_t esize(const NetLayout& L) { return L.precision == FK_PRECISION_BF16 ? 2 : 4; }
+
+int64_t tensor_bytes(const NetLayout& L, int64_t tiles, int channels) {
+  int64_t b = tiles * L.P * (int64_t)kTile * channels * esize(L);
+  return (b + 255) / 256 * 256;
+}
+
+int64_t workspace_layout(const NetLayout& L, int64_t batch, int mode, char* base, Tensors* T) {
+  int64_t tiles = (batch + kTile - 1) / kTile;
+  int64_t tb = tensor_bytes(L, tiles, L.F);
+  int64_t off = 0;
+  auto take = [&](int64_t bytes) -> void* {
+    void* ptr = base ? base + off : nullptr;
+    off += (bytes + 255) / 256 * 256;
+    return ptr;
+  };
+  if (T) memset(T, 0, sizeof(*T));
+  Tensors tmp;
+  Tensors* t = T ? T : &tmp;
+  if (mode == FK_AR2D_INFER) {
+    t->v[0] = take(tb);
+    t->v[1] = take(tb);
+    t->h[0] = take(tb);
+    t->h[1] = take(tb);
+    t->cat[0] = take(tb);
+  } else {
+    for (int i = 0; i < L.n_cc; ++i) {
+      t->v[i] = take(tb);
+      t->h[i] = take(tb);
+      t->cat[i] = take(tb);
+      t->t[i] = take(tb);
+      t->rv[i] = take(tb);
+    }
+  }
+  t->row_partial = static_cast<float2*>(take(tiles * L.H * kTile * sizeof(float2)));
+  t->bytes = off;
+  return off;
+}
+
+// ============================================================== weight packing
+struct PackArgs {
+  const float* params;
+  char* packed;
+  int n_convs;
+  int bf16;
+  ConvDesc conv[kMaxConvs];
+};
+
+// One CTA per conv: weight-norm scale per output channel (wrappers.py:130-134:
+// v * rsqrt(max(sum v^2, 1e-12)) * exp(g)), then the operand layout.
+__global__ void pack_kernel(const __grid_constant__ PackArgs a) {
+  const ConvDesc& c = a.conv[blockIdx.x];
+  __shared__ float scale[64];
+  const float* v = a.params + c.p_kernel;
+  for (int n = threadIdx.x; n < c.cout; n += blockDim.x) {
+    float s = 1.f;
+    if (c.p_g >= 0) {
+      float sq = 0.f;
+      for (int k = 0; k < c.K; ++k) {
+        float x = v[(int64_t)k * c.cout + n];
+        sq += x * x;
+      }
+      s = rsqrtf(fmaxf(sq, 1e-12f)) * expf(a.params[c.p_g + n]);
+    }
+    scale[n] = s;
+  }
+  __syncthreads();
+  float* bias = reinterpret_cast<float*>(a.packed + c.b_off);
+  for (int n = threadIdx.x; n < c.Npad; n += blockDim.x) bias[n] = n < c.cout ? a.params[c.p_bias + n] : 0.f;
+  {
+    float* w = reinterpret_cast<float*>(a.packed + c.w32_off);
+    int total = c.K * c.cout;
+    for (int i = threadIdx.x; i < total; i += blockDim.x) w[i] = v[i] * scale[i % c.cout];
+  }
+  if (a.bf16) {
+    __nv_bfloat16* w = reinterpret_cast<__nv_bfloat16*>(a.packed + c.w_off);
+    int total = c.Kpad * c.Npad;
+    for (int i = threadIdx.x; i < total; i += blockDim.x) {
+      // element (k, n) of the no-swizzle K-major operand at ((k/8)*Npad + n)*8 + k%8
+      int kg = i / (c.Npad * 8);
+      int rem = i - kg * c.Npad * 8;
+      int n = rem / 8, e = rem % 8;
+      int k = kg * 8 + e;
+      float x = (k < c.K && n < c.cout) ? v[(int64_t)k * c.cout + n] * scale[n] : 0.f;
+      w[i] = __float2bfloat16_rn(x);
+    }
+  }
+}
+
+// ============================================================== GEMM engines
+// ---- FP32 CUDA-core engine
+template <int F>
+__device__ void simt_main(const OpArgs& a, int64_t tile, int m, int r, int c, int H, int W, int P, float* acc) {
+#pragma unroll
+  for (int n = 0; n < F; ++n) acc[n] = 0.f;
+  const float* Wm = static_cast<const float*>(a.main.w);
+  const int nt = num_taps(a.kind);
+  for (int t = 0; t < nt; ++t) {
+    int dr, dc;
+    tap_offset(a.kind, t, dr, dc);
+    int rr = r + dr, cc = c + dc;
+    if (rr < 0 || rr >= H || cc < 0 || cc >= W) continue;
+    int pix = rr * W + cc;
+    if (a.first) {
+      float s = spin_at(a.spins, a.batch, P, tile * kTile + m, pix);
+      const float4* w4 = reinterpret_cast<const float4*>(Wm + (int64_t)t * F);
+#pragma unroll
+      for (int n4 = 0; n4 < F / 4; ++n4) {
+        float4 wv = __ldg(w4 + n4);
+        acc[4 * n4 + 0] += s * wv.x;
+        acc[4 * n4 + 1] += s * wv.y;
+        acc[4 * n4 + 2] += s * wv.z;
+        acc[4 * n4 + 3] += s * wv.w;
+      }
+    } else {
+      const float* x = blk<float>(a.in, tile, P, pix, F);
+      for (int g = 0; g < F / 8; ++g) {
+        float v[8];
+        ld8(x + ((int64_t)g * kTile + m) * 8, v);
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+          const float4* w4 = reinterpret_cast<const float4*>(Wm + ((int64_t)t * F + g * 8 + e) * F);
+#pragma unroll
+          for (int n4 = 0; n4 < F / 4; ++n4) {
+            float4 wv = __ldg(w4 + n4);
+            acc[4 * n4 + 0] += v[e] * wv.x;
+            acc[4 * n4 + 1] += v[e] * wv.y;
+            acc[4 * n4 + 2] += v[e] * wv.z;
+            acc[4 * n4 + 3] += v[e] * wv.w;
+          }
+        }
+      }
+    }
+  }
+}
+
+// out[0..NC) = in[0..KC) x W[KC][NC] (fp32, row-major)
+template <int KC, int NC>
+__device__ __forceinline__ void simt_chain(const ConvW& cw, const float* in, float* out) {
+  const float* Wc = static_cast<const float*>(cw.w);
+#pragma unroll
+  for (int n = 0; n < NC; ++n) out[n] = 0.f;
+#pragma unroll 4
+  for (int k = 0; k < KC; ++k) {
+    float x = in[k];
+#pragma unroll
+    for (int n = 0; n < NC; ++n) out[n] += x * __ldg(Wc + k * NC + n);
+  }
+}
+
+// ---- BF16 tcgen05 engine
+struct TcSmem {
+  uint32_t a, w, ca, cw;    // shared addresses of the regions
+  uint8_t* a_ptr;
+  uint8_t* ca_ptr;
+  uint8_t* w_ptr;
+  uint8_t* cw_ptr;
+  uint64_t* bar_load;
+  uint64_t* bar_mma;
+  uint32_t* tmem_slot;
+  int taps_per_group;
+};
+
+template <int F>
+struct TcCfg {
+  static constexpr int kTapBytesA = kTile * F * 2;
+  static constexpr int kTapBytesW = F * F * 2;
+  static constexpr int kChainNpad = (F / 2) < 16 ? 16 : (F / 2);
+  static constexpr int kGroupBudget = 176 * 1024;
+  static constexpr int kTaps = (kGroupBudget / (kTapBytesA + kTapBytesW)) > 9 ? 9
+                                                                             : (kGroupBudget / (kTapBytesA + kTapBytesW));
+  static constexpr int kBytesA = kTaps * kTapBytesA;
+  static constexpr int kBytesW = kTaps * kTapBytesW;
+  static constexpr int kBytesCA = kTile * F * 2;
+  static constexpr int kBytesCW = F * 32 * 2;
+  static constexpr int kSmem = kBytesA + kBytesW + kBytesCA + kBytesCW + 64;
+};
+
+template <int F>
+__device__ __forceinline__ void tc_carve(uint8_t* base, TcSmem& s) {
+  using C = TcCfg<F>;
+  s.a_ptr = base;
+  s.w_ptr = base + C::kBytesA;
+  s.ca_ptr = s.w_ptr + C::kBytesW;
+  s.cw_ptr = s.ca_ptr + C::kBytesCA;
+  uint8_t* bars = s.cw_ptr + C::kBytesCW;
+  s.bar_load = reinterpret_cast<uint64_t*>(bars);
+  s.bar_mma = reinterpret_cast<uint64_t*>(bars + 8);
+  s.tmem_slot = reinterpret_cast<uint32_t*>(bars + 16);
+  s.a = smem_u32(s.a_ptr);
+  s.w = smem_u32(s.w_ptr);
+  s.ca = smem_u32(s.ca_ptr);
+  s.cw = smem_u32(s.cw_ptr);
+  s.taps_per_group = C::kTaps;
+}
+
+struct TcState {
+  uint32_t tmem;
+  uint32_t ph_load, ph_mma;
+  int* err;
+  bool abort;
+};
+
+constexpr uint32_t kTmemCols = 128;
+constexpr uint32_t kChainCol = 64;
+
+// Setup: barriers + 128 TMEM columns (warp 0 allocates).
+__device__ __forceinline__ void tc_setup(TcSmem& s, TcState& st, int* err) {
+  if (threadIdx.x == 0) {
+    mbar_init(s.bar_load, 1);
+    mbar_init(s.bar_mma, 1);
+    fence_mbar_init();
+  }
+  if (threadIdx.x < 32) {
+    tmem_alloc(s.tmem_slot, kTmemCols);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  st.tmem = *s.tmem_slot;
+  st.ph_load = 0;
+  st.ph_mma = 0;
+  st.err = err;
+  st.abort = false;
+}
+
+__device__ __forceinline__ void tc_teardown(TcState& st) {
+  tc_fence_before();
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    tc_fence_after();
+    tmem_dealloc(st.tmem, kTmemCols);
+  }
+}
+
+__device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t& ph, TcState& st) {
+  bool ok = mbar_wait(bar, ph, st.err);
+  ph ^= 1u;
+  if (!ok) st.abort = true;
+  return ok;
+}
+
+// Loads TMEM columns [col, col+N) of this thread's lane (sample) into v.
+template <int N>
+__device__ __forceinline__ void tc_read(const TcState& st, uint32_t col, float* v) {
+  uint32_t lane_base = (uint32_t)((threadIdx.x / 32) * 32) << 16;
+#pragma unroll
+  for (int q = 0; q < N / 16; ++q) tmem_ld16(st.tmem + lane_base + col + q * 16, v + q * 16);
+  tmem_ld_wait();
+}
+
+// Main conv GEMM of one op at (tile, r, c) into acc[F] (pre-bias) on tensor cores.
+// The chained 1x1 weights are brought in with the first load group.
+template <int F>
+__device__ void tc_main(const OpArgs& a, TcSmem& s, TcState& st, int64_t tile, int m, int r, int c, int H, int W,
+                        int P, float* acc) {
+  using C = TcCfg<F>;
+  const uint32_t idesc = umma_idesc_bf16(128, F);
+  const int chain_bytes = F * ((a.kind == kConvC) ? 16 : C::kChainNpad) * 2;
+  const bool has_chain = !(a.kind == kConvC && !a.last);
+  const char* wbase = static_cast<const char*>(a.main.w);
+  if (a.first) {
+    // cin = 1: thread m builds its K = 16 row (taps, zero padded) in place of the
+    // im2col; weights are [2][F][8].
+    float v[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) v[k] = 0.f;
+    const int nt = num_taps(a.kind);
+    for (int t = 0; t < nt; ++t) {
+      int dr, dc;
+      tap_offset(a.kind, t, dr, dc);
+      int rr = r + dr, cc = c + dc;
+      if (rr >= 0 && rr < H && cc >= 0 && cc < W) v[t] = spin_at(a.spins, a.batch, P, tile * kTile + m, rr * W + cc);
+    }
+    st8(reinterpret_cast<__nv_bfloat16*>(s.a_ptr + m * 16), v);
+    st8(reinterpret_cast<__nv_bfloat16*>(s.a_ptr + 2048 + m * 16), v + 8);
+    fence_proxy_async_smem();
+    if (threadIdx.x == 0) {
+      uint32_t wbytes = 2 * F * 16;
+      mbar_arrive_expect_tx(s.bar_load, wbytes + (has_chain ? chain_bytes : 0));
+      bulk_g2s(s.w_ptr, wbase, wbytes, s.bar_load);
+      if (has_chain) bulk_g2s(s.cw_ptr, a.chain.w, chain_bytes, s.bar_load);
+    }
+    __syncthreads();
+    if (!tc_wait(s.bar_load, st.ph_load, st)) return;
+    if (threadIdx.x == 0) {
+      tc_fence_after();
+      uint64_t ad = umma_sdesc(s.a, 2048, 128);
+      uint64_t bd = umma_sdesc(s.w, F * 16, 128);
+      umma_bf16(st.tmem, ad, bd, idesc, 0u);
+      umma_commit(s.bar_mma);
+    }
+    if (!tc_wait(s.bar_mma, st.ph_mma, st)) return;
+    tc_fence_after();
+  } else {
+    int taps[9];
+    int pix[9];
+    int nvalid = 0;
+    const int nt = num_taps(a.kind);
+    for (int t = 0; t < nt; ++t) {
+      int dr, dc;
+      tap_offset(a.kind, t, dr, dc);
+      int rr = r + dr, cc = c + dc;
+      if (rr >= 0 && rr < H && cc >= 0 && cc < W) {
+        taps[nvalid] = t;
+        pix[nvalid] = rr * W + cc;
+        ++nvalid;
+      }
+    }
+    const uint32_t wslice = F * F * 2;  // K-range of one tap: F/8 groups x F rows x 16 B
+    for (int g0 = 0; g0 < nvalid; g0 += C::kTaps) {
+      int ng = nvalid - g0 < C::kTaps ? nvalid - g0 : C::kTaps;
+      if (threadIdx.x == 0) {
+        uint32_t bytes = ng * (C::kTapBytesA + wslice) + ((g0 == 0 && has_chain) ? chain_bytes : 0);
+        mbar_arrive_expect_tx(s.bar_load, bytes);
+        for (int j = 0; j < ng; ++j) {
+          const __nv_bfloat16* src = blk<__nv_bfloat16>(a.in, tile, P, pix[g0 + j], F);
+          bulk_g2s(s.a_ptr + j * C::kTapBytesA, src, C::kTapBytesA, s.bar_load);
+          bulk_g2s(s.w_ptr + j * wslice, wbase + (int64_t)taps[g0 + j] * wslice, wslice, s.bar_load);
+        }
+        if (g0 == 0 && has_chain) bulk_g2s(s.cw_ptr, a.chain.w, chain_bytes, s.bar_load);
+      }
+      if (!tc_wait(s.bar_load, st.ph_load, st)) return;
+      if (threadIdx.x == 0) {
+        tc_fence_after();
+        for (int j = 0; j < ng; ++j) {
+#pragma unroll
+          for (int ks = 0; ks < F / 16; ++ks) {
+            uint64_t ad = umma_sdesc(s.a + j * C::kTapBytesA + ks * 2 * 2048, 2048, 128);
+            uint64_t bd = umma_sdesc(s.w + j * wslice + ks * 2 * F * 16, F * 16, 128);
+            umma_bf16(st.tmem, ad, bd, idesc, (g0 + j + ks) > 0 ? 1u : 0u);
+          }
+        }
+        umma_commit(s.bar_mma);
+      }
+      if (!tc_wait(s.bar_mma, st.ph_mma, st)) return;
+      tc_fence_after();
+    }
+  }
+  tc_read<F>(st, 0, acc);
+}
+
+// out[0..NCPAD) = in[0..KC) x Wchain on tensor cores (weights already in smem).
+template <int KC, int NCPAD>
+__device__ void tc_chain(TcSmem& s, TcState& st, int m, const float* in, float* out) {
+  __nv_bfloat16* ca = reinterpret_cast<__nv_bfloat16*>(s.ca_ptr);
+#pragma unroll
+  for (int g = 0; g < KC / 8; ++g) st8(ca + ((int64_t)g * kTile + m) * 8, in + 8 * g);
+  fence_proxy_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    tc_fence_after();
+    const uint32_t idesc = umma_idesc_bf16(128, NCPAD);
+#pragma unroll
+    for (int ks = 0; ks < KC / 16; ++ks) {
+      uint64_t ad = umma_sdesc(s.ca + ks * 2 * 2048, 2048, 128);
+      uint64_t bd = umma_sdesc(s.cw + ks * 2 * NCPAD * 16, NCPAD * 16, 128);
+      umma_bf16(st.tmem + kChainCol, ad, bd, idesc, ks > 0 ? 1u : 0u);
+    }
+    umma_commit(s.bar_mma);
+  }
+  if (!tc_wait(s.bar_mma, st.ph_mma, st)) return;
+  tc_fence_after();
+  tc_read<NCPAD>(st, kChainCol, out);
+}
+
+// End of one op on the tensor-core engine: TMEM reads are done before the next
+// MMA, and this op's global stores (generic proxy) are visible to the bulk
+// copies (async proxy) that later ops of the same kernel issue.
+__device__ __forceinline__ void tc_op_end() {
+  asm volatile("fence.proxy.async;" ::: "memory");
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+}
+
+// ============================================================== one op (shared epilogue)
+// Result of the head at one pixel: normalised (Re0, Re1, Im0, Im1).
+struct HeadOut {
+  float re0, re1, im0, im1;
+};
+
+__device__ __forceinline__ HeadOut normalise_head(const float* l) {
+  // abstract_machine.py:56-57, autoregressive.py:7-15 (norm_type 2)
+  float a = 2.f * l[0], b = 2.f * l[1];
+  float mx = fmaxf(a, b);
+  float lse = 0.5f * (mx + logf(expf(a - mx) + expf(b - mx)));
+  return HeadOut{l[0] - lse, l[1] - lse, l[2], l[3]};
+}
+
+template <int F, bool TC>
+struct Engine;
+
+template <int F>
+struct Engine<F, false> {
+  TcSmem* s;
+  TcState* st;
+  __device__ void main(const OpArgs& a, int64_t tile, int m, int r, int c, int H, int W, int P, float* acc) {
+    simt_main<F>(a, tile, m, r, c, H, W, P, acc);
+  }
+  template <int KC, int NC, int NCPAD>
+  __device__ void chain(const OpArgs& a, int m, const float* in, float* out) {
+    simt_chain<KC, NC>(a.chain, in, out);
+  }
+  __device__ void end() {}
+  __device__ bool aborted() const { return false; }
+};
+
+template <int F>
+struct Engine<F, true> {
+  TcSmem* s;
+  TcState* st;
+  __device__ void main(const OpArgs& a, int64_t tile, int m, int r, int c, int H, int W, int P, float* acc) {
+    tc_main<F>(a, *s, *st, tile, m, r, c, H, W, P, acc);
+  }
+  template <int KC, int NC, int NCPAD>
+  __device__ void chain(const OpArgs& a, int m, const float* in, float* out) {
+    tc_chain<KC, NCPAD>(*s, *st, m, in, out);
+  }
+  __device__ void end() { tc_op_end(); }
+  __device__ bool aborted() const { return st->abort; }
+};
+
+// Runs one op at pixel (r, c) of `tile`. For the final C op returns the head
+// output in *head (valid for every thread).
+template <int F, bool TC, typename T>
+__device__ void run_op(const OpArgs& a, Engine<F, TC>& eng, int64_t tile, int r, int c, int H, int W, int P,
+                       HeadOut* head) {
+  const int m = threadIdx.x;
+  float acc[F];
+  eng.main(a, tile, m, r, c, H, W, P, acc);
+  if (eng.aborted()) return;
+  const float* bm = a.main.b;
+  const float* bc = a.chain.b;
+  const int pix = r * W + c;
+  constexpr int F2 = F / 2;
+  constexpr int NC2 = F2 < 16 ? 16 : F2;
+  if (a.kind == kConvV) {
+#pragma unroll
+    for (int n = 0; n < F; ++n) acc[n] += __ldg(bm + n);
+    if (a.stream_out) {
+      float o[F];
+      if (a.res) {
+        load_row(blk<T>(a.res, tile, P, pix, F), m, 0, F, o);
+#pragma unroll
+        for (int n = 0; n < F; ++n) o[n] = fmaxf(o[n] + acc[n], 0.f);
+      } else {
+#pragma unroll
+        for (int n = 0; n < F; ++n) o[n] = fmaxf(acc[n], 0.f);
+      }
+      store_row(blk<T>(a.stream_out, tile, P, pix, F), m, 0, F, o);
+    }
+#pragma unroll
+    for (int n = 0; n < F; ++n) acc[n] = fmaxf(acc[n], 0.f);
+    if (a.aux_out) store_row(blk<T>(a.aux_out, tile, P, pix, F), m, 0, F, acc);
+    float u[NC2];
+    eng.template chain<F, F2, NC2>(a, m, acc, u);
+    if (eng.aborted()) return;
+#pragma unroll
+    for (int n = 0; n < F2; ++n) u[n] = fmaxf(u[n] + __ldg(bc + n), 0.f);
+    if (r + 1 < H) store_row(blk<T>(a.cat, tile, P, pix + W, F), m, F2, F2, u);
+    if (r == 0) {
+#pragma unroll
+      for (int n = 0; n < F2; ++n) u[n] = fmaxf(__ldg(bc + n), 0.f);
+      store_row(blk<T>(a.cat, tile, P, c, F), m, F2, F2, u);
+    }
+  } else if (a.kind == kConvH) {
+#pragma unroll
+    for (int n = 0; n < F; ++n) acc[n] = fmaxf(acc[n] + __ldg(bm + n), 0.f);
+    if (a.aux_out) store_row(blk<T>(a.aux_out, tile, P, pix, F), m, 0, F, acc);
+    float z[NC2];
+    eng.template chain<F, F2, NC2>(a, m, acc, z);
+    if (eng.aborted()) return;
+#pragma unroll
+    for (int n = 0; n < F2; ++n) z[n] = fmaxf(z[n] + __ldg(bc + n), 0.f);
+    const int sh = a.last ? 1 : 0;
+    if (c + sh < W) store_row(blk<T>(a.cat, tile, P, pix + sh, F), m, 0, F2, z);
+    if (sh && c == 0) {
+#pragma unroll
+      for (int n = 0; n < F2; ++n) z[n] = fmaxf(__ldg(bc + n), 0.f);
+      store_row(blk<T>(a.cat, tile, P, pix, F), m, 0, F2, z);
+    }
+  } else {
+#pragma unroll
+    for (int n = 0; n < F; ++n) acc[n] += __ldg(bm + n);
+    if (!a.last) {
+      float o[F];
+      if (a.res) {
+        load_row(blk<T>(a.res, tile, P, pix, F), m, 0, F, o);
+#pragma unroll
+        for (int n = 0; n < F; ++n) o[n] = fmaxf(o[n] + acc[n], 0.f);
+      } else {
+#pragma unroll
+        for (int n = 0; n < F; ++n) o[n] = fmaxf(acc[n], 0.f);
+      }
+      store_row(blk<T>(a.stream_out, tile, P, pix, F), m, 0, F, o);
+    } else {
+#pragma unroll
+      for (int n = 0; n < F; ++n) acc[n] = fmaxf(acc[n], 0.f);
+      if (a.stream_out) store_row(blk<T>(a.stream_out, tile, P, pix, F), m, 0, F, acc);
+      float l[16];
+      eng.template chain<F, 4, 16>(a, m, acc, l);
+      if (eng.aborted()) return;
+#pragma unroll
+      for (int n = 0; n < 4; ++n) l[n] += __ldg(bc + n);
+      *head = normalise_head(l);
+    }
+  }
+  eng.end();
+}
+
+// ============================================================== forward kernel
+// Grid: one CTA per (tile, row); the CTA walks the row's pixels.
+template <int F, bool TC>
+__global__ void __launch_bounds__(128) op_row_kernel(const __grid_constant__ OpArgs a, int H, int W, int* err) {
+  using T = typename std::conditional<TC, __nv_bfloat16, float>::type;
+  extern __shared__ __align__(1024) uint8_t smem[];
+  const int P = H * W;
+  const int64_t tile = blockIdx.x / H;
+  const int r = blockIdx.x % H;
+  TcSmem s;
+  TcState st;
+  if (TC) {
+    tc_carve<F>(smem, s);
+    tc_setup(s, st, err);
+  }
+  Engine<F, TC> eng{&s, &st};
+  const int m = threadIdx.x;
+  const int64_t sample = tile * kTile + m;
+  Kahan kre, kim;
+  for (int c = 0; c < W; ++c) {
+    HeadOut h;
+    run_op<F, TC, T>(a, eng, tile, r, c, H, W, P, &h);
+    if (eng.aborted()) break;
+    if (a.kind == kConvC && a.last) {
+      int pix = r * W + c;
+      float s0 = spin_at(a.spins, a.batch, P, sample, pix);
+      bool up = s0 > 0.f;
+      kre.add(up ? h.re0 : h.re1);
+      kim.add(up ? h.im0 : h.im1);
+      if (a.cond && sample < a.batch) {
+        reinterpret_cast<float4*>(a.cond)[sample * P + pix] = make_float4(h.re0, h.re1, h.im0, h.im1);
+      }
+    }
+  }
+  if (a.kind == kConvC && a.last && !eng.aborted()) {
+    a.row_partial[((int64_t)tile * H + r) * kTile + m] = make_float2(kre.s - kre.c, kim.s - kim.c);
+  }
+  if (TC) tc_teardown(st);
+}
+
+// log psi = compensated sum over rows of the row partials (same order in the
+// forward and in the sampler, so both give bitwise the same value).
+__global__ void row_reduce_kernel(const float2* __restrict__ part, int64_t batch, int H, float2* __restrict__ out) {
+  int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= batch) return;
+  int64_t tile = b / kTile;
+  int m = (int)(b % kTile);
+  Kahan re, im;
+  for (int r = 0; r < H; ++r) {
+    float2 p = part[((int64_t)tile * H + r) * kTile + m];
+    re.add(p.x);
+    im.add(p.y);
+  }
+  out[b] = make_float2(re.s - re.c, im.s - im.c);
+}
+
+// ============================================================== op list
+static ConvW convw(const NetLayout& L, const void* packed, int idx) {
+  const ConvDesc& c = L.conv[idx];
+  ConvW w;
+  w.w = static_cast<const char*>(packed) + c.w_off;
+  w.b = reinterpret_cast<const float*>(static_cast<const char*>(packed) + c.b_off);
+  w.K = c.K;
+  w.Npad = c.Npad;
+  return w;
+}
+
+// The three ops of causal conv i with the given tensors.
+static void make_ops(const NetLayout& L, const void* packed, int i, const int8_t* spins, int64_t batch,
+                     const void* vin, const void* hin, const void* vres, const void* hres, void* vout, void* hout,
+                     void* cat, void* t_aux, void* rv_aux, OpArgs ops[3]) {
+  const bool first = i == 0, last = i == L.n_cc - 1;
+  for (int k = 0; k < 3; ++k) {
+    memset(&ops[k], 0, sizeof(OpArgs));
+    ops[k].first = first;
+    ops[k].last = last;
+    ops[k].cin = first ? 1 : L.F;
+    ops[k].spins = spins;
+    ops[k].batch = batch;
+    ops[k].cat = cat;
+  }
+  OpArgs& v = ops[0];
+  v.kind = kConvV;
+  v.in = vin;
+  v.main = convw(L, packed, conv_index(i, kConvV));
+  v.chain = convw(L, packed, conv_index(i, kConvY));
+  v.res = vres;
+  v.stream_out = last ? nullptr : vout;
+  v.aux_out = rv_aux;
+  OpArgs& h = ops[1];
+  h.kind = kConvH;
+  h.in = hin;
+  h.main = convw(L, packed, conv_index(i, kConvH));
+  h.chain = convw(L, packed, conv_index(i, kConvX));
+  h.aux_out = t_aux;
+  OpArgs& c = ops[2];
+  c.kind = kConvC;
+  c.first = 0;  // the combine conv always reads the F-channel concat
+  c.cin = L.F;
+  c.in = cat;
+  c.main = convw(L, packed, conv_index(i, kConvC));
+  if (last) c.chain = convw(L, packed, L.n_convs - 1);
+  c.res = hres;
+  c.stream_out = hout;
+}
+
+// Input/output tensors of causal conv i in the two workspace modes.
+struct CCTensors {
+  const void *vin, *hin, *vres, *hres;
+  void *vout, *hout, *cat, *t, *rv;
+};
+
+static CCTensors cc_tensors(const NetLayout& L, const Tensors& T, int mode, int i) {
+  CCTensors x;
+  memset(&x, 0, sizeof(x));
+  const bool last = i == L.n_cc - 1;
+  // residual: the second conv of block b (i = 2b+2) adds the block input S_{2b}
+  const bool second = (i >= 2) && (i % 2 == 0) && !last;
+  if (mode == FK_AR2D_SAVE) {
+    x.vin = i == 0 ? nullptr : T.v[i - 1];
+    x.hin = i == 0 ? nullptr : T.h[i - 1];
+    x.vres = second ? T.v[i - 2] : nullptr;
+    x.hres = second ? T.h[i - 2] : nullptr;
+    x.vout = T.v[i];
+    x.hout = T.h[i];
+    x.cat = T.cat[i];
+    x.t = T.t[i];
+    x.rv = T.rv[i];
+  } else {
+    // ping-pong: S_i lives in slot (i % 2) except that block outputs return to
+    // the block input's slot: S_{2b+2} overwrites S_{2b} in place (residual read
+    // and write happen at the same pixel by the same thread).
+    auto slot = [&](int j) { return (j == 0) ? 0 : ((j % 2 == 1) ? 1 : 0); };
+    x.vin = i == 0 ? nullptr : T.v[slot(i - 1)];
+    x.hin = i == 0 ? nullptr : T.h[slot(i - 1)];
+    x.vres = second ? T.v[slot(i - 2)] : nullptr;
+    x.hres = second ? T.h[slot(i - 2)] : nullptr;
+    x.vout = T.v[slot(i)];
+    x.hout = last ? nullptr : T.h[slot(i)];
+    x.cat = T.cat[0];
+  }
+  return x;
+}
+
+template <int F, bool TC>
+static int launch_op(const OpArgs& a, int64_t tiles, int H, int W, int* err, cudaStream_t s) {
+  size_t smem = TC ? (size_t)TcCfg<F>::kSmem : 0;
+  if (TC) {
+    static bool attr_set = false;
+    if (!attr_set) {
+      FK_CUDA(cudaFuncSetAttribute(op_row_kernel<F, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)TcCfg<F>::kSmem));
+      attr_set = true;
+    }
+  }
+  op_row_kernel<F, TC><<<(unsigned)(tiles * H), 128, smem, s>>>(a, H, W, err);
+  return check_cuda(launched(), "op_row_kernel");
+}
+
+template <int F, bool TC>
+static int forward_impl(const NetLayout& L, const void* packed, const int8_t* spins, int64_t batch,
+                        float* log_psi, float* cond, const Tensors& T, int mode, cudaStream_t s) {
+  int64_t tiles = (batch + kTile - 1) / kTile;
+  int* err = device_error_word();
+  for (int i = 0; i < L.n_cc; ++i) {
+    CCTensors x = cc_tensors(L, T, mode, i);
+    OpArgs ops[3];
+    make_ops(L, packed, i, spins, batch, x.vin, x.hin, x.vres, x.hres, x.vout, x.hout, x.cat, x.t, x.rv, ops);
+    if (i == L.n_cc - 1) {
+      ops[2].row_partial = T.row_partial;
+      ops[2].cond = cond;
+    }
+    for (int k = 0; k < 3; ++k) {
+      int st = launch_op<F, TC>(ops[k], tiles, L.H, L.W, err, s);
+      if (st != FK_OK) return st;
+    }
+  }
+  row_reduce_kernel<<<(unsigned)((batch + 255) / 256), 256, 0, s>>>(T.row_partial, batch, L.H,
+                                                                    reinterpret_cast<float2*>(log_psi));
+  return check_cuda(launched(), "row_reduce_kernel");
+}
+
+// ============================================================== sampler
+// One persistent CTA per tile walks the sites in raster order:
+//   start : Cat_i[0, :][F/2:F] = relu(b_y,i) for all i; Cat_last[:, 0][0:F/2] = relu(b_x,last)
+//   site (r, c):  head at (r, c) -> draw s(r, c)
+//                 for i < last: H op_i (r, c), C op_i (r, c);  H op_last (r, c)
+//   end of row r: for every i: V op_i over (r, 0..W-1)
+// Every (layer, pixel) is evaluated once, after all the sites it depends on.
+struct SampleArgs {
+  OpArgs op[40][3];
+  int n_cc;
+  int64_t batch;
+  uint32_t seed_lo, seed_hi, off_lo, off_hi;
+  int8_t* spins;
+  float2* row_partial;
+};
+
+template <int F, bool TC>
+__global__ void __launch_bounds__(128) sample_kernel(const __grid_constant__ SampleArgs a, int H, int W, int* err) {
+  using T = typename std::conditional<TC, __nv_bfloat16, float>::type;
+  extern __shared__ __align__(1024) uint8_t smem[];
+  const int P = H * W;
+  const int64_t tile = blockIdx.x;
+  const int m = threadIdx.x;
+  const int64_t sample = tile * kTile + m;
+  const int last = a.n_cc - 1;
+  constexpr int F2 = F / 2;
+  // boundary rows/columns of the shifted tensors
+  for (int i = 0; i < a.n_cc; ++i) {
+    const OpArgs& v = a.op[i][0];
+    float u[F2];
+#pragma unroll
+    for (int n = 0; n < F2; ++n) u[n] = fmaxf(__ldg(v.chain.b + n), 0.f);
+    for (int c = 0; c < W; ++c) store_row(blk<T>(v.cat, tile, P, c, F), m, F2, F2, u);
+  }
+  {
+    const OpArgs& h = a.op[last][1];
+    float z[F2];
+#pragma unroll
+    for (int n = 0; n < F2; ++n) z[n] = fmaxf(__ldg(h.chain.b + n), 0.f);
+    for (int r = 0; r < H; ++r) store_row(blk<T>(h.cat, tile, P, r * W, F), m, 0, F2, z);
+  }
+  if (TC) asm volatile("fence.proxy.async;" ::: "memory");
+  __syncthreads();
+  TcSmem s;
+  TcState st;
+  if (TC) {
+    tc_carve<F>(smem, s);
+    tc_setup(s, st, err);
+  }
+  Engine<F, TC> eng{&s, &st};
+  for (int r = 0; r < H && !eng.aborted(); ++r) {
+    Kahan kre, kim;
+    for (int c = 0; c < W; ++c) {
+      const int pix = r * W + c;
+      HeadOut h;
+      run_op<F, TC, T>(a.op[last][2], eng, tile, r, c, H, W, P, &h);
+      if (eng.aborted()) break;
+      // deepar/samplers/autoregressive.py:41-43 (+1 iff p(+1) > U), drawn with
+      // Philox counter (sample, site, offset).
+      U4 x = philox4x32(U4{(uint32_t)sample, (uint32_t)pix, a.off_lo, a.off_hi}, a.seed_lo, a.seed_hi);
+      float u = philox_uniform(x.x);
+      bool up = expf(2.f * h.re0) > u;
+      kre.add(up ? h.re0 : h.re1);
+      kim.add(up ? h.im0 : h.im1);
+      if (sample < a.batch) a.spins[sample * P + pix] = up ? (int8_t)1 : (int8_t)-1;
+      __syncthreads();
+      for (int i = 0; i < last && !eng.aborted(); ++i) {
+        run_op<F, TC, T>(a.op[i][1], eng, tile, r, c, H, W, P, &h);
+        __syncthreads();
+        run_op<F, TC, T>(a.op[i][2], eng, tile, r, c, H, W, P, &h);
+        __syncthreads();
+      }
+      if (eng.aborted()) break;
+      run_op<F, TC, T>(a.op[last][1], eng, tile, r, c, H, W, P, &h);
+      __syncthreads();
+    }
+    if (eng.aborted()) break;
+    a.row_partial[((int64_t)tile * H + r) * kTile + m] = make_float2(kre.s - kre.c, kim.s - kim.c);
+    for (int i = 0; i < a.n_cc && !eng.aborted(); ++i) {
+      for (int c = 0; c < W; ++c) {
+        HeadOut h;
+        run_op<F, TC, T>(a.op[i][0], eng, tile, r, c, H, W, P, &h);
+        __syncthreads();
+      }
+    }
+  }
+  if (TC) tc_teardown(st);
+}
+
+template <int F, bool TC>
+static int sample_impl(const NetLayout& L, const void* packed, int64_t batch, uint64_t seed, uint64_t offset,
+                       int8_t* spins, float* log_psi, const Tensors& T, cudaStream_t s) {
+  int64_t tiles = (batch + kTile - 1) / kTile;
+  SampleArgs* a = new SampleArgs;
+  memset(a, 0, sizeof(SampleArgs));
+  a->n_cc = L.n_cc;
+  a->batch = batch;
+  a->seed_lo = (uint32_t)seed;
+  a->seed_hi = (uint32_t)(seed >> 32);
+  a->off_lo = (uint32_t)offset;
+  a->off_hi = (uint32_t)(offset >> 32);
+  a->spins = spins;
+  a->row_partial = T.row_partial;
+  for (int i = 0; i < L.n_cc; ++i) {
+    CCTensors x = cc_tensors(L, T, FK_AR2D_SAVE, i);
+    make_ops(L, packed, i, spins, batch, x.vin, x.hin, x.vres, x.hres, x.vout, x.hout, x.cat, x.t, x.rv, a->op[i]);
+  }
+  size_t smem = TC ? (size_t)TcCfg<F>::kSmem : 0;
+  int st = FK_OK;
+  if (TC) {
+    st = check_cuda(cudaFuncSetAttribute(sample_kernel<F, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)TcCfg<F>::kSmem),
+                    "cudaFuncSetAttribute");
+  }
+  if (st == FK_OK) {
+    sample_kernel<F, TC><<<(unsigned)tiles, 128, smem, s>>>(*a, L.H, L.W, device_error_word());
+    st = check_cuda(launched(), "sample_kernel");
+  }
+  delete a;
+  if (st != FK_OK) return st;
+  row_reduce_kernel<<<(unsigned)((batch + 255) / 256), 256, 0, s>>>(T.row_partial, batch, L.H,
+                                                                    reinterpret_cast<float2*>(log_psi));
+  return check_cuda(launched(), "row_reduce_kernel");
+}
+
+}  // namespace fk
+
+using namespace fk;
+
+extern "C" {
+
+int64_t fk_ar2d_num_params(const fk_ar2d_desc* desc) {
+  NetLayout L;
+  if (build_layout(desc, &L) != FK_OK) return -1;
+  return L.num_params;
+}
+
+int64_t fk_ar2d_packed_bytes(const fk_ar2d_desc* desc) {
+  NetLayout L;
+  if (build_layout(desc, &L) != FK_OK) return -1;
+  return L.packed_bytes;
+}
+
+int fk_ar2d_pack(const fk_ar2d_desc* desc, const float* params, void* packed, void* stream) {
+  NetLayout L;
+  int st = build_layout(desc, &L);
+  if (st != FK_OK) return st;
+  FK_CHECK_ARG(params && packed, "fk_ar2d_pack: NULL buffer");
+  PackArgs* a = new PackArgs;
+  a->params = params;
+  a->packed = static_cast<char*>(packed);
+  a->n_convs = L.n_convs;
+  a->bf16 = L.precision == FK_PRECISION_BF16;
+  memcpy(a->conv, L.conv, sizeof(L.conv));
+  pack_kernel<<<L.n_convs, 256, 0, static_cast<cudaStream_t>(stream)>>>(*a);
+  delete a;
+  FK_CUDA(launched());
+  return FK_OK;
+}
+
+int64_t fk_ar2d_workspace_bytes(const fk_ar2d_desc* desc, int64_t batch, int32_t mode) {
+  NetLayout L;
+  if (build_layout(desc, &L) != FK_OK || batch < 0) return -1;
+  return workspace_layout(L, batch, mode, nullptr, nullptr);
+}
+
+int fk_ar2d_forward(const fk_ar2d_desc* desc, const void* packed, const int8_t* spins, int64_t batch,
+                    float* log_psi, float* cond, void* workspace, int64_t workspace_bytes, int32_t mode,
+                    void* stream) {
+  NetLayout L;
+  int st = build_layout(desc, &L);
+  if (st != FK_OK) return st;
+  FK_CHECK_ARG(packed && spins && log_psi && batch >= 0, "fk_ar2d_forward: NULL buffer");
+  FK_CHECK_ARG(mode == FK_AR2D_INFER || mode == FK_AR2D_SAVE, "fk_ar2d_forward: bad mode %d", mode);
+  if (batch == 0) return FK_OK;
+  Tensors T;
+  int64_t need = workspace_layout(L, batch, mode, static_cast<char*>(workspace), &T);
+  FK_CHECK_ARG(workspace && workspace_bytes >= need, "fk_ar2d_forward: workspace %lld < %lld bytes",
+               (long long)workspace_bytes, (long long)need);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const bool tc = L.precision == FK_PRECISION_BF16;
+  switch (L.F) {
+    case 16: return tc ? forward_impl<16, true>(L, packed, spins, batch, log_psi, cond, T, mode, s)
+                       : forward_impl<16, false>(L, packed, spins, batch, log_psi, cond, T, mode, s);
+    case 32: return tc ? forward_impl<32, true>(L, packed, spins, batch, log_psi, cond, T, mode, s)
+                       : forward_impl<32, false>(L, packed, spins, batch, log_psi, cond, T, mode, s);
+    default: return tc ? forward_impl<64, true>(L, packed, spins, batch, log_psi, cond, T, mode, s)
+                       : forward_impl<64, false>(L, packed, spins, batch, log_psi, cond, T, mode, s);
+  }
+}
+
+int fk_ar2d_sample(const fk_ar2d_desc* desc, const void* packed, int64_t batch, uint64_t seed, uint64_t offset,
+                   int8_t* spins, float* log_psi, void* workspace, int64_t workspace_bytes, void* stream) {
+  NetLayout L;
+  int st = build_layout(desc, &L);
+  if (st != FK_OK) return st;
+  FK_CHECK_ARG(packed && spins && log_psi && batch >= 0, "fk_ar2d_sample: NULL buffer");
+  if (batch == 0) return FK_OK;
+  Tensors T;
+  int64_t need = workspace_layout(L, batch, FK_AR2D_SAVE, static_cast<char*>(workspace), &T);
+  FK_CHECK_ARG(workspace && workspace_bytes >= need, "fk_ar2d_sample: workspace %lld < %lld bytes",
+               (long long)workspace_bytes, (long long)need);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const bool tc = L.precision == FK_PRECISION_BF16;
+  switch (L.F) {
+    case 16: return tc ? sample_impl<16, true>(L, packed, batch, seed, offset, spins, log_psi, T, s)
+                       : sample_impl<16, false>(L, packed, batch, seed, offset, spins, log_psi, T, s);
+    case 32: return tc ? sample_impl<32, true>(L, packed, batch, seed, offset, spins, log_psi, T, s)
+                       : sample_impl<32, false>(L, packed, batch, seed, offset, spins, log_psi, T, s);
+    default: return tc ? sample_impl<64, true>(L, packed, batch, seed, offset, spins, log_psi, T, s)
+                       : sample_impl<64, false>(L, packed, batch, seed, offset, spins, log_psi, T, s);
+  }
+}
+
+}  // extern "C"

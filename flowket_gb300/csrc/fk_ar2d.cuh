@@ -1,0 +1,142 @@
+// ConvNetAutoregressive2D on GB300: shared declarations of the forward,
+// sampling and adjoint kernels.
+//
+// Activation layout ("sample-major blocked"): a tensor with C channels is
+// stored per tile of 128 samples and per lattice pixel as a block
+// [C/8][128][8] of elements, blocks ordered (tile, pixel). One block is
+// exactly the no-swizzle K-major operand layout of a tcgen05 MMA with
+// M = 128 samples and K = C channels (rows 16 B apart, K-groups 2 KB apart),
+// so a convolution tap is one contiguous bulk copy and the implicit GEMM needs
+// no im2col: a 3x3 causal conv at pixel (r, c) is the sum over the in-bounds
+// taps of [128 x C] x [C x F] products. Out-of-lattice taps are skipped (the
+// reference's ZeroPadding2D).
+#pragma once
+
+#include "fk_common.cuh"
+
+namespace fk {
+
+constexpr int kTile = 128;  // samples per tile = MMA M
+
+enum ConvKind { kConvV = 0, kConvH = 1, kConvX = 2, kConvY = 3, kConvC = 4 };
+
+// One conv of the network (kernel, bias, optional weight-norm gain).
+struct ConvDesc {
+  int64_t p_kernel, p_bias, p_g;  // float offsets into the flat parameter vector (p_g < 0: none)
+  int64_t w_off, b_off;           // byte offsets into the packed buffer (weights, fp32 bias)
+  int64_t w32_off;                // byte offset of the fp32 [K][cout] effective kernel (== w_off on fp32)
+  int kh, kw, cin, cout;
+  int K, Kpad, Npad;              // GEMM K (taps*cin), padded K / N for the bf16 operand
+};
+
+constexpr int kMaxConvs = 5 * 38 + 1;
+
+struct NetLayout {
+  int H, W, P, depth, F, wn, precision, n_cc;
+  int n_convs;
+  int64_t num_params;
+  int64_t packed_bytes;
+  ConvDesc conv[kMaxConvs];
+};
+
+int build_layout(const fk_ar2d_desc* d, NetLayout* L);
+
+inline int conv_index(int cc, int kind) { return cc * 5 + kind; }
+
+// Packed weights as seen by one op.
+struct ConvW {
+  const void* w;    // fp32 [K][N] or bf16 [Kpad/8][Npad][8]
+  const float* b;   // bias [N]
+  int K, Npad;
+};
+
+struct OpArgs {
+  int kind;          // kConvV, kConvH or kConvC
+  int first;         // input is the spin lattice (cin = 1)
+  int last;          // op of the final causal conv (H: right shift; C: output head)
+  int cin;
+  const int8_t* spins;  // [batch][P] +-1 (first-layer ops, head spin lookup)
+  const void* in;       // input tensor, blocked, cin channels
+  ConvW main, chain;    // main conv; chained 1x1 (y for V, x for H, head for the last C)
+  const void* res;      // residual for the stream output (NULL: none)
+  void* stream_out;     // V/H stream output (last C: relu(Hp) when saving)
+  void* aux_out;        // V: relu(Vp) when saving; H: relu(conv_h) when saving
+  void* cat;            // concat tensor (F channels): H writes [0,F/2), V writes [F/2,F)
+  float2* row_partial;  // last C: [tiles][H][128] log psi partial per row
+  float* cond;          // last C: [batch][P][4] normalised conditionals (optional)
+  int64_t batch;
+};
+
+// Workspace tensors of one forward.
+struct Tensors {
+  // FK_AR2D_INFER: v[0..1], h[0..1], cat[0]; FK_AR2D_SAVE: one set per causal conv.
+  void* v[40];
+  void* h[40];
+  void* cat[40];
+  void* t[40];
+  void* rv[40];
+  float2* row_partial;
+  int64_t bytes;
+};
+
+// ---------------------------------------------------------------- device helpers
+template <typename T>
+__device__ __forceinline__ T* blk(const void* base, int64_t tile, int P, int pix, int C) {
+  return reinterpret_cast<T*>(const_cast<void*>(base)) + ((tile * P + pix) * (int64_t)C) * kTile;
+}
+
+__device__ __forceinline__ void ld8(const float* p, float* v) {
+  float4 a = reinterpret_cast<const float4*>(p)[0];
+  float4 b = reinterpret_cast<const float4*>(p)[1];
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+  v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+__device__ __forceinline__ void ld8(const __nv_bfloat16* p, float* v) {
+  unpack_bf16x8(*reinterpret_cast<const uint4*>(p), v);
+}
+__device__ __forceinline__ void st8(float* p, const float* v) {
+  reinterpret_cast<float4*>(p)[0] = make_float4(v[0], v[1], v[2], v[3]);
+  reinterpret_cast<float4*>(p)[1] = make_float4(v[4], v[5], v[6], v[7]);
+}
+__device__ __forceinline__ void st8(__nv_bfloat16* p, const float* v) {
+  uint4 u;
+  u.x = pack_bf16x2(v[0], v[1]);
+  u.y = pack_bf16x2(v[2], v[3]);
+  u.z = pack_bf16x2(v[4], v[5]);
+  u.w = pack_bf16x2(v[6], v[7]);
+  *reinterpret_cast<uint4*>(p) = u;
+}
+
+// Store `n` channels (multiple of 8) of thread row m into a block at channel offset c0.
+template <typename T>
+__device__ __forceinline__ void store_row(T* block, int m, int c0, int n, const float* v) {
+  for (int g = 0; g < n / 8; ++g) st8(block + ((int64_t)((c0 / 8) + g) * kTile + m) * 8, v + 8 * g);
+}
+template <typename T>
+__device__ __forceinline__ void load_row(const T* block, int m, int c0, int n, float* v) {
+  for (int g = 0; g < n / 8; ++g) ld8(block + ((int64_t)((c0 / 8) + g) * kTile + m) * 8, v + 8 * g);
+}
+
+// Tap offsets of the three ops (kernel element t = i*kw + j).
+__device__ __forceinline__ void tap_offset(int kind, int t, int& dr, int& dc) {
+  if (kind == kConvV) {
+    dr = t / 3 - 2;
+    dc = t % 3 - 1;
+  } else if (kind == kConvH) {
+    dr = 0;
+    dc = t - 2;
+  } else {
+    dr = t / 3 - 2;
+    dc = t % 3 - 2;
+  }
+}
+__device__ __forceinline__ int num_taps(int kind) { return kind == kConvH ? 3 : 9; }
+
+__device__ __forceinline__ float spin_at(const int8_t* spins, int64_t batch, int P, int64_t sample, int pix) {
+  return sample < batch ? (float)spins[sample * P + pix] : 1.f;
+}
+
+int64_t tensor_bytes(const NetLayout& L, int64_t tiles, int channels);
+int64_t workspace_layout(const NetLayout& L, int64_t batch, int mode, char* base, Tensors* T);
+
+}  // namespace fk

@@ -1,0 +1,669 @@
+// Adjoint of log psi through ConvNetAutoregressive2D (hand-written backward).
+//
+// Seeds w[b] = (w_re, w_im) weight Re and Im log psi of sample b. With
+// log psi = sum_sites (Re_s - lse/2, Im_s) (abstract_machine.py:56-57) the
+// head gradient per site is
+//   dRe_j = w_re (delta_{j,s} - softmax(2 Re)_j),   dIm_j = w_im delta_{j,s}.
+// The gradient then runs through the causal convs in reverse, one kernel
+// family per op (thread = sample, CTA = tile x lattice row, like the forward):
+//   head    : gL, gHp_last = (W_o^T gL) . [relu(Hp) > 0]
+//   C^T     : gCat = sum_taps gHp[q - tap] W_c^T, masked by [Cat > 0];
+//             X half -> gT at (r, c - s) via W_x^T and [T > 0];
+//             Y half -> gVp at (r - 1, c) via W_y^T and [relu(Vp) > 0], plus the
+//             stream gradient of V.
+//   V^T/H^T : gradients of the conv inputs, plus the residual gradient of the
+//             block input, masked by the previous conv's relu.
+// Weight gradients are sum_q X[q + tap] (x) G[q] per tap, either summed over
+// samples (block reduction + atomics) or kept per sample (param-major
+// [num_params][batch], the rows of O_k). Weight normalisation is applied last:
+// dv = e^g/|v| (dW - u (u.dW)), dg = e^g (u.dW) (deepar/layers/wrappers.py:123-134).
+// Activations are read from the forward/sampler workspace (bf16 or fp32);
+// gradients are fp32 throughout.
+#include "fk_ar2d.cuh"
+
+#include <string.h>
+
+namespace fk {
+
+__device__ __forceinline__ void load_g(const float* t, int64_t tile, int P, int pix, int C, int m, int c0, int n,
+                                       float* v) {
+  load_row(blk<float>(t, tile, P, pix, C), m, c0, n, v);
+}
+__device__ __forceinline__ void store_g(float* t, int64_t tile, int P, int pix, int C, int m, int c0, int n,
+                                        const float* v) {
+  store_row(blk<float>(t, tile, P, pix, C), m, c0, n, v);
+}
+
+// acc[ci] += sum_n g[n] W[row0 + ci][n]  (W fp32 [K][N] row-major)
+template <int CI, int N>
+__device__ __forceinline__ void dot_rows(const float* __restrict__ W, int row0, const float* g, float* acc) {
+#pragma unroll 4
+  for (int ci = 0; ci < CI; ++ci) {
+    const float* w = W + (int64_t)(row0 + ci) * N;
+    float s = 0.f;
+#pragma unroll
+    for (int n = 0; n < N; ++n) s += g[n] * __ldg(w + n);
+    acc[ci] += s;
+  }
+}
+
+struct HeadBwdArgs {
+  const void* hlast;     // relu(Hp) of the final conv (act type)
+  const float* wo;       // [F][4]
+  const float* bo;       // [4]
+  const int8_t* spins;
+  const float2* seeds;   // [batch]
+  int64_t batch;
+  float* gL;             // [tiles][P][8ch] fp32 (4 used)
+  float* ghp;            // [tiles][P][F] fp32
+};
+
+template <int F, typename T>
+__global__ void __launch_bounds__(128) head_bwd_kernel(const __grid_constant__ HeadBwdArgs a, int H, int W) {
+  const int P = H * W;
+  const int64_t tile = blockIdx.x / H;
+  const int r = blockIdx.x % H;
+  const int m = threadIdx.x;
+  const int64_t b = tile * kTile + m;
+  float2 w = b < a.batch ? a.seeds[b] : make_float2(0.f, 0.f);
+  for (int c = 0; c < W; ++c) {
+    const int pix = r * W + c;
+    float g[F];
+    load_row(blk<T>(a.hlast, tile, P, pix, F), m, 0, F, g);
+    float l[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) l[j] = __ldg(a.bo + j);
+#pragma unroll 8
+    for (int k = 0; k < F; ++k) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) l[j] += g[k] * __ldg(a.wo + k * 4 + j);
+    }
+    float pi0 = 1.f / (1.f + expf(2.f * (l[1] - l[0])));
+    float pi1 = 1.f - pi0;
+    bool up = spin_at(a.spins, a.batch, P, b, pix) > 0.f;
+    float gl[8] = {w.x * ((up ? 1.f : 0.f) - pi0), w.x * ((up ? 0.f : 1.f) - pi1), up ? w.y : 0.f,
+                   up ? 0.f : w.y, 0.f, 0.f, 0.f, 0.f};
+    store_g(a.gL, tile, P, pix, 8, m, 0, 8, gl);
+    float gh[F];
+#pragma unroll 8
+    for (int k = 0; k < F; ++k) {
+      float s = 0.f;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) s += __ldg(a.wo + k * 4 + j) * gl[j];
+      gh[k] = g[k] > 0.f ? s : 0.f;
+    }
+    store_g(a.ghp, tile, P, pix, F, m, 0, F, gh);
+  }
+}
+
+struct CBwdArgs {
+  const float* ghp;      // gradient of Hp (masked), F
+  const void* cat;       // saved Cat
+  const void* t;         // saved T = relu(conv_h)
+  const void* rv;        // saved relu(Vp)
+  const float* gvpd;     // masked stream gradient of V_{i+1} (NULL on the final conv)
+  const float* wc;       // [9F][F]
+  const float* wx;       // [F][F/2]
+  const float* wy;       // [F][F/2]
+  int shift;             // 1 on the final conv (right shift)
+  float* gcatm;          // out: masked Cat gradient, F
+  float* gt;             // out: gradient of the h-conv pre-activation (masked), F
+  float* gvp;            // out: gradient of Vp (masked), F
+};
+
+template <int F, typename T>
+__global__ void __launch_bounds__(128) c_bwd_kernel(const __grid_constant__ CBwdArgs a, int H, int W) {
+  constexpr int F2 = F / 2;
+  const int P = H * W;
+  const int64_t tile = blockIdx.x / H;
+  const int r = blockIdx.x % H;
+  const int m = threadIdx.x;
+  for (int c = 0; c < W; ++c) {
+    const int pix = r * W + c;
+    float gcat[F];
+#pragma unroll
+    for (int k = 0; k < F; ++k) gcat[k] = 0.f;
+    for (int t = 0; t < 9; ++t) {
+      int rs = r + 2 - t / 3, cs = c + 2 - t % 3;
+      if (rs >= H || cs >= W) continue;
+      float g[F];
+      load_g(a.ghp, tile, P, rs * W + cs, F, m, 0, F, g);
+      dot_rows<F, F>(a.wc, t * F, g, gcat);
+    }
+    float cat[F];
+    load_row(blk<T>(a.cat, tile, P, pix, F), m, 0, F, cat);
+#pragma unroll
+    for (int k = 0; k < F; ++k) gcat[k] = cat[k] > 0.f ? gcat[k] : 0.f;
+    store_g(a.gcatm, tile, P, pix, F, m, 0, F, gcat);
+    // X half -> T at (r, c - s)
+    const int cx = c - a.shift;
+    if (cx >= 0) {
+      float tt[F], gt[F];
+      load_row(blk<T>(a.t, tile, P, r * W + cx, F), m, 0, F, tt);
+#pragma unroll
+      for (int k = 0; k < F; ++k) gt[k] = 0.f;
+      dot_rows<F, F2>(a.wx, 0, gcat, gt);
+#pragma unroll
+      for (int k = 0; k < F; ++k) gt[k] = tt[k] > 0.f ? gt[k] : 0.f;
+      store_g(a.gt, tile, P, r * W + cx, F, m, 0, F, gt);
+    }
+    if (a.shift && c == W - 1) {
+      float z[F];
+#pragma unroll
+      for (int k = 0; k < F; ++k) z[k] = 0.f;
+      store_g(a.gt, tile, P, pix, F, m, 0, F, z);
+    }
+    // Y half -> Vp at (r - 1, c)
+    if (r >= 1) {
+      const int py = pix - W;
+      float rv[F], gv[F];
+      load_row(blk<T>(a.rv, tile, P, py, F), m, 0, F, rv);
+      if (a.gvpd) {
+        load_g(a.gvpd, tile, P, py, F, m, 0, F, gv);
+      } else {
+#pragma unroll
+        for (int k = 0; k < F; ++k) gv[k] = 0.f;
+      }
+      float gr[F];
+#pragma unroll
+      for (int k = 0; k < F; ++k) gr[k] = 0.f;
+      dot_rows<F, F2>(a.wy, 0, gcat + F2, gr);
+#pragma unroll
+      for (int k = 0; k < F; ++k) gv[k] += rv[k] > 0.f ? gr[k] : 0.f;
+      store_g(a.gvp, tile, P, py, F, m, 0, F, gv);
+    }
+    if (r == H - 1) {
+      float gv[F];
+      if (a.gvpd) {
+        load_g(a.gvpd, tile, P, pix, F, m, 0, F, gv);
+      } else {
+#pragma unroll
+        for (int k = 0; k < F; ++k) gv[k] = 0.f;
+      }
+      store_g(a.gvp, tile, P, pix, F, m, 0, F, gv);
+    }
+  }
+}
+
+struct VHBwdArgs {
+  const float* gvp;      // gradient of Vp (masked), F
+  const float* gt;       // gradient of the h-conv pre-activation (masked), F
+  const float* wv;       // [9F][F]
+  const float* wh;       // [3F][F]
+  const float* res_v;    // masked stream gradient of the block's second conv (residual path) or NULL
+  const float* res_h;
+  const void* vprev;     // saved V_{i-1} (relu mask)
+  const void* hprev;     // saved H_{i-1}
+  float* gvpd_prev;      // out: masked stream gradient of V_{i-1}
+  float* ghp_prev;       // out: masked gradient of Hp_{i-1}
+};
+
+template <int F, typename T>
+__global__ void __launch_bounds__(128) vh_bwd_kernel(const __grid_constant__ VHBwdArgs a, int H, int W) {
+  const int P = H * W;
+  const int64_t tile = blockIdx.x / H;
+  const int r = blockIdx.x % H;
+  const int m = threadIdx.x;
+  for (int c = 0; c < W; ++c) {
+    const int pix = r * W + c;
+    float gv[F], gh[F];
+#pragma unroll
+    for (int k = 0; k < F; ++k) {
+      gv[k] = 0.f;
+      gh[k] = 0.f;
+    }
+    for (int t = 0; t < 9; ++t) {  // V taps: (dr, dc) = (t/3 - 2, t%3 - 1)
+      int rs = r + 2 - t / 3, cs = c + 1 - t % 3;
+      if (rs >= H || cs < 0 || cs >= W) continue;
+      float g[F];
+      load_g(a.gvp, tile, P, rs * W + cs, F, m, 0, F, g);
+      dot_rows<F, F>(a.wv, t * F, g, gv);
+    }
+    for (int t = 0; t < 3; ++t) {  // H taps: dc = t - 2
+      int cs = c + 2 - t;
+      if (cs >= W) continue;
+      float g[F];
+      load_g(a.gt, tile, P, r * W + cs, F, m, 0, F, g);
+      dot_rows<F, F>(a.wh, t * F, g, gh);
+    }
+    if (a.res_v) {
+      float x[F];
+      load_g(a.res_v, tile, P, pix, F, m, 0, F, x);
+#pragma unroll
+      for (int k = 0; k < F; ++k) gv[k] += x[k];
+      load_g(a.res_h, tile, P, pix, F, m, 0, F, x);
+#pragma unroll
+      for (int k = 0; k < F; ++k) gh[k] += x[k];
+    }
+    float v[F], h[F];
+    load_row(blk<T>(a.vprev, tile, P, pix, F), m, 0, F, v);
+    load_row(blk<T>(a.hprev, tile, P, pix, F), m, 0, F, h);
+#pragma unroll
+    for (int k = 0; k < F; ++k) {
+      gv[k] = v[k] > 0.f ? gv[k] : 0.f;
+      gh[k] = h[k] > 0.f ? gh[k] : 0.f;
+    }
+    store_g(a.gvpd_prev, tile, P, pix, F, m, 0, F, gv);
+    store_g(a.ghp_prev, tile, P, pix, F, m, 0, F, gh);
+  }
+}
+
+// ---------------------------------------------------------------- weight gradients
+struct WgArgs {
+  int ntaps;
+  int dr[9], dc[9];
+  const void* X;        // activations (act type), cin channels; NULL -> spins
+  const int8_t* spins;
+  int cin;
+  const float* G;       // fp32 blocked, gC channels; uses [g0, g0 + N)
+  int gC, g0, N;
+  float* dW;            // summed raw kernel gradient [ntaps*cin][N]
+  float* dB;            // summed bias gradient [N]
+  float* O;             // per-sample: O[(k_off + k*N + n) * batch + b]
+  int64_t o_kernel, o_bias;
+  int64_t batch;
+  int items;            // work items = ntaps * ceil(cin/8) * ceil(N/8)
+};
+
+constexpr int kItemsPerCta = 4;
+
+template <typename T>
+__global__ void __launch_bounds__(128) wgrad_kernel(const __grid_constant__ WgArgs a, int H, int W) {
+  __shared__ float red[4][64];
+  const int P = H * W;
+  const int64_t tile = blockIdx.x;
+  const int m = threadIdx.x;
+  const int64_t b = tile * kTile + m;
+  const int kchunks = (a.cin + 7) / 8;
+  const int nchunks = (a.N + 7) / 8;
+  for (int it = blockIdx.y * kItemsPerCta; it < a.items && it < (int)(blockIdx.y + 1) * kItemsPerCta; ++it) {
+    const int t = it / (kchunks * nchunks);
+    const int kc = (it / nchunks) % kchunks;
+    const int nc = it % nchunks;
+    const bool with_bias = (t == 0 && kc == 0);
+    float acc[8][8];
+    float gb[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      gb[i] = 0.f;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+    }
+    for (int r = 0; r < H; ++r) {
+      for (int c = 0; c < W; ++c) {
+        float g[8];
+        load_row(blk<float>(a.G, tile, P, r * W + c, a.gC), m, a.g0 + nc * 8, 8, g);
+        if (with_bias) {
+#pragma unroll
+          for (int j = 0; j < 8; ++j) gb[j] += g[j];
+        }
+        int rs = r + a.dr[t], cs = c + a.dc[t];
+        if (rs < 0 || rs >= H || cs < 0 || cs >= W) continue;
+        float x[8];
+        if (a.X) {
+          load_row(blk<T>(a.X, tile, P, rs * W + cs, a.cin), m, kc * 8, 8, x);
+        } else {
+#pragma unroll
+          for (int i = 0; i < 8; ++i) x[i] = 0.f;
+          x[0] = spin_at(a.spins, a.batch, P, b, rs * W + cs);
+        }
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+#pragma unroll
+          for (int j = 0; j < 8; ++j) acc[i][j] += x[i] * g[j];
+        }
+      }
+    }
+    const int kmax = a.cin - kc * 8 < 8 ? a.cin - kc * 8 : 8;
+    const int nmax = a.N - nc * 8 < 8 ? a.N - nc * 8 : 8;
+    if (a.O) {
+      if (b < a.batch) {
+        for (int i = 0; i < kmax; ++i) {
+          int64_t row = (int64_t)(t * a.cin + kc * 8 + i) * a.N + nc * 8;
+          for (int j = 0; j < nmax; ++j) a.O[(a.o_kernel + row + j) * a.batch + b] = acc[i][j];
+        }
+        if (with_bias)
+          for (int j = 0; j < nmax; ++j) a.O[(a.o_bias + nc * 8 + j) * a.batch + b] = gb[j];
+      }
+    } else {
+      // block reduction over the 128 samples, then one atomic per element
+      const int lane = m & 31, warp = m >> 5;
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          float v = acc[i][j];
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+          acc[i][j] = v;
+        }
+      }
+      if (lane == 0) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+          for (int j = 0; j < 8; ++j) red[warp][i * 8 + j] = acc[i][j];
+      }
+      __syncthreads();
+      if (m < 64) {
+        int i = m / 8, j = m % 8;
+        float v = red[0][m] + red[1][m] + red[2][m] + red[3][m];
+        if (i < kmax && j < nmax) atomicAdd(&a.dW[(int64_t)(t * a.cin + kc * 8 + i) * a.N + nc * 8 + j], v);
+      }
+      __syncthreads();
+      if (with_bias) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          float v = gb[j];
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+          gb[j] = v;
+        }
+        if (lane == 0)
+          for (int j = 0; j < 8; ++j) red[warp][j] = gb[j];
+        __syncthreads();
+        if (m < nmax) atomicAdd(&a.dB[nc * 8 + m], red[0][m] + red[1][m] + red[2][m] + red[3][m]);
+        __syncthreads();
+      }
+    }
+  }
+}
+
+// Weight-normalisation chain rule for one conv. Summed: one thread per output
+// channel. Per-sample: one thread per (output channel, sample) on the O rows.
+struct WnArgs {
+  const float* params;
+  int64_t p_kernel, p_g;
+  int K, N;
+  float* grad;     // summed: flat gradient (kernel slot holds dW on entry)
+  float* O;        // per-sample rows (kernel slot holds dW on entry)
+  int64_t batch;
+};
+
+__global__ void wn_kernel(const __grid_constant__ WnArgs a) {
+  int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t cols = a.O ? (int64_t)a.N * a.batch : a.N;
+  if (idx >= cols) return;
+  int n = (int)(idx % a.N);
+  int64_t b = idx / a.N;
+  const float* v = a.params + a.p_kernel;
+  float sq = 0.f;
+  for (int k = 0; k < a.K; ++k) sq += v[(int64_t)k * a.N + n] * v[(int64_t)k * a.N + n];
+  float inv = rsqrtf(fmaxf(sq, 1e-12f));
+  float eg = expf(a.params[a.p_g + n]);
+  auto at = [&](int k) -> float& {
+    return a.O ? a.O[(a.p_kernel + (int64_t)k * a.N + n) * a.batch + b] : a.grad[a.p_kernel + (int64_t)k * a.N + n];
+  };
+  float dot = 0.f;
+  for (int k = 0; k < a.K; ++k) dot += at(k) * v[(int64_t)k * a.N + n] * inv;
+  for (int k = 0; k < a.K; ++k) {
+    float u = v[(int64_t)k * a.N + n] * inv;
+    at(k) = eg * inv * (at(k) - u * dot);
+  }
+  if (a.O)
+    a.O[(a.p_g + n) * a.batch + b] = eg * dot;
+  else
+    a.grad[a.p_g + n] = eg * dot;
+}
+
+// ---------------------------------------------------------------- driver
+struct BwdTensors {
+  float* gvpd[40];
+  float* ghp[40];
+  float* gcatm;
+  float* gt;
+  float* gvp;
+  float* gl;
+  int64_t bytes;
+};
+
+static int64_t bwd_layout(const NetLayout& L, int64_t batch, char* base, BwdTensors* T) {
+  int64_t tiles = (batch + kTile - 1) / kTile;
+  int64_t tb = tiles * L.P * (int64_t)kTile * L.F * 4;
+  int64_t off = 0;
+  auto take = [&](int64_t bytes) -> float* {
+    float* p = base ? reinterpret_cast<float*>(base + off) : nullptr;
+    off += (bytes + 255) / 256 * 256;
+    return p;
+  };
+  BwdTensors tmp;
+  BwdTensors* t = T ? T : &tmp;
+  memset(t, 0, sizeof(*t));
+  for (int i = 0; i < L.n_cc; ++i) {
+    t->gvpd[i] = take(tb);
+    t->ghp[i] = take(tb);
+  }
+  t->gcatm = take(tb);
+  t->gt = take(tb);
+  t->gvp = take(tb);
+  t->gl = take(tiles * L.P * (int64_t)kTile * 8 * 4);
+  t->bytes = off;
+  return off;
+}
+
+static const float* w32(const NetLayout& L, const void* packed, int idx) {
+  return reinterpret_cast<const float*>(static_cast<const char*>(packed) + L.conv[idx].w32_off);
+}
+
+static void tap_list(int kind, WgArgs& w) {
+  if (kind == kConvV) {
+    w.ntaps = 9;
+    for (int t = 0; t < 9; ++t) {
+      w.dr[t] = t / 3 - 2;
+      w.dc[t] = t % 3 - 1;
+    }
+  } else if (kind == kConvH) {
+    w.ntaps = 3;
+    for (int t = 0; t < 3; ++t) {
+      w.dr[t] = 0;
+      w.dc[t] = t - 2;
+    }
+  } else {
+    w.ntaps = 9;
+    for (int t = 0; t < 9; ++t) {
+      w.dr[t] = t / 3 - 2;
+      w.dc[t] = t % 3 - 2;
+    }
+  }
+}
+
+template <typename T>
+static int launch_wgrad(const NetLayout& L, WgArgs& w, const ConvDesc& cd, float* grad, float* O, int64_t batch,
+                        cudaStream_t s) {
+  int64_t tiles = (batch + kTile - 1) / kTile;
+  w.batch = batch;
+  w.items = w.ntaps * ((w.cin + 7) / 8) * ((w.N + 7) / 8);
+  if (O) {
+    w.O = O;
+    w.o_kernel = cd.p_kernel;
+    w.o_bias = cd.p_bias;
+  } else {
+    w.dW = grad + cd.p_kernel;
+    w.dB = grad + cd.p_bias;
+  }
+  dim3 grid((unsigned)tiles, (unsigned)((w.items + kItemsPerCta - 1) / kItemsPerCta));
+  wgrad_kernel<T><<<grid, 128, 0, s>>>(w, L.H, L.W);
+  return check_cuda(launched(), "wgrad_kernel");
+}
+
+template <int F, typename T>
+static int backward_impl(const NetLayout& L, const void* packed, const float* params, const int8_t* spins,
+                         int64_t batch, const float* seeds, const Tensors& A, const BwdTensors& G, float* grad,
+                         float* O, cudaStream_t s) {
+  const int64_t tiles = (batch + kTile - 1) / kTile;
+  const unsigned rows = (unsigned)(tiles * L.H);
+  const int last = L.n_cc - 1;
+  int st;
+  // Per-sample rows are written exactly once per (parameter, sample); the
+  // summed gradient accumulates with atomics and starts from zero.
+  if (!O) FK_CUDA(cudaMemsetAsync(grad, 0, (size_t)L.num_params * sizeof(float), s));
+  {
+    HeadBwdArgs h;
+    const int io = L.n_convs - 1;
+    h.hlast = A.h[last];
+    h.wo = w32(L, packed, io);
+    h.bo = reinterpret_cast<const float*>(static_cast<const char*>(packed) + L.conv[io].b_off);
+    h.spins = spins;
+    h.seeds = reinterpret_cast<const float2*>(seeds);
+    h.batch = batch;
+    h.gL = G.gl;
+    h.ghp = G.ghp[last];
+    head_bwd_kernel<F, T><<<rows, 128, 0, s>>>(h, L.H, L.W);
+    FK_CUDA(launched());
+    WgArgs w;
+    memset(&w, 0, sizeof(w));
+    w.ntaps = 1;
+    w.X = A.h[last];
+    w.cin = F;
+    w.G = G.gl;
+    w.gC = 8;
+    w.g0 = 0;
+    w.N = 4;
+    w.spins = spins;
+    if ((st = launch_wgrad<T>(L, w, L.conv[io], grad, O, batch, s)) != FK_OK) return st;
+  }
+  for (int i = last; i >= 0; --i) {
+    const ConvDesc& cv = L.conv[conv_index(i, kConvV)];
+    const ConvDesc& ch = L.conv[conv_index(i, kConvH)];
+    const ConvDesc& cx = L.conv[conv_index(i, kConvX)];
+    const ConvDesc& cy = L.conv[conv_index(i, kConvY)];
+    const ConvDesc& cc = L.conv[conv_index(i, kConvC)];
+    CBwdArgs c;
+    c.ghp = G.ghp[i];
+    c.cat = A.cat[i];
+    c.t = A.t[i];
+    c.rv = A.rv[i];
+    c.gvpd = (i == last) ? nullptr : G.gvpd[i];
+    c.wc = w32(L, packed, conv_index(i, kConvC));
+    c.wx = w32(L, packed, conv_index(i, kConvX));
+    c.wy = w32(L, packed, conv_index(i, kConvY));
+    c.shift = (i == last) ? 1 : 0;
+    c.gcatm = G.gcatm;
+    c.gt = G.gt;
+    c.gvp = G.gvp;
+    c_bwd_kernel<F, T><<<rows, 128, 0, s>>>(c, L.H, L.W);
+    FK_CUDA(launched());
+    // weight gradients of the five convs of causal conv i
+    WgArgs w;
+    memset(&w, 0, sizeof(w));
+    w.spins = spins;
+    tap_list(kConvC, w);
+    w.X = A.cat[i];
+    w.cin = F;
+    w.G = G.ghp[i];
+    w.gC = F;
+    w.N = F;
+    if ((st = launch_wgrad<T>(L, w, cc, grad, O, batch, s)) != FK_OK) return st;
+    memset(&w, 0, sizeof(w));
+    w.spins = spins;
+    w.ntaps = 1;
+    w.dr[0] = 0;
+    w.dc[0] = (i == last) ? -1 : 0;
+    w.X = A.t[i];
+    w.cin = F;
+    w.G = G.gcatm;
+    w.gC = F;
+    w.g0 = 0;
+    w.N = F / 2;
+    if ((st = launch_wgrad<T>(L, w, cx, grad, O, batch, s)) != FK_OK) return st;
+    w.dr[0] = -1;
+    w.dc[0] = 0;
+    w.X = A.rv[i];
+    w.g0 = F / 2;
+    if ((st = launch_wgrad<T>(L, w, cy, grad, O, batch, s)) != FK_OK) return st;
+    memset(&w, 0, sizeof(w));
+    w.spins = spins;
+    tap_list(kConvH, w);
+    w.X = i == 0 ? nullptr : A.h[i - 1];
+    w.cin = i == 0 ? 1 : F;
+    w.G = G.gt;
+    w.gC = F;
+    w.N = F;
+    if ((st = launch_wgrad<T>(L, w, ch, grad, O, batch, s)) != FK_OK) return st;
+    tap_list(kConvV, w);
+    w.X = i == 0 ? nullptr : A.v[i - 1];
+    w.G = G.gvp;
+    if ((st = launch_wgrad<T>(L, w, cv, grad, O, batch, s)) != FK_OK) return st;
+    if (i > 0) {
+      VHBwdArgs v;
+      v.gvp = G.gvp;
+      v.gt = G.gt;
+      v.wv = w32(L, packed, conv_index(i, kConvV));
+      v.wh = w32(L, packed, conv_index(i, kConvH));
+      // cc i = 2b+1 is the first conv of a block whose second conv (2b+2)
+      // adds the block input S_{2b} = S_{i-1} as residual.
+      const bool block_first = (i % 2 == 1) && (i + 1 < last);
+      v.res_v = block_first ? G.gvpd[i + 1] : nullptr;
+      v.res_h = block_first ? G.ghp[i + 1] : nullptr;
+      v.vprev = A.v[i - 1];
+      v.hprev = A.h[i - 1];
+      v.gvpd_prev = G.gvpd[i - 1];
+      v.ghp_prev = G.ghp[i - 1];
+      vh_bwd_kernel<F, T><<<rows, 128, 0, s>>>(v, L.H, L.W);
+      FK_CUDA(launched());
+    }
+  }
+  if (L.wn) {
+    for (int k = 0; k < L.n_convs - 1; ++k) {
+      const ConvDesc& cd = L.conv[k];
+      WnArgs a;
+      a.params = params;
+      a.p_kernel = cd.p_kernel;
+      a.p_g = cd.p_g;
+      a.K = cd.K;
+      a.N = cd.cout;
+      a.grad = grad;
+      a.O = O;
+      a.batch = batch;
+      int64_t cols = O ? (int64_t)cd.cout * batch : cd.cout;
+      wn_kernel<<<(unsigned)((cols + 127) / 128), 128, 0, s>>>(a);
+      FK_CUDA(launched());
+    }
+  }
+  return FK_OK;
+}
+
+}  // namespace fk
+
+using namespace fk;
+
+extern "C" {
+
+int64_t fk_ar2d_backward_workspace_bytes(const fk_ar2d_desc* desc, int64_t batch) {
+  NetLayout L;
+  if (build_layout(desc, &L) != FK_OK || batch < 0) return -1;
+  return bwd_layout(L, batch, nullptr, nullptr);
+}
+
+int fk_ar2d_backward(const fk_ar2d_desc* desc, const void* packed, const float* params, const int8_t* spins,
+                     int64_t batch, const float* w, const void* saved, int64_t saved_bytes, void* workspace,
+                     int64_t workspace_bytes, float* grad, float* per_sample, void* stream) {
+  NetLayout L;
+  int st = build_layout(desc, &L);
+  if (st != FK_OK) return st;
+  FK_CHECK_ARG(packed && params && spins && w && saved, "fk_ar2d_backward: NULL buffer");
+  FK_CHECK_ARG(grad || per_sample, "fk_ar2d_backward: need grad or per_sample");
+  if (batch == 0) return FK_OK;
+  Tensors A;
+  int64_t need = workspace_layout(L, batch, FK_AR2D_SAVE, static_cast<char*>(const_cast<void*>(saved)), &A);
+  FK_CHECK_ARG(saved_bytes >= need, "fk_ar2d_backward: saved workspace %lld < %lld bytes", (long long)saved_bytes,
+               (long long)need);
+  BwdTensors G;
+  int64_t gneed = bwd_layout(L, batch, static_cast<char*>(workspace), &G);
+  FK_CHECK_ARG(workspace && workspace_bytes >= gneed, "fk_ar2d_backward: workspace %lld < %lld bytes",
+               (long long)workspace_bytes, (long long)gneed);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  float* O = per_sample;
+  float* g = per_sample ? nullptr : grad;
+  const bool bf = L.precision == FK_PRECISION_BF16;
+  switch (L.F) {
+    case 16: return bf ? backward_impl<16, __nv_bfloat16>(L, packed, params, spins, batch, w, A, G, g, O, s)
+                       : backward_impl<16, float>(L, packed, params, spins, batch, w, A, G, g, O, s);
+    case 32: return bf ? backward_impl<32, __nv_bfloat16>(L, packed, params, spins, batch, w, A, G, g, O, s)
+                       : backward_impl<32, float>(L, packed, params, spins, batch, w, A, G, g, O, s);
+    default: return bf ? backward_impl<64, __nv_bfloat16>(L, packed, params, spins, batch, w, A, G, g, O, s)
+                       : backward_impl<64, float>(L, packed, params, spins, batch, w, A, G, g, O, s);
+  }
+}
+
+}  // extern "C"

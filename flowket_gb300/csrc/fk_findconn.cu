@@ -1,0 +1,475 @@
+// Kernel (c): connected-configuration enumeration, compaction and the local
+// energy reduction.
+//
+// Enumeration is integer work: one thread per sample packs its +-1 row into
+// 64-bit words (bit = 1 for spin -1), walks the bonds in the reference's slot
+// order and writes (flip pair, matrix element, use flag) per slot. Dense
+// configurations and the compact list of used connections are expanded by a
+// separate, fully coalesced kernel (one thread per 16-byte chunk of a row).
+#include "fk_common.cuh"
+
+namespace fk {
+
+constexpr int kMaxSites = 1024;
+constexpr int kWords = kMaxSites / 64;
+
+struct SpinBits {
+  uint64_t w[kWords];
+  __device__ __forceinline__ int get(int k) const { return ((w[k >> 6] >> (k & 63)) & 1) ? -1 : 1; }
+};
+
+__device__ __forceinline__ void load_bits(const int8_t* __restrict__ row, int n, SpinBits& s) {
+  for (int i = 0; i < kWords; ++i) s.w[i] = 0;
+  for (int k = 0; k < n; ++k) {
+    if (row[k] < 0) s.w[k >> 6] |= (uint64_t)1 << (k & 63);
+  }
+}
+
+__device__ __forceinline__ void put_slot(int64_t slot, int64_t batch, int64_t b, int f0, int f1, double m,
+                                         uint8_t u, int16_t* flips, double* mel, uint8_t* use) {
+  int64_t o = slot * batch + b;
+  reinterpret_cast<short2*>(flips)[o] = make_short2((short)f0, (short)f1);
+  mel[o] = m;
+  use[o] = u;
+}
+
+// operators/heisenberg.py:129-166 (calc_conn_and_mel) and :117-127.
+__global__ void heisenberg_kernel(const int8_t* __restrict__ spins, int64_t batch, int hh, int ww, int dim,
+                                  int pbc, double off, int16_t* flips, double* mel, uint8_t* use) {
+  int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= batch) return;
+  int n = hh * ww;
+  SpinBits s;
+  load_bits(spins + b * n, n, s);
+  int diag = 0;
+  for (int i = 0; i < hh; ++i) {
+    for (int j = 0; j < ww; ++j) {
+      int site = i * ww + j;
+      int d = 0;
+      int s1 = s.get(site);
+      if (hh > 1) {
+        int64_t slot = 1 + (int64_t)site * dim + d;
+        if (i + 1 < hh || pbc) {
+          int o = (i + 1 < hh ? i + 1 : 0) * ww + j;
+          int s2 = s.get(o);
+          diag += s1 * s2;
+          uint8_t u = s1 != s2;
+          put_slot(slot, batch, b, u ? site : -1, u ? o : -1, u ? off : 0.0, u, flips, mel, use);
+        } else {
+          put_slot(slot, batch, b, -1, -1, 0.0, 0, flips, mel, use);
+        }
+        d += 1;
+      }
+      if (ww > 1) {
+        int64_t slot = 1 + (int64_t)site * dim + d;
+        if (j + 1 < ww || pbc) {
+          int o = i * ww + (j + 1 < ww ? j + 1 : 0);
+          int s2 = s.get(o);
+          diag += s1 * s2;
+          uint8_t u = s1 != s2;
+          put_slot(slot, batch, b, u ? site : -1, u ? o : -1, u ? off : 0.0, u, flips, mel, use);
+        } else {
+          put_slot(slot, batch, b, -1, -1, 0.0, 0, flips, mel, use);
+        }
+        d += 1;
+      }
+      // Slots of this site that the lattice never fills (an axis of size 1
+      // on a 2D shape) keep the untouched sample, element 0, unused.
+      for (; d < dim; ++d) put_slot(1 + (int64_t)site * dim + d, batch, b, -1, -1, 0.0, 0, flips, mel, use);
+    }
+  }
+  put_slot(0, batch, b, -1, -1, (double)diag, 1, flips, mel, use);
+}
+
+// operators/ising.py:17-46: diagonal accumulated per site in float32, one
+// single-flip slot per site in row-major order with element -h.
+__global__ void ising_kernel(const int8_t* __restrict__ spins, int64_t batch, int hh, int ww, int one_dim,
+                             double h, double j, int pbc, int16_t* flips, double* mel, uint8_t* use) {
+  int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= batch) return;
+  int n = hh * ww;
+  SpinBits s;
+  load_bits(spins + b * n, n, s);
+  float total = 0.f;
+  for (int i = 0; i < hh; ++i) {
+    for (int k = 0; k < ww; ++k) {
+      int site = i * ww + k;
+      float m = 0.f;
+      double s1 = (double)s.get(site);
+      if (one_dim) {
+        double nb = (i + 1 < hh) ? (double)s.get(site + 1) : (pbc ? (double)s.get(0) : 0.0);
+        m = (float)((double)m - j * s1 * nb);
+      } else {
+        if (hh > 1) {
+          double nb = (i + 1 < hh) ? (double)s.get((i + 1) * ww + k) : (pbc ? (double)s.get(k) : 0.0);
+          m = (float)((double)m - j * s1 * nb);
+        }
+        if (ww > 1) {
+          double nb = (k + 1 < ww) ? (double)s.get(i * ww + k + 1) : (pbc ? (double)s.get(i * ww) : 0.0);
+          m = (float)((double)m - j * s1 * nb);
+        }
+      }
+      total += m;
+      put_slot(1 + site, batch, b, site, -1, -h, 1, flips, mel, use);
+    }
+  }
+  put_slot(0, batch, b, -1, -1, (double)total, 1, flips, mel, use);
+}
+
+// Emits the J1-J2 edges (a, c, colour) in the order of operators/j1j2.py:13-35.
+template <typename F>
+__device__ __forceinline__ void for_each_j1j2_edge(int l1, int l2, int pbc, F&& f) {
+  for (int h = 0; h < l1; ++h) {
+    for (int w = 0; w < l2 - 1; ++w) {
+      f(w + l2 * h, w + 1 + l2 * h, 1);
+      if (h < l1 - 1) {
+        f(w + l2 * h, w + l2 * (h + 1), 1);
+        f(w + l2 * h, w + 1 + l2 * (h + 1), 2);
+      } else if (pbc) {
+        f(w + l2 * h, w, 1);
+        f(w + l2 * h, w + 1, 2);
+      }
+      if (h > 0) {
+        f(w + l2 * h, w + 1 + l2 * (h - 1), 2);
+      } else if (pbc) {
+        f(w + l2 * h, w + 1 + l2 * (l1 - 1), 2);
+      }
+    }
+    int w = l2 - 1;
+    if (pbc) {
+      f(l2 - 1 + l2 * h, l2 * h, 1);
+      f(w + l2 * h, l2 * ((h + 1) % l1), 2);
+      f(w + l2 * h, l2 * ((l1 + h - 1) % l1), 2);
+    }
+    if (h < l1 - 1) {
+      f(w + l2 * h, w + l2 * (h + 1), 1);
+    } else if (pbc) {
+      f(w + l2 * h, w, 1);
+    }
+  }
+}
+
+// J_c (sz sz + sx sx + sy sy) per edge (j1j2.py:37-48): diagonal J_c s_a s_c,
+// exchange element 2 J_c for antiparallel edges, packed in edge order; the
+// padding slots are zero configurations (flip code -2), element 0, unused
+// (netket_operator.py:56-66).
+__global__ void j1j2_kernel(const int8_t* __restrict__ spins, int64_t batch, int l1, int l2, double j2, int pbc,
+                            int n_slots, int16_t* flips, double* mel, uint8_t* use) {
+  int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= batch) return;
+  int n = l1 * l2;
+  SpinBits s;
+  load_bits(spins + b * n, n, s);
+  double diag = 0.0;
+  int k = 1;
+  for_each_j1j2_edge(l1, l2, pbc, [&](int a, int c, int col) {
+    double jc = col == 1 ? 1.0 : j2;
+    int sa = s.get(a), sc = s.get(c);
+    diag += jc * (double)(sa * sc);
+    if (sa != sc && k < n_slots) {
+      put_slot(k, batch, b, a, c, 2.0 * jc, 1, flips, mel, use);
+      ++k;
+    }
+  });
+  for (; k < n_slots; ++k) put_slot(k, batch, b, -2, -2, 0.0, 0, flips, mel, use);
+  put_slot(0, batch, b, -1, -1, diag, 1, flips, mel, use);
+}
+
+// Dense or compact expansion of configurations: thread per (row, 16-byte chunk).
+// row r takes base sample src[r] and flip pair fl[r]; a flip code of -2 writes
+// an all-zero configuration.
+__global__ void expand_kernel(const int8_t* __restrict__ spins, int n, int64_t rows,
+                              const int32_t* __restrict__ src, int64_t batch, const short2* __restrict__ fl,
+                              const int64_t* __restrict__ rows_dev, int8_t* __restrict__ out) {
+  int chunks = (n + 15) / 16;
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (rows_dev && *rows_dev < rows) rows = *rows_dev;
+  if (t >= rows * chunks) return;
+  int64_t r = t / chunks;
+  int ch = (int)(t - r * chunks);
+  int64_t b = src ? src[r] : (r % batch);
+  short2 f = fl[r];
+  int8_t buf[16];
+  int k0 = ch * 16;
+  for (int q = 0; q < 16; ++q) {
+    int k = k0 + q;
+    int8_t v = 0;
+    if (k < n && f.x != -2) {
+      v = spins[b * n + k];
+      if (k == f.x || k == f.y) v = (int8_t)-v;
+    }
+    buf[q] = v;
+  }
+  int8_t* dst = out + r * n + k0;
+  int cnt = n - k0 < 16 ? n - k0 : 16;
+  if (cnt == 16 && ((reinterpret_cast<uintptr_t>(dst) & 15) == 0)) {
+    *reinterpret_cast<int4*>(dst) = *reinterpret_cast<int4*>(buf);
+  } else {
+    for (int q = 0; q < cnt; ++q) dst[q] = buf[q];
+  }
+}
+
+// ---- compaction
+__global__ void count_kernel(const uint8_t* __restrict__ use, int64_t batch, int n_slots, int skip_self,
+                             int64_t* __restrict__ counts) {
+  int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= batch) return;
+  int64_t c = 0;
+  for (int k = skip_self ? 1 : 0; k < n_slots; ++k) c += use[(int64_t)k * batch + b] ? 1 : 0;
+  counts[b] = c;
+}
+
+// Single-block exclusive scan of counts into offsets[0..batch], offsets[batch] = total.
+__global__ void scan_kernel(const int64_t* __restrict__ counts, int64_t batch, int64_t* __restrict__ offsets,
+                            int64_t* __restrict__ total) {
+  __shared__ int64_t part[1024];
+  int t = threadIdx.x;
+  int64_t per = (batch + blockDim.x - 1) / blockDim.x;
+  int64_t lo = t * per, hi = lo + per < batch ? lo + per : batch;
+  int64_t s = 0;
+  for (int64_t i = lo; i < hi; ++i) s += counts[i];
+  part[t] = s;
+  __syncthreads();
+  if (t == 0) {
+    int64_t run = 0;
+    for (int i = 0; i < (int)blockDim.x; ++i) {
+      int64_t v = part[i];
+      part[i] = run;
+      run += v;
+    }
+    offsets[batch] = run;
+    *total = run;
+  }
+  __syncthreads();
+  int64_t run = part[t];
+  for (int64_t i = lo; i < hi; ++i) {
+    offsets[i] = run;
+    run += counts[i];
+  }
+}
+
+__global__ void fill_rows_kernel(const uint8_t* __restrict__ use, const int16_t* __restrict__ flips,
+                                 const double* __restrict__ mel, int64_t batch, int n_slots, int skip_self,
+                                 const int64_t* __restrict__ offsets, int64_t max_rows, int32_t* __restrict__ owner,
+                                 double* __restrict__ cmel, short2* __restrict__ cflips) {
+  int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= batch) return;
+  int64_t r = offsets[b];
+  for (int k = skip_self ? 1 : 0; k < n_slots; ++k) {
+    int64_t o = (int64_t)k * batch + b;
+    if (!use[o]) continue;
+    if (r < max_rows) {
+      owner[r] = (int32_t)b;
+      cmel[r] = mel[o];
+      cflips[r] = reinterpret_cast<const short2*>(flips)[o];
+    }
+    ++r;
+  }
+}
+
+// ---- local energy: one warp per sample, Kahan-compensated FP32 complex sum of
+// mel * exp(logpsi_row - logpsi_self) (the reference forms the ratio in
+// complex64, observables/monte_carlo/operator.py:28-33), diagonal added in FP64.
+__global__ void local_energy_kernel(const float2* __restrict__ lp_self, const double* __restrict__ mel_self,
+                                    int64_t batch, const float2* __restrict__ lp_rows,
+                                    const double* __restrict__ cmel, const int64_t* __restrict__ offsets,
+                                    double2* __restrict__ local) {
+  int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (w >= batch) return;
+  float2 l0 = lp_self[w];
+  int64_t lo = offsets[w], hi = offsets[w + 1];
+  Kahan re, im;
+  for (int64_t r = lo + lane; r < hi; r += 32) {
+    float2 l = lp_rows[r];
+    float a = expf(l.x - l0.x);
+    float sn, cs;
+    sincosf(l.y - l0.y, &sn, &cs);
+    float m = (float)cmel[r];
+    re.add(m * a * cs);
+    im.add(m * a * sn);
+  }
+  // pairwise tree over lanes, carrying the compensation terms
+  float rs = re.s, rc = re.c, is = im.s, ic = im.c;
+  for (int o = 16; o > 0; o >>= 1) {
+    rs += __shfl_xor_sync(0xffffffffu, rs, o);
+    rc += __shfl_xor_sync(0xffffffffu, rc, o);
+    is += __shfl_xor_sync(0xffffffffu, is, o);
+    ic += __shfl_xor_sync(0xffffffffu, ic, o);
+  }
+  if (lane == 0) local[w] = make_double2((double)rs - (double)rc + mel_self[w], (double)is - (double)ic);
+}
+
+// FP64 mean / variance and loss weights; single block, compensated by
+// accumulating in double over a fixed pairwise order.
+__global__ void energy_stats_kernel(const double2* __restrict__ local, int64_t batch, double* stats,
+                                    float2* __restrict__ w) {
+  __shared__ double sre[1024], sim[1024];
+  int t = threadIdx.x;
+  double a = 0.0, c = 0.0;
+  for (int64_t i = t; i < batch; i += blockDim.x) {
+    a += local[i].x;
+    c += local[i].y;
+  }
+  sre[t] = a;
+  sim[t] = c;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (t < o) {
+      sre[t] += sre[t + o];
+      sim[t] += sim[t + o];
+    }
+    __syncthreads();
+  }
+  double mre = sre[0] / (double)batch, mim = sim[0] / (double)batch;
+  __syncthreads();
+  double v = 0.0;
+  for (int64_t i = t; i < batch; i += blockDim.x) {
+    double d = local[i].x - mre;
+    v += d * d;
+  }
+  sre[t] = v;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (t < o) sre[t] += sre[t + o];
+    __syncthreads();
+  }
+  if (t == 0) {
+    stats[0] = mre;
+    stats[1] = mim;
+    stats[2] = sre[0] / (double)batch;
+  }
+  // y = conj(E - Ebar)/B ; loss = mean 2 Re(logpsi y) -> weights 2Re(y)/B, -2Im(y)/B
+  double inv = 1.0 / (double)batch;
+  for (int64_t i = t; i < batch; i += blockDim.x) {
+    double yre = (local[i].x - mre) * inv;
+    double yim = -(local[i].y - mim) * inv;
+    w[i] = make_float2((float)(2.0 * yre * inv), (float)(-2.0 * yim * inv));
+  }
+}
+
+static int launch_expand(const int8_t* spins, int n, int64_t rows, const int32_t* src, int64_t batch,
+                         const short2* fl, const int64_t* rows_dev, int8_t* out, cudaStream_t s) {
+  if (rows == 0) return FK_OK;
+  int chunks = (n + 15) / 16;
+  int64_t total = rows * chunks;
+  expand_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(spins, n, rows, src, batch, fl, rows_dev, out);
+  return check_cuda(launched(), "expand_kernel");
+}
+
+static int dense_conn(const int8_t* spins, int64_t batch, int n, int n_slots, const int16_t* flips, int8_t* conn,
+                      cudaStream_t s) {
+  if (!conn) return FK_OK;
+  return launch_expand(spins, n, (int64_t)n_slots * batch, nullptr, batch, reinterpret_cast<const short2*>(flips),
+                       nullptr, conn, s);
+}
+
+}  // namespace fk
+
+using namespace fk;
+
+extern "C" {
+
+int fk_find_conn_heisenberg(const int8_t* spins, int64_t batch, int32_t height, int32_t width, int32_t dim,
+                            int32_t pbc, int32_t unitary_rotation, int16_t* flips, double* mel, uint8_t* use,
+                            int8_t* conn, void* stream) {
+  if (batch == 0) return FK_OK;
+  FK_CHECK_ARG(spins && flips && mel && use && batch >= 0, "fk_find_conn_heisenberg: NULL buffer");
+  FK_CHECK_ARG(height >= 1 && width >= 1 && height * width <= kMaxSites, "fk_find_conn_heisenberg: lattice %dx%d",
+               height, width);
+  FK_CHECK_ARG(dim == 1 || dim == 2, "fk_find_conn_heisenberg: dim must be 1 or 2");
+  FK_CHECK_ARG(dim == 2 || width == 1, "fk_find_conn_heisenberg: a chain is passed as height=L, width=1");
+  if (batch == 0) return FK_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  heisenberg_kernel<<<(unsigned)((batch + 127) / 128), 128, 0, s>>>(spins, batch, height, width, dim, pbc,
+                                                                    unitary_rotation ? -2.0 : 2.0, flips, mel,
+                                                                    use);
+  FK_CUDA(launched());
+  return dense_conn(spins, batch, height * width, height * width * dim + 1, flips, conn, s);
+}
+
+int fk_find_conn_ising(const int8_t* spins, int64_t batch, int32_t height, int32_t width, double h, double j,
+                       int32_t pbc, int16_t* flips, double* mel, uint8_t* use, int8_t* conn, void* stream) {
+  if (batch == 0) return FK_OK;
+  FK_CHECK_ARG(spins && flips && mel && use && batch >= 0, "fk_find_conn_ising: NULL buffer");
+  FK_CHECK_ARG(height >= 1 && width >= 1 && height * width <= kMaxSites, "fk_find_conn_ising: lattice %dx%d",
+               height, width);
+  if (batch == 0) return FK_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // width == 0 would mean a chain; chains are passed as (L, 1) with one_dim=1 when width==1 and height>1.
+  int one_dim = (width == 1) ? 1 : 0;
+  ising_kernel<<<(unsigned)((batch + 127) / 128), 128, 0, s>>>(spins, batch, height, width, one_dim, h, j, pbc,
+                                                               flips, mel, use);
+  FK_CUDA(launched());
+  return dense_conn(spins, batch, height * width, height * width + 1, flips, conn, s);
+}
+
+int fk_find_conn_j1j2(const int8_t* spins, int64_t batch, int32_t height, int32_t width, double j2, int32_t pbc,
+                      int16_t* flips, double* mel, uint8_t* use, int8_t* conn, void* stream) {
+  if (batch == 0) return FK_OK;
+  FK_CHECK_ARG(spins && flips && mel && use && batch >= 0, "fk_find_conn_j1j2: NULL buffer");
+  FK_CHECK_ARG(height >= 2 && width >= 2 && height * width <= kMaxSites, "fk_find_conn_j1j2: lattice %dx%d",
+               height, width);
+  if (batch == 0) return FK_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int n_slots = 4 * height * width + 1;
+  j1j2_kernel<<<(unsigned)((batch + 127) / 128), 128, 0, s>>>(spins, batch, height, width, j2, pbc, n_slots,
+                                                              flips, mel, use);
+  FK_CUDA(launched());
+  return dense_conn(spins, batch, height * width, n_slots, flips, conn, s);
+}
+
+int64_t fk_compact_workspace_bytes(int64_t batch) { return (batch + 1) * 8 + 256; }
+
+int fk_compact_connections(const int8_t* spins, int64_t batch, int32_t n_sites, int32_t n_slots,
+                           const int16_t* flips, const double* mel, const uint8_t* use, int32_t skip_self,
+                           int8_t* configs, int32_t* owner, double* cmel, int16_t* cflips, int64_t* offsets,
+                           int64_t max_rows, int64_t* n_rows, void* workspace, int64_t workspace_bytes,
+                           void* stream) {
+  FK_CHECK_ARG(spins && flips && mel && use && owner && cmel && cflips && offsets && n_rows,
+               "fk_compact_connections: NULL buffer");
+  FK_CHECK_ARG(workspace && workspace_bytes >= fk_compact_workspace_bytes(batch),
+               "fk_compact_connections: workspace too small");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int64_t* counts = static_cast<int64_t*>(workspace);
+  if (batch == 0) {
+    FK_CUDA(cudaMemsetAsync(n_rows, 0, sizeof(int64_t), s));
+    return FK_OK;
+  }
+  count_kernel<<<(unsigned)((batch + 255) / 256), 256, 0, s>>>(use, batch, n_slots, skip_self, counts);
+  scan_kernel<<<1, 1024, 0, s>>>(counts, batch, offsets, n_rows);
+  fill_rows_kernel<<<(unsigned)((batch + 127) / 128), 128, 0, s>>>(
+      use, flips, mel, batch, n_slots, skip_self, offsets, max_rows, owner, cmel,
+      reinterpret_cast<short2*>(cflips));
+  FK_CUDA(launched(3));
+  if (configs) {
+    // rows beyond max_rows are not written; the caller sizes max_rows for the worst case
+    return launch_expand(spins, n_sites, max_rows, owner, batch, reinterpret_cast<const short2*>(cflips), n_rows,
+                         configs, s);
+  }
+  return FK_OK;
+}
+
+int fk_local_energy_reduce(const float* log_psi_self, const double* mel_self, int64_t batch,
+                           const float* log_psi_rows, const int64_t* offsets, const double* cmel, double* local,
+                           void* stream) {
+  FK_CHECK_ARG(log_psi_self && mel_self && offsets && local && batch >= 0, "fk_local_energy_reduce: NULL buffer");
+  if (batch == 0) return FK_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int64_t threads = batch * 32;
+  local_energy_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
+      reinterpret_cast<const float2*>(log_psi_self), mel_self, batch, reinterpret_cast<const float2*>(log_psi_rows),
+      cmel, offsets, reinterpret_cast<double2*>(local));
+  FK_CUDA(launched());
+  return FK_OK;
+}
+
+int fk_energy_stats(const double* local, int64_t batch, double* stats, float* w, void* stream) {
+  FK_CHECK_ARG(local && stats && w && batch > 0, "fk_energy_stats: bad arguments");
+  energy_stats_kernel<<<1, 1024, 0, static_cast<cudaStream_t>(stream)>>>(
+      reinterpret_cast<const double2*>(local), batch, stats, reinterpret_cast<float2*>(w));
+  FK_CUDA(launched());
+  return FK_OK;
+}
+
+}  // extern "C"

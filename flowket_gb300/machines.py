@@ -1,0 +1,247 @@
+"""Wave-function machines (flowket.machines drop-ins) over the CUDA library.
+
+``ConvNetAutoregressive2D`` mirrors machines/conv_net_autoregressive_2D.py:8-78
+(the PixelCNN-style causal conv net with vertical/horizontal streams, weight
+normalisation with exponential norm, auto-normalised conditionals of
+machines/abstract_machine.py:49-71). ``RBM`` mirrors machines/rbm.py:35-48 and
+``RBMSym`` machines/rbm.py:51-65.
+
+Parameters live in one flat FP32 CUDA tensor in Keras layer order; every
+evaluation calls the library (no CPU fallback).
+"""
+import math
+
+import numpy as np
+import torch
+
+from . import _lib
+
+
+def _device(device):
+    if device is None:
+        device = torch.device("cuda", torch.cuda.current_device()) if torch.cuda.is_available() else None
+    if device is None:
+        raise _lib.FlowketError("flowket_gb300 machines need a CUDA device")
+    return torch.device(device)
+
+
+def ar2d_param_layout(depth, channels, weights_normalization):
+    """(name, shape, offset) of every parameter in the flat vector, matching
+    the library's layout: per causal conv i and conv in (v, h, x, y, c):
+    kernel (kh, kw, cin, cout), bias, [g]; then out.kernel, out.bias."""
+    f = channels
+    out = []
+    off = 0
+
+    def add(name, shape):
+        nonlocal off
+        out.append((name, shape, off))
+        off += int(np.prod(shape))
+
+    for i in range(2 * depth - 2):
+        cin = 1 if i == 0 else f
+        for conv, shape in (("v", (3, 3, cin, f)), ("h", (1, 3, cin, f)), ("x", (1, 1, f, f // 2)),
+                            ("y", (1, 1, f, f // 2)), ("c", (3, 3, f, f))):
+            add(f"cc{i}.{conv}.kernel", shape)
+            add(f"cc{i}.{conv}.bias", (shape[-1],))
+            if weights_normalization:
+                add(f"cc{i}.{conv}.g", (shape[-1],))
+    add("out.kernel", (1, 1, f, 4))
+    add("out.bias", (4,))
+    return out, off
+
+
+def glorot_uniform_init(layout, seed, weights_normalization):
+    """Seeded Glorot-uniform kernels (limit sqrt(6/(fan_in+fan_out)), keras
+    Conv2D default), zero biases, g = log(||v|| + 1e-10) (deepar/layers/wrappers.py:26-39)."""
+    gen = torch.Generator().manual_seed(seed)
+    flat = {}
+    for name, shape, _ in layout:
+        if name.endswith(".kernel"):
+            kh, kw, cin, cout = shape
+            limit = math.sqrt(6.0 / (kh * kw * cin + kh * kw * cout))
+            k = (torch.rand(shape, generator=gen, dtype=torch.float64) * 2 - 1) * limit
+            flat[name] = k
+            base = name[:-len(".kernel")]
+            flat[base + ".bias"] = torch.zeros(cout, dtype=torch.float64)
+            if weights_normalization and base != "out":
+                flat[base + ".g"] = torch.log(torch.sqrt((k * k).sum(dim=(0, 1, 2))) + 1e-10)
+    return flat
+
+
+class ConvNetAutoregressive2D:
+    """flowket.machines.ConvNetAutoregressive2D on GB300.
+
+    ``hilbert_state_shape`` replaces the Keras input layer (H, W).
+    ``precision`` selects the BF16 tcgen05 path ('bf16') or the plain FP32
+    CUDA-core path ('fp32')."""
+
+    def __init__(self, hilbert_state_shape, depth, num_of_channels, kernel_size=3, weights_normalization=True,
+                 exponential_norm=True, precision="bf16", seed=0, device=None, params=None):
+        if kernel_size != 3 or not exponential_norm:
+            raise ValueError("only kernel_size=3 with exponential_norm=True (the reference defaults) is supported")
+        shape = tuple(int(x) for x in hilbert_state_shape)
+        if len(shape) != 2:
+            raise ValueError("ConvNetAutoregressive2D needs a 2D hilbert_state_shape (use (1, L) for a chain)")
+        self.hilbert_state_shape = shape
+        self.depth = int(depth)
+        self.num_of_channels = int(num_of_channels)
+        self.weights_normalization = bool(weights_normalization)
+        self.precision = precision
+        self.device = _device(device)
+        self.desc = _lib.Ar2dDesc(shape[0], shape[1], self.depth, self.num_of_channels,
+                                  1 if self.weights_normalization else 0,
+                                  _lib.FK_PRECISION_BF16 if precision == "bf16" else _lib.FK_PRECISION_FP32)
+        lib = _lib.load()
+        self.layout, n = ar2d_param_layout(self.depth, self.num_of_channels, self.weights_normalization)
+        n_lib = lib.fk_ar2d_num_params(ctypes_ref(self.desc))
+        if n_lib < 0:
+            _lib.check(-1, "ConvNetAutoregressive2D")
+        assert n_lib == n, (n_lib, n)
+        self.num_params = n
+        if params is None:
+            init = glorot_uniform_init(self.layout, seed, self.weights_normalization)
+            flat = torch.cat([init[name].reshape(-1) for name, _, _ in self.layout]).to(torch.float32)
+        else:
+            flat = torch.as_tensor(params, dtype=torch.float32).reshape(-1)
+            assert flat.numel() == n
+        self.params = flat.to(self.device).contiguous()
+        self._packed = torch.empty(lib.fk_ar2d_packed_bytes(ctypes_ref(self.desc)), dtype=torch.uint8,
+                                   device=self.device)
+        self._packed_version = None
+        self._manual_version = 0
+        self._ws = {}
+
+    # ------------------------------------------------------------------ params
+    def named_params(self):
+        return {name: self.params[off:off + int(np.prod(shape))].view(shape) for name, shape, off in self.layout}
+
+    def params_dict_cpu(self, dtype=torch.float64):
+        return {k: v.detach().cpu().to(dtype).clone() for k, v in self.named_params().items()}
+
+    def count_params(self):
+        return self.num_params
+
+    def params_updated(self):
+        """Call after writing `params` through a raw pointer (the optimisers do)."""
+        self._manual_version += 1
+
+    def packed(self):
+        """Weight-normalised, operand-layout weights (repacked after updates)."""
+        ver = (self.params._version, self._manual_version)
+        if self._packed_version != ver:
+            _lib.call("fk_ar2d_pack", ctypes_ref(self.desc), _lib.ptr(self.params), _lib.ptr(self._packed),
+                      _lib.stream_ptr())
+            self._packed_version = ver
+        return self._packed
+
+    def workspace(self, batch, mode):
+        key = (mode, batch)
+        ws = self._ws.get(key)
+        if ws is None:
+            nbytes = _lib.load().fk_ar2d_workspace_bytes(ctypes_ref(self.desc), batch, mode)
+            if nbytes < 0:
+                _lib.check(-1, "fk_ar2d_workspace_bytes")
+            ws = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+            if len(self._ws) > 8:
+                self._ws.clear()
+            self._ws[key] = ws
+        return ws
+
+    # ------------------------------------------------------------------ evaluation
+    def _spins(self, spins):
+        s = torch.as_tensor(spins)
+        if s.device != self.device or s.dtype != torch.int8:
+            s = s.to(device=self.device, dtype=torch.int8)
+        return s.reshape(s.shape[0], self.hilbert_state_shape[0] * self.hilbert_state_shape[1]).contiguous()
+
+    def forward(self, spins, mode=_lib.FK_AR2D_INFER, with_cond=False, workspace=None):
+        """Returns (log_psi float32 (B, 2) (re, im), cond (B, N, 4) or None, workspace)."""
+        s = self._spins(spins)
+        b = s.shape[0]
+        lp = torch.empty((b, 2), dtype=torch.float32, device=self.device)
+        cond = torch.empty((b, s.shape[1], 4), dtype=torch.float32, device=self.device) if with_cond else None
+        ws = workspace if workspace is not None else self.workspace(b, mode)
+        _lib.call("fk_ar2d_forward", ctypes_ref(self.desc), _lib.ptr(self.packed()), _lib.ptr(s), b,
+                  _lib.ptr(lp), _lib.ptr(cond), _lib.ptr(ws), ws.numel(), mode, _lib.stream_ptr())
+        return lp, cond, ws
+
+    def log_psi(self, spins, chunk=1 << 16):
+        """Complex log psi (B,) (machines/abstract_machine.py:31-46)."""
+        s = self._spins(spins)
+        outs = []
+        for i in range(0, s.shape[0], chunk):
+            lp, _, _ = self.forward(s[i:i + chunk])
+            outs.append(torch.complex(lp[:, 0], lp[:, 1]))
+        return torch.cat(outs) if outs else torch.empty(0, dtype=torch.complex64, device=self.device)
+
+    def predict(self, spins, batch_size=None):
+        """Keras model.predict drop-in: (B, 1) complex64."""
+        return self.log_psi(spins, chunk=batch_size or (1 << 16)).unsqueeze(1)
+
+    __call__ = predict
+
+    def conditional_log_wave_function(self, spins):
+        """(B, H, W, 2) complex normalised conditionals (abstract_machine.py:56-57)."""
+        _, cond, _ = self.forward(spins, with_cond=True)
+        h, w = self.hilbert_state_shape
+        c = cond.view(-1, h, w, 4)
+        return torch.complex(c[..., 0:2], c[..., 2:4])
+
+    def conditional_log_probs(self, spins):
+        """(B, H, W, 2) log-probabilities 2 Re cond (abstract_machine.py:56-57)."""
+        _, cond, _ = self.forward(spins, with_cond=True)
+        h, w = self.hilbert_state_shape
+        return 2.0 * cond.view(-1, h, w, 4)[..., 0:2]
+
+
+def ctypes_ref(struct):
+    import ctypes
+    return ctypes.byref(struct)
+
+
+def _ar2d_backward(machine, spins, seeds, saved, per_sample=False):
+    """Adjoint of sum_b (w_re Re log psi_b + w_im Im log psi_b): flat gradient
+    (num_params,) or per-sample rows O (num_params, B) (param-major)."""
+    s = machine._spins(spins)
+    b = s.shape[0]
+    w = torch.as_tensor(seeds, dtype=torch.float32, device=machine.device).reshape(b, 2).contiguous()
+    lib = _lib.load()
+    nbytes = lib.fk_ar2d_backward_workspace_bytes(ctypes_ref(machine.desc), b)
+    key = ("bwd", b)
+    ws = machine._ws.get(key)
+    if ws is None or ws.numel() < nbytes:
+        ws = torch.empty(nbytes, dtype=torch.uint8, device=machine.device)
+        machine._ws[key] = ws
+    if per_sample:
+        out = torch.empty((machine.num_params, b), dtype=torch.float32, device=machine.device)
+        grad_p, ps_p = None, _lib.ptr(out)
+    else:
+        out = torch.empty(machine.num_params, dtype=torch.float32, device=machine.device)
+        grad_p, ps_p = _lib.ptr(out), None
+    _lib.call("fk_ar2d_backward", ctypes_ref(machine.desc), _lib.ptr(machine.packed()), _lib.ptr(machine.params),
+              _lib.ptr(s), b, _lib.ptr(w), _lib.ptr(saved), saved.numel(), _lib.ptr(ws), ws.numel(), grad_p, ps_p,
+              _lib.stream_ptr())
+    return out
+
+
+ConvNetAutoregressive2D.backward = _ar2d_backward
+
+
+def _ar2d_log_derivatives(machine, spins, saved=None):
+    """Per-sample complex O_k = d log psi / d theta_k (num_params, B) complex64
+    (the reference's predictions_jacobian, machines/abstract_machine.py:24-28)."""
+    s = machine._spins(spins)
+    if saved is None:
+        _, _, saved = machine.forward(s, mode=_lib.FK_AR2D_SAVE)
+    b = s.shape[0]
+    ones = torch.zeros((b, 2), dtype=torch.float32, device=machine.device)
+    ones[:, 0] = 1
+    o_re = machine.backward(s, ones, saved, per_sample=True)
+    ones[:, 0] = 0
+    ones[:, 1] = 1
+    o_im = machine.backward(s, ones, saved, per_sample=True)
+    return torch.complex(o_re, o_im)
+
+
+ConvNetAutoregressive2D.log_derivatives = _ar2d_log_derivatives

@@ -1,0 +1,109 @@
+"""Optimisers (flowket.optimizers / tf.keras drop-ins) updating a machine's
+flat parameter vector on the GPU.
+
+* ``Adam``: tf.keras Adam of TF 1.x (lr_t = lr sqrt(1-b2^t)/(1-b1^t),
+  epsilon = K.epsilon() = 1e-7), the optimiser of experiments/train.py:52
+  and the examples.
+* ``ComplexValuesStochasticReconfiguration``: optimizers/stochastic_reconfiguration/optimizer.py:14-183,
+  solved in sample space (see flowket_gb300.sr).
+"""
+import torch
+
+from . import _lib
+
+
+class Adam:
+    def __init__(self, machine, lr=1e-3, beta_1=0.9, beta_2=0.999, epsilon=1e-7):
+        self.machine = machine
+        self.lr, self.beta_1, self.beta_2, self.epsilon = float(lr), float(beta_1), float(beta_2), float(epsilon)
+        self.m = torch.zeros_like(machine.params)
+        self.v = torch.zeros_like(machine.params)
+        self.iterations = 0
+
+    def apply_gradient(self, grad):
+        self.iterations += 1
+        _lib.call("fk_adam_step", _lib.ptr(self.machine.params), _lib.ptr(grad), _lib.ptr(self.m), _lib.ptr(self.v),
+                  self.machine.num_params, self.iterations, self.lr, self.beta_1, self.beta_2, self.epsilon,
+                  _lib.stream_ptr())
+        self.machine.params_updated()
+
+    def state_dict(self):
+        return {"m": self.m, "v": self.v, "iterations": self.iterations}
+
+    def load_state_dict(self, state):
+        self.m.copy_(state["m"])
+        self.v.copy_(state["v"])
+        self.iterations = int(state["iterations"])
+
+
+class ComplexValuesStochasticReconfiguration:
+    """Stochastic reconfiguration (optimizers/stochastic_reconfiguration/optimizer.py:14-183)
+    in sample space on the GPU.
+
+    For a machine with real parameters and complex log psi (the AR network) the
+    update solves S x = F with S = Re<O_c^* O_c> + diag_shift I and
+    F = Re<O_c^* (E - Ebar)>, via the 2B x 2B Gram of Y = [Re O_c | Im O_c]:
+    alpha = (Y^T Y / B + diag_shift I)^-1 [Re E_c; Im E_c], x = Y alpha / B,
+    theta <- theta - lr x. The solve is FP64 CG with the reference's tolerance
+    rule (linear_equations.py:34-137); ``iterative_solver=False`` runs CG to
+    1e-10 instead of a Cholesky factorisation."""
+
+    def __init__(self, machine, predictions_jacobian=None, lr=0.01, diag_shift=0.05, iterative_solver=True,
+                 compute_jvp_instead_of_full_jacobian=False, use_cholesky=True, conjugate_gradient_tol=1e-3,
+                 iterative_solver_max_iterations=200, **kwargs):
+        self.machine = machine
+        self.lr = float(lr)
+        self.diag_shift = float(diag_shift)
+        self.iterative_solver = iterative_solver
+        self.tol = float(conjugate_gradient_tol) if iterative_solver else 1e-10
+        self.max_iter = int(iterative_solver_max_iterations or 1000) if iterative_solver else 2000
+        self.iterations = 0
+        self.last_stats = None
+        self._buf = {}
+
+    def _buffers(self, n, dev):
+        if n not in self._buf:
+            lib = _lib.load()
+            self._buf = {n: dict(gram=torch.empty((n, n), dtype=torch.float64, device=dev),
+                                 alpha=torch.empty(n, dtype=torch.float64, device=dev),
+                                 rhs=torch.empty(n, dtype=torch.float64, device=dev),
+                                 stats=torch.zeros(3, dtype=torch.float64, device=dev),
+                                 ws=torch.empty(lib.fk_sr_solve_workspace_bytes(n), dtype=torch.uint8, device=dev))}
+        return self._buf[n]
+
+    def update(self, spins, local, w, saved):
+        x = self.direction(spins, local, saved)
+        m = self.machine
+        _lib.call("fk_axpy", m.num_params, -self.lr, _lib.ptr(x), _lib.ptr(m.params), _lib.stream_ptr())
+        m.params_updated()
+        self.iterations += 1
+        self.last_stats = self._buf[2 * spins.shape[0]]["stats"]
+
+    def direction(self, spins, local, saved):
+        """The solution x of the SR system (no update), for tests."""
+        lr, self.lr = self.lr, 0.0
+        m = self.machine
+        b = spins.shape[0]
+        ones = torch.zeros((b, 2), dtype=torch.float32, device=m.device)
+        ones[:, 0] = 1
+        o_re = m.backward(spins, ones, saved, per_sample=True)
+        ones[:, 0] = 0
+        ones[:, 1] = 1
+        o_im = m.backward(spins, ones, saved, per_sample=True)
+        p = m.num_params
+        st = _lib.stream_ptr()
+        _lib.call("fk_center_columns", _lib.ptr(o_re), p, b, None, st)
+        _lib.call("fk_center_columns", _lib.ptr(o_im), p, b, None, st)
+        n = 2 * b
+        bf = self._buffers(n, m.device)
+        _lib.call("fk_sr_gram", _lib.ptr(o_re), _lib.ptr(o_im), p, b, _lib.ptr(bf["gram"]), n * n, st)
+        bf["rhs"][:b] = local[:, 0] - local[:, 0].mean()
+        bf["rhs"][b:] = local[:, 1] - local[:, 1].mean()
+        _lib.call("fk_sr_solve", _lib.ptr(bf["gram"]), n, 1.0 / b, self.diag_shift, _lib.ptr(bf["rhs"]), self.tol,
+                  self.max_iter, _lib.ptr(bf["alpha"]), _lib.ptr(bf["stats"]), _lib.ptr(bf["ws"]), bf["ws"].numel(),
+                  st)
+        x = torch.empty(p, dtype=torch.float32, device=m.device)
+        _lib.call("fk_sr_backmap", _lib.ptr(o_re), _lib.ptr(o_im), p, b, _lib.ptr(bf["alpha"]), 1.0 / b, 0.0, None,
+                  _lib.ptr(x), st)
+        self.lr = lr
+        return x

@@ -1,0 +1,209 @@
+/*
+ * flowket_gb300 -- C ABI of the GB300 (sm_103a) variational Monte Carlo hot path.
+ *
+ * Conventions
+ *   - Every entry point returns an int status: FK_OK (0) or a negative FK_ERR_*;
+ *     fk_last_error() returns the message of the last failure on this thread.
+ *   - All device buffers are caller owned. Scratch memory is passed in as a
+ *     workspace whose size comes from the matching *_bytes() query; the library
+ *     allocates nothing on these paths and never synchronises the stream.
+ *   - `stream` is a cudaStream_t passed as void*.
+ *   - Spins are int8 +-1 at the boundary, row-major [batch][H*W]; complex
+ *     numbers are interleaved (re, im) pairs.
+ *   - Citations name the reference (FlowKet) interface each entry point replaces,
+ *     as path:line within the FlowKet source tree.
+ */
+#ifndef FLOWKET_GB300_H
+#define FLOWKET_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FK_OK 0
+#define FK_ERR_ARG (-1)         /* bad argument or unsupported shape */
+#define FK_ERR_CUDA (-2)        /* a CUDA runtime call failed */
+#define FK_ERR_TIMEOUT (-3)     /* a device-side wait gave up (see fk_device_status) */
+#define FK_ERR_NONFINITE (-4)   /* a non-finite value where the reference raises */
+
+#define FK_PRECISION_FP32 0     /* plain FP32 CUDA-core path */
+#define FK_PRECISION_BF16 1     /* BF16 tcgen05 tensor-core path, FP32 accumulate */
+
+#define FK_AR2D_INFER 0         /* forward keeps only a rolling set of activations */
+#define FK_AR2D_SAVE 1          /* forward keeps every activation for the adjoint */
+
+const char* fk_last_error(void);
+/* Reads (and optionally clears) the device error word set by bounded waits. */
+int fk_device_status(int* status, int clear, void* stream);
+/* Library build string (arch, version). */
+const char* fk_version(void);
+/* Number of kernel launches this library has issued in this process. */
+int64_t fk_kernel_launches(void);
+
+/* ------------------------------------------------------------------ operators
+ * Connected-configuration enumeration (kernel c). For every sample b and slot c
+ * (slot 0 = the sample itself) writes:
+ *   flips[c][b][2]  int16 sites exchanged/flipped by slot c (-1 = none),
+ *   mel[c][b]       float64 matrix element,
+ *   use[c][b]       uint8 1 iff the slot is a real connection,
+ *   conn[c][b][N]   int8 connected configuration (optional, may be NULL).
+ * Slot order and values are those of the reference operator.
+ */
+/* operators/heisenberg.py:47-121 (HeisenbergFindConn.find_conn); slots = N*dim+1,
+ * dim = number of lattice axes (1 for a chain, 2 for H x W). */
+int fk_find_conn_heisenberg(const int8_t* spins, int64_t batch, int32_t height, int32_t width, int32_t dim,
+                            int32_t pbc, int32_t unitary_rotation, int16_t* flips, double* mel, uint8_t* use,
+                            int8_t* conn, void* stream);
+/* operators/ising.py:17-46 (Ising.find_conn); slots = N+1. */
+int fk_find_conn_ising(const int8_t* spins, int64_t batch, int32_t height, int32_t width, double h, double j,
+                       int32_t pbc, int16_t* flips, double* mel, uint8_t* use, int8_t* conn, void* stream);
+/* operators/j1j2.py:7-69 via operators/netket_operator.py:46-66; slots = 4N+1,
+ * exchange connections packed in edge order, unused slots zero. */
+int fk_find_conn_j1j2(const int8_t* spins, int64_t batch, int32_t height, int32_t width, double j2, int32_t pbc,
+                      int16_t* flips, double* mel, uint8_t* use, int8_t* conn, void* stream);
+
+/* Compaction of the used slots (observables/monte_carlo/operator.py:6-10):
+ * offsets[b] .. offsets[b+1] are the rows of sample b in the compact list
+ * (offsets int64 [B+1]); owner[row] = b; cmel[row] = matrix element;
+ * cflips[row][2] = the slot's flip pair; configs[row][N] = the connected
+ * configuration (optional, may be NULL). Slot 0 is skipped when skip_self != 0.
+ * *n_rows (device int64) receives the row count; rows beyond max_rows are
+ * counted but not written. Workspace: fk_compact_workspace_bytes(batch). */
+int64_t fk_compact_workspace_bytes(int64_t batch);
+int fk_compact_connections(const int8_t* spins, int64_t batch, int32_t n_sites, int32_t n_slots,
+                           const int16_t* flips, const double* mel, const uint8_t* use, int32_t skip_self,
+                           int8_t* configs, int32_t* owner, double* cmel, int16_t* cflips, int64_t* offsets,
+                           int64_t max_rows, int64_t* n_rows, void* workspace, int64_t workspace_bytes,
+                           void* stream);
+
+/* E_loc(b) = mel_self[b] + sum over rows of b of cmel * exp(logpsi_row - logpsi_b)
+ * (observables/monte_carlo/operator.py:20-42): the ratio in FP32 as the
+ * reference's complex64, Kahan-compensated FP32 sum, diagonal added in FP64.
+ * log psi arrays are [.][2] float32; local [B][2] float64. */
+int fk_local_energy_reduce(const float* log_psi_self, const double* mel_self, int64_t batch,
+                           const float* log_psi_rows, const int64_t* offsets, const double* cmel, double* local,
+                           void* stream);
+/* Mean and variance of the local energies (observables/monte_carlo/observable.py:10-14)
+ * and the loss weights w[b] = (2 Re y, -2 Im y) / B with y = conj(E - Ebar)/B
+ * (optimization/variational_monte_carlo.py:38-40, optimization/loss.py:4-5).
+ * stats = {Re mean, Im mean, var(Re)} float64; w float32 [B][2]. */
+int fk_energy_stats(const double* local, int64_t batch, double* stats, float* w, void* stream);
+
+/* ------------------------------------------------------------------ AR2D machine */
+typedef struct fk_ar2d_desc {
+  int32_t height;                /* lattice rows (1 for a chain) */
+  int32_t width;                 /* lattice columns */
+  int32_t depth;                 /* ConvNetAutoregressive2D depth, >= 2 */
+  int32_t channels;              /* num_of_channels: 16, 32 or 64 */
+  int32_t weights_normalization; /* 1 = WeightNormalization(exponential_norm=True) */
+  int32_t precision;             /* FK_PRECISION_FP32 or FK_PRECISION_BF16 */
+} fk_ar2d_desc;
+
+/* Flat FP32 parameter vector in Keras layer order: per causal conv i and conv
+ * x in (v, h, x, y, c): kernel (kh,kw,cin,cout), bias (cout), g (cout, only
+ * with weight normalisation); then out.kernel (1,1,F,4), out.bias (4).
+ * machines/conv_net_autoregressive_2D.py:24-74. */
+int64_t fk_ar2d_num_params(const fk_ar2d_desc* desc);
+int64_t fk_ar2d_packed_bytes(const fk_ar2d_desc* desc);
+/* Weight normalisation (deepar/layers/wrappers.py:123-134) and packing into the
+ * kernels' operand layouts. */
+int fk_ar2d_pack(const fk_ar2d_desc* desc, const float* params, void* packed, void* stream);
+int64_t fk_ar2d_workspace_bytes(const fk_ar2d_desc* desc, int64_t batch, int32_t mode);
+/* log psi (machines/abstract_machine.py:31-71, model.predict): log_psi [B][2];
+ * cond [B][N][4] = (Re0, Re1, Im0, Im1) normalised conditionals, optional.
+ * Index 0 of the last axis pair is spin +1 (deepar/layers/one_hot.py:7-9). */
+int fk_ar2d_forward(const fk_ar2d_desc* desc, const void* packed, const int8_t* spins, int64_t batch,
+                    float* log_psi, float* cond, void* workspace, int64_t workspace_bytes, int32_t mode,
+                    void* stream);
+/* Exact autoregressive sampling in raster order (deepar/samplers/fast_autoregressive.py:13-76,
+ * samplers/fast_autoregressive/__init__.py:8): one persistent CTA per 128
+ * samples walks the sites, evaluates each (layer, site) once and draws the
+ * site with Philox4x32-10 (counter = sample, site, offset). Writes spins [B][N],
+ * log_psi [B][2], and leaves the activations in `workspace` (FK_AR2D_SAVE
+ * layout) for fk_ar2d_backward. */
+int fk_ar2d_sample(const fk_ar2d_desc* desc, const void* packed, int64_t batch, uint64_t seed, uint64_t offset,
+                   int8_t* spins, float* log_psi, void* workspace, int64_t workspace_bytes, void* stream);
+/* Adjoint of log psi through the masked convolutions. Seeds w [B][2] weight
+ * Re and Im log psi of each sample. grad [num_params] = d/dtheta sum_b
+ * (w_re Re log psi_b + w_im Im log psi_b) (the Keras loss gradient of
+ * optimization/loss.py:4-5; utils/jacobian.py:114-127 per example). When
+ * per_sample != NULL it receives per_sample[b][num_params] instead of the sum.
+ * `saved` is the FK_AR2D_SAVE workspace of the forward/sample that produced
+ * the activations of these spins. */
+int64_t fk_ar2d_backward_workspace_bytes(const fk_ar2d_desc* desc, int64_t batch);
+int fk_ar2d_backward(const fk_ar2d_desc* desc, const void* packed, const float* params, const int8_t* spins,
+                     int64_t batch, const float* w, const void* saved, int64_t saved_bytes, void* workspace,
+                     int64_t workspace_bytes, float* grad, float* per_sample, void* stream);
+
+/* ------------------------------------------------------------------ optimisers */
+/* tf.keras Adam (TF 1.x): lr_t = lr sqrt(1-b2^t)/(1-b1^t), epsilon 1e-7.
+ * m, v, params, grad float32 [n]; `step` is t (1-based). */
+int fk_adam_step(float* params, const float* grad, float* m, float* v, int64_t n, int64_t step, float lr,
+                 float beta1, float beta2, float epsilon, void* stream);
+/* y += a x (float32): the SR parameter update W <- W - lr x
+ * (optimizers/complex_values_optimizer.py:48-58). */
+int fk_axpy(int64_t n, float a, const float* x, float* y, void* stream);
+
+/* ------------------------------------------------------------------ RBM + Metropolis-Hastings
+ * Complex RBM parameters as interleaved float32 (re, im):
+ * [a (n_visible) | b (n_hidden) | W (n_visible x n_hidden, row-major)].
+ * log psi = a.s + sum_j lncosh(b_j + W_j.s) (machines/rbm.py:35-48). */
+int fk_rbm_log_psi(const float* params, int32_t n_visible, int32_t n_hidden, const int8_t* spins, int64_t batch,
+                   float* log_psi, void* stream);
+/* Local energy from an operator enumeration (flips/mel/use as written by the
+ * fk_find_conn_* entry points), ratios from incremental theta updates
+ * (observables/monte_carlo/operator.py:13-53 with the RBM as wave function). */
+int fk_rbm_local_energy(const float* params, int32_t n_visible, int32_t n_hidden, const int8_t* spins, int64_t batch,
+                        const int16_t* flips, const double* mel, const uint8_t* use, int32_t n_slots, double* local,
+                        void* stream);
+/* Per-sample complex O_k (layers/complex/base_layer.py:18-35 convention:
+ * holomorphic derivative), parameter-major float32 [P][batch] re and im. */
+int fk_rbm_log_derivatives(const float* params, int32_t n_visible, int32_t n_hidden, const int8_t* spins,
+                           int64_t batch, float* o_re, float* o_im, void* stream);
+/* Persistent Metropolis-Hastings (samplers/metropolis_hastings.py:51-145):
+ * kind 0 = Local, 1 = Exchange; chains [n_chains][n_visible] and log_psi [n_chains][2]
+ * in/out; warmup_sweeps unrecorded sweeps, then samples_per_chain records every
+ * unused+1 sweeps into samples [n_chains][samples_per_chain][n_visible];
+ * *accepted (device) += accepted proposals. Philox counter (chain, sweep, 0x4D48). */
+int fk_rbm_mh_sweeps(const float* params, int32_t n_visible, int32_t n_hidden, int32_t height, int32_t width,
+                     int32_t kind, int8_t* chains, float* log_psi, int64_t n_chains, int64_t warmup_sweeps,
+                     int32_t samples_per_chain, int32_t unused, uint64_t seed, uint64_t sweep_offset, int8_t* samples,
+                     unsigned long long* accepted, void* stream);
+/* Independent-proposal step: accept candidates with
+ * min(1, |psi(s')|^2 q(s) / (|psi(s)|^2 q(s'))), log q = 2 Re log psi_q. The
+ * symmetric-proposal rule of MetropolisHastingsGlobal (metropolis_hastings.py:148-157)
+ * with the proposal ratio added, so any proposal leaves |psi|^2 invariant. */
+int fk_mh_independent_step(int8_t* chains, float* lp_chain, float* lq_chain, const int8_t* candidates,
+                           const float* lp_cand, const float* lq_cand, int64_t n_chains, int32_t n_visible,
+                           uint64_t seed, uint64_t step, unsigned long long* accepted, void* stream);
+
+/* ------------------------------------------------------------------ SR (kernel d)
+ * Sample-space stochastic reconfiguration
+ * (optimizers/stochastic_reconfiguration/optimizer.py:33-124): per-sample
+ * log-derivative rows O are parameter-major float32 [n_params][n_samples]. */
+/* Subtracts the mean over the columns from every row (J - mean(J), optimizer.py:111-114). */
+int fk_center_columns(float* y, int64_t rows, int64_t cols, float* mean, void* stream);
+/* gram (n x n float64, n = n_samples or 2 n_samples when o_im != NULL) =
+ * Y^T Y with Y = [o_re | o_im]: FP32 products, FP32 chunk sums reduced in FP64. */
+int64_t fk_sr_gram_workspace_bytes(int64_t n_params, int64_t n_samples);
+int fk_sr_gram(const float* o_re, const float* o_im, int64_t n_params, int64_t n_samples, double* gram,
+               int64_t gram_elems, void* stream);
+/* FP64 conjugate gradients on (scale * gram + shift I) x = rhs, stopping at
+ * ||r|| <= tol ||rhs|| or max_iter (linear_equations.py:34-137); stats (device,
+ * optional) = {iterations, ||r||^2, tol^2 ||rhs||^2}. No host synchronisation. */
+int64_t fk_sr_solve_workspace_bytes(int64_t n);
+int fk_sr_solve(const double* gram, int64_t n, double scale, double shift, const double* rhs, double tol,
+                int32_t max_iter, double* x, double* stats, void* workspace, int64_t workspace_bytes,
+                void* stream);
+/* x = scale * Y alpha (complex_values_optimizer.py:48-58 update direction);
+ * params -= lr * x when params != NULL; x written to x_out when != NULL. */
+int fk_sr_backmap(const float* o_re, const float* o_im, int64_t n_params, int64_t n_samples, const double* alpha,
+                  double scale, float lr, float* params, float* x_out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FLOWKET_GB300_H */

@@ -1,0 +1,82 @@
+"""Adjoint kernel: gradients against the oracle's autograd (float64).
+
+Tolerances: FP32 path ||g - g_ref|| / ||g_ref|| < 1e-4. BF16 path (bf16
+activations from the tensor-core forward, fp32 weights and gradients): the
+stated bound is ||g - g_ref|| / ||g_ref|| < 1e-1 with cosine similarity
+> 0.995, for random +-seeds (which maximise cancellation between samples).
+"""
+import numpy as np
+import pytest
+import torch
+
+from oracle import ar2d
+
+pytestmark = pytest.mark.gpu
+
+CASES = [((4, 4), 3, 16, True), ((3, 5), 4, 32, False), ((4, 4), 2, 64, True), ((1, 12), 4, 16, True)]
+
+
+def _setup(shape, depth, f, wn, precision, b=150, seed=0):
+    from flowket_gb300 import _lib
+    from flowket_gb300.machines import ConvNetAutoregressive2D
+    m = ConvNetAutoregressive2D(shape, depth, f, weights_normalization=wn, precision=precision, seed=seed)
+    rng = np.random.default_rng(seed + 1)
+    s = rng.choice([-1, 1], size=(b,) + shape).astype(np.int8)
+    w = rng.normal(size=(b, 2)).astype(np.float32)
+    sc = torch.as_tensor(s).cuda()
+    _, _, saved = m.forward(sc, mode=_lib.FK_AR2D_SAVE)
+    return m, s, sc, w, saved
+
+
+def _flat(m, grads):
+    return torch.cat([grads[name].reshape(-1) for name, _, _ in m.layout]).numpy()
+
+
+@pytest.mark.parametrize("shape,depth,f,wn", CASES)
+def test_gradient_fp32_matches_autograd(cuda, shape, depth, f, wn):
+    m, s, sc, w, saved = _setup(shape, depth, f, wn, "fp32")
+    got = m.backward(sc, w, saved).cpu().numpy().astype(np.float64)
+    ref = _flat(m, ar2d.weighted_gradient(m.params_dict_cpu(), s, depth, wn, w[:, 0], w[:, 1]))
+    rel = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+    assert rel < 1e-4, rel
+
+
+@pytest.mark.parametrize("shape,depth,f,wn", CASES[:2])
+def test_gradient_bf16_within_bound(cuda, shape, depth, f, wn):
+    m, s, sc, w, saved = _setup(shape, depth, f, wn, "bf16")
+    got = m.backward(sc, w, saved).cpu().numpy().astype(np.float64)
+    ref = _flat(m, ar2d.weighted_gradient(m.params_dict_cpu(), s, depth, wn, w[:, 0], w[:, 1]))
+    rel = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+    cos = got @ ref / (np.linalg.norm(got) * np.linalg.norm(ref))
+    assert rel < 1e-1 and cos > 0.995, (rel, cos)
+
+
+def test_per_sample_rows_match_autograd(cuda):
+    shape, depth, f, wn = (3, 4), 3, 16, True
+    m, s, sc, w, saved = _setup(shape, depth, f, wn, "fp32", b=130)
+    o = m.log_derivatives(sc, saved).cpu().numpy()
+    for b in (0, 77, 129):
+        e = np.zeros(130)
+        e[b] = 1.0
+        gre = _flat(m, ar2d.weighted_gradient(m.params_dict_cpu(), s, depth, wn, e, 0 * e))
+        gim = _flat(m, ar2d.weighted_gradient(m.params_dict_cpu(), s, depth, wn, 0 * e, e))
+        ref = gre + 1j * gim
+        assert np.linalg.norm(o[:, b] - ref) / np.linalg.norm(ref) < 1e-4
+    # the summed gradient is the seed-weighted sum of the rows
+    summed = m.backward(sc, w, saved).cpu().numpy()
+    np.testing.assert_allclose(o.real @ w[:, 0] + o.imag @ w[:, 1], summed, rtol=1e-3, atol=1e-5)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "bf16"])
+def test_sampler_activations_feed_the_adjoint(cuda, precision):
+    """The sampler's workspace holds the same activations as a forward pass."""
+    from flowket_gb300 import _lib
+    from flowket_gb300.machines import ConvNetAutoregressive2D
+    from flowket_gb300.samplers import FastAutoregressiveSampler
+    m = ConvNetAutoregressive2D((4, 4), 3, 16, weights_normalization=True, precision=precision, seed=2)
+    spins, lp, saved = FastAutoregressiveSampler(m, 200, seed=3).sample()
+    w = torch.randn((200, 2), device="cuda")
+    g1 = m.backward(spins, w, saved).clone()
+    _, _, saved2 = m.forward(spins, mode=_lib.FK_AR2D_SAVE)
+    g2 = m.backward(spins, w, saved2)
+    assert torch.equal(g1, g2)

@@ -1,0 +1,67 @@
+"""The C-ABI library builds, loads and exports every symbol the header declares
+(no GPU needed: nothing here launches a kernel)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    text = open(os.path.join(ROOT, "include", "flowket_gb300.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(fk_[a-z0-9_]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def built():
+    from flowket_gb300 import build
+    return build.build()
+
+
+def test_header_declares_entry_points():
+    names = _declared()
+    for must in ("fk_find_conn_heisenberg", "fk_ar2d_forward", "fk_ar2d_sample", "fk_ar2d_backward",
+                 "fk_local_energy_reduce", "fk_adam_step"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(built):
+    lib = ctypes.CDLL(built)
+    missing = [n for n in _declared() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_ctypes_binding_covers_header(built):
+    from flowket_gb300 import _lib
+    _lib.load()
+    bound = set(_lib._SIGNATURES)
+    missing = [n for n in _declared() if n not in bound]
+    assert not missing, missing
+
+
+def test_descriptor_queries_without_gpu(built):
+    from flowket_gb300 import _lib
+    from flowket_gb300.machines import ar2d_param_layout
+    lib = _lib.load()
+    for (h, w, d, f, wn) in [(4, 4, 5, 16, 0), (10, 10, 10, 32, 1), (16, 16, 20, 64, 1)]:
+        desc = _lib.Ar2dDesc(h, w, d, f, wn, 1)
+        n = lib.fk_ar2d_num_params(ctypes.byref(desc))
+        assert n == ar2d_param_layout(d, f, bool(wn))[1]
+        assert lib.fk_ar2d_workspace_bytes(ctypes.byref(desc), 4096, 1) > 0
+    # 42,756 parameters for depth 5, 16 channels without weight norm
+    assert lib.fk_ar2d_num_params(ctypes.byref(_lib.Ar2dDesc(4, 4, 5, 16, 0, 1))) == 42756
+    bad = _lib.Ar2dDesc(4, 4, 5, 24, 0, 1)
+    assert lib.fk_ar2d_num_params(ctypes.byref(bad)) < 0
+    assert b"channels" in lib.fk_last_error()
+
+
+def test_bad_arguments_are_rejected_without_launch(built):
+    from flowket_gb300 import _lib
+    lib = _lib.load()
+    st = lib.fk_find_conn_heisenberg(None, 1, 4, 4, 2, 1, 1, None, None, None, None, None)
+    assert st == -1 and b"NULL" in lib.fk_last_error()
+    st = lib.fk_adam_step(None, None, None, None, 4, 0, 1e-3, 0.9, 0.999, 1e-7, None)
+    assert st == -1

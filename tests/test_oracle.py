@@ -209,3 +209,48 @@ def test_rbm_log_derivatives_match_finite_differences():
     q["W"][2, 3] += h
     fd = (rbm.rbm_log_psi(q, s) - rbm.rbm_log_psi(p, s)) / h
     assert np.allclose(fd, o[:, 6 + 12 + 2 * 12 + 3], atol=1e-5)
+
+
+def test_oracle_gradient_matches_finite_differences():
+    """The oracle's autograd (the reference for the adjoint kernel) against
+    central differences in float64."""
+    shape, depth, f = (3, 3), 3, 8
+    params = ar2d.params_to(ar2d.init_params(shape, depth, f, True, seed=4), torch.float64)
+    rng = np.random.default_rng(7)
+    for k in params:  # biases off zero so that no relu sits on its kink
+        if k.endswith(".bias"):
+            params[k] = torch.as_tensor(rng.normal(scale=0.1, size=params[k].shape))
+    s = rng.choice([-1, 1], size=(5,) + shape).astype(np.int8)
+    wre, wim = rng.normal(size=5), rng.normal(size=5)
+    g = ar2d.weighted_gradient(params, s, depth, True, wre, wim)
+
+    def loss(p):
+        lp = ar2d.log_psi_numpy(p, s, depth, True)
+        return float(np.sum(wre * lp.real + wim * lp.imag))
+
+    for name, idx in [("cc1.c.kernel", (1, 2, 3, 4)), ("cc0.v.kernel", (2, 1, 0, 5)), ("cc2.y.g", (1,)),
+                      ("out.bias", (2,)), ("cc3.x.bias", (3,))]:
+        h = 1e-6
+        p1 = {k: v.clone() for k, v in params.items()}
+        p2 = {k: v.clone() for k, v in params.items()}
+        p1[name][idx] += h
+        p2[name][idx] -= h
+        fd = (loss(p1) - loss(p2)) / (2 * h)
+        assert fd == pytest.approx(float(g[name][idx]), rel=1e-5, abs=1e-8), name
+
+
+def test_fast_sampler_restatement_equals_slow_sampler():
+    """deepar/samplers/fast_autoregressive.py and deepar/samplers/autoregressive.py
+    draw the same samples from the same uniforms."""
+    from oracle.fast_sampler import FastSamplerCPU
+    shape, depth = (3, 4), 4
+    params = ar2d.init_params(shape, depth, 8, True, seed=2)
+    fast = FastSamplerCPU(params, shape, depth, True, dtype=torch.float64).sample(64, seed=3, offset=1)
+
+    def cond_lp(batch):
+        re, _ = ar2d.conditional_log_wave_function(ar2d.params_to(params, torch.float64), torch.as_tensor(batch),
+                                                   depth, True)
+        return 2.0 * re.detach().numpy()
+
+    slow = samplers.autoregressive_sample(cond_lp, shape, 64, seed=3, offset=1)
+    assert np.array_equal(fast, slow.astype(np.int8))
