@@ -379,7 +379,6 @@ int fk_find_conn_heisenberg(const int8_t* spins, int64_t batch, int32_t height, 
                height, width);
   FK_CHECK_ARG(dim == 1 || dim == 2, "fk_find_conn_heisenberg: dim must be 1 or 2");
   FK_CHECK_ARG(dim == 2 || width == 1, "fk_find_conn_heisenberg: a chain is passed as height=L, width=1");
-  if (batch == 0) return FK_OK;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   heisenberg_kernel<<<(unsigned)((batch + 127) / 128), 128, 0, s>>>(spins, batch, height, width, dim, pbc,
                                                                     unitary_rotation ? -2.0 : 2.0, flips, mel,
@@ -394,7 +393,6 @@ int fk_find_conn_ising(const int8_t* spins, int64_t batch, int32_t height, int32
   FK_CHECK_ARG(spins && flips && mel && use && batch >= 0, "fk_find_conn_ising: NULL buffer");
   FK_CHECK_ARG(height >= 1 && width >= 1 && height * width <= kMaxSites, "fk_find_conn_ising: lattice %dx%d",
                height, width);
-  if (batch == 0) return FK_OK;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   // width == 0 would mean a chain; chains are passed as (L, 1) with one_dim=1 when width==1 and height>1.
   int one_dim = (width == 1) ? 1 : 0;
@@ -410,7 +408,6 @@ int fk_find_conn_j1j2(const int8_t* spins, int64_t batch, int32_t height, int32_
   FK_CHECK_ARG(spins && flips && mel && use && batch >= 0, "fk_find_conn_j1j2: NULL buffer");
   FK_CHECK_ARG(height >= 2 && width >= 2 && height * width <= kMaxSites, "fk_find_conn_j1j2: lattice %dx%d",
                height, width);
-  if (batch == 0) return FK_OK;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   int n_slots = 4 * height * width + 1;
   j1j2_kernel<<<(unsigned)((batch + 127) / 128), 128, 0, s>>>(spins, batch, height, width, j2, pbc, n_slots,

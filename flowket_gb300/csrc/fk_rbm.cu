@@ -252,9 +252,9 @@ __global__ void __launch_bounds__(128) rbm_mh_kernel(const __grid_constant__ MhA
           if (f1 >= 0) s[f1] = (int8_t)-s[f1];
         }
         __syncwarp();
-        ++acc_count;
+        if (t >= a.warmup_sweeps) ++acc_count;  // warm-up moves are not counted (metropolis_hastings.py:58-64)
       }
-    } else {
+    } else if (t >= a.warmup_sweeps) {
       ++acc_count;  // the unchanged candidate is accepted (exp(0) > U)
     }
     if (t >= a.warmup_sweeps) {

@@ -245,3 +245,106 @@ def _ar2d_log_derivatives(machine, spins, saved=None):
 
 
 ConvNetAutoregressive2D.log_derivatives = _ar2d_log_derivatives
+
+
+class RBM:
+    """flowket.machines.RBM (machines/rbm.py:35-48): complex RBM with alpha*N
+    hidden units, log psi = a.s + sum_j lncosh(b_j + W_j.s). Parameters are
+    one float32 tensor of interleaved complex values [a | b | W]; real and
+    imaginary parts are initialised N(0, stddev) (rbm.py:23)."""
+
+    def __init__(self, hilbert_state_shape, alpha=1, stddev=1.0, use_float64_ops=False, seed=0, device=None,
+                 params=None):
+        if use_float64_ops:
+            raise ValueError("the GPU RBM computes in complex64 (use_float64_ops=False)")
+        self.hilbert_state_shape = tuple(int(x) for x in hilbert_state_shape)
+        self.n = int(np.prod(self.hilbert_state_shape))
+        self.m = int(alpha) * self.n
+        self.alpha = int(alpha)
+        self.device = _device(device)
+        self.num_complex_params = self.n + self.m + self.n * self.m
+        if params is None:
+            gen = torch.Generator().manual_seed(seed)
+            params = torch.randn(2 * self.num_complex_params, generator=gen, dtype=torch.float64) * stddev
+        self.params = torch.as_tensor(params, dtype=torch.float32).reshape(-1).to(self.device).contiguous()
+        assert self.params.numel() == 2 * self.num_complex_params
+        self.num_params = self.params.numel()
+
+    def params_updated(self):
+        pass
+
+    def complex_params(self):
+        c = torch.view_as_complex(self.params.view(-1, 2))
+        n, m = self.n, self.m
+        return {"a": c[:n], "b": c[n:n + m], "W": c[n + m:].view(n, m)}
+
+    def _spins(self, spins):
+        s = torch.as_tensor(spins)
+        if s.device != self.device or s.dtype != torch.int8:
+            s = s.to(device=self.device, dtype=torch.int8)
+        return s.reshape(s.shape[0], self.n).contiguous()
+
+    def log_psi_pairs(self, spins):
+        s = self._spins(spins)
+        out = torch.empty((s.shape[0], 2), dtype=torch.float32, device=self.device)
+        _lib.call("fk_rbm_log_psi", _lib.ptr(self.params), self.n, self.m, _lib.ptr(s), s.shape[0], _lib.ptr(out),
+                  _lib.stream_ptr())
+        return out
+
+    def log_psi(self, spins):
+        lp = self.log_psi_pairs(spins)
+        return torch.complex(lp[:, 0], lp[:, 1])
+
+    def predict(self, spins, batch_size=None):
+        return self.log_psi(spins).unsqueeze(1)
+
+    __call__ = predict
+
+    def local_energy(self, operator, spins):
+        flips, mel, use, s = operator.enumerate(spins)
+        local = torch.empty((s.shape[0], 2), dtype=torch.float64, device=self.device)
+        _lib.call("fk_rbm_local_energy", _lib.ptr(self.params), self.n, self.m, _lib.ptr(s), s.shape[0],
+                  _lib.ptr(flips), _lib.ptr(mel), _lib.ptr(use), mel.shape[0], _lib.ptr(local), _lib.stream_ptr())
+        return local
+
+    def log_derivatives_split(self, spins):
+        """(O_re, O_im) parameter-major (num_complex_params, B)."""
+        s = self._spins(spins)
+        b = s.shape[0]
+        o_re = torch.empty((self.num_complex_params, b), dtype=torch.float32, device=self.device)
+        o_im = torch.empty_like(o_re)
+        _lib.call("fk_rbm_log_derivatives", _lib.ptr(self.params), self.n, self.m, _lib.ptr(s), b, _lib.ptr(o_re),
+                  _lib.ptr(o_im), _lib.stream_ptr())
+        return o_re, o_im
+
+    def log_derivatives(self, spins):
+        o_re, o_im = self.log_derivatives_split(spins)
+        return torch.complex(o_re, o_im)
+
+
+class RBMSym(RBM):
+    """flowket.machines.RBMSym (machines/rbm.py:51-65): translation-invariant
+    kernel (shape + (alpha,)), a single visible bias; evaluated through the
+    dense RBM kernels after expanding every translation of the bare kernel
+    (layers/complex/dense.py:53-85: column f*T + t, bias repeated)."""
+
+    def __init__(self, hilbert_state_shape, alpha=1, stddev=1.0, use_float64_ops=False, seed=0, device=None):
+        shape = tuple(int(x) for x in hilbert_state_shape)
+        n = int(np.prod(shape))
+        gen = torch.Generator().manual_seed(seed)
+        bare_w = torch.complex(torch.randn(shape + (alpha,), generator=gen, dtype=torch.float64) * stddev,
+                               torch.randn(shape + (alpha,), generator=gen, dtype=torch.float64) * stddev)
+        bare_b = torch.complex(torch.randn(alpha, generator=gen, dtype=torch.float64) * stddev,
+                               torch.randn(alpha, generator=gen, dtype=torch.float64) * stddev)
+        bare_a = torch.complex(torch.randn(1, generator=gen, dtype=torch.float64) * stddev,
+                               torch.randn(1, generator=gen, dtype=torch.float64) * stddev)
+        self.bare = {"W": bare_w, "b": bare_b, "a": bare_a}
+        import itertools
+        dims = tuple(range(len(shape)))
+        trans = [torch.roll(bare_w, t, dims) for t in itertools.product(*[range(d) for d in shape])]
+        w = torch.stack(trans, dim=-1).reshape(n, alpha * len(trans))
+        b = bare_b.repeat_interleave(n)
+        a = bare_a.expand(n)
+        full = torch.cat([a, b, w.reshape(-1)])
+        super().__init__(shape, alpha=alpha, device=device,
+                         params=torch.view_as_real(full).reshape(-1).to(torch.float32))

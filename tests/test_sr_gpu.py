@@ -1,0 +1,72 @@
+"""Kernel set (d): sample-space SR against the oracle's parameter-space solve."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import ar2d, sr as ref_sr
+
+pytestmark = pytest.mark.gpu
+
+
+def test_gram_and_solve_match_numpy(cuda):
+    from flowket_gb300 import _lib
+    rng = np.random.default_rng(0)
+    p, b = 3000, 96
+    a = rng.normal(size=(p, b)).astype(np.float32)
+    c = rng.normal(size=(p, b)).astype(np.float32)
+    ta, tc = torch.as_tensor(a).cuda(), torch.as_tensor(c).cuda()
+    n = 2 * b
+    gram = torch.empty((n, n), dtype=torch.float64, device="cuda")
+    _lib.call("fk_sr_gram", _lib.ptr(ta), _lib.ptr(tc), p, b, _lib.ptr(gram), n * n, _lib.stream_ptr())
+    y = np.concatenate([a, c], axis=1).astype(np.float64)
+    want = y.T @ y
+    np.testing.assert_allclose(gram.cpu().numpy(), want, rtol=1e-5, atol=1e-3)
+    rhs = torch.as_tensor(rng.normal(size=n)).cuda()
+    x = torch.empty(n, dtype=torch.float64, device="cuda")
+    stats = torch.zeros(3, dtype=torch.float64, device="cuda")
+    ws = torch.empty(_lib.load().fk_sr_solve_workspace_bytes(n), dtype=torch.uint8, device="cuda")
+    _lib.call("fk_sr_solve", _lib.ptr(gram), n, 1.0 / p, 0.05, _lib.ptr(rhs), 1e-12, 500, _lib.ptr(x),
+              _lib.ptr(stats), _lib.ptr(ws), ws.numel(), _lib.stream_ptr())
+    ref = np.linalg.solve(want / p + 0.05 * np.eye(n), rhs.cpu().numpy())
+    np.testing.assert_allclose(x.cpu().numpy(), ref, rtol=1e-8, atol=1e-10)
+    assert 0 < stats[0].item() <= 500
+
+
+def test_sr_direction_matches_parameter_space_solve(cuda):
+    """(Re<O_c^* O_c> + lambda) x = Re<O_c^* E_c>: the sample-space GPU solve
+    equals the oracle's parameter-space solve on the same O and E_loc."""
+    from flowket_gb300 import _lib
+    from flowket_gb300.machines import ConvNetAutoregressive2D
+    from flowket_gb300.operators import Heisenberg
+    from flowket_gb300.observables import Observable
+    from flowket_gb300.optimizers import ComplexValuesStochasticReconfiguration
+    shape, depth, f = (3, 4), 2, 16
+    m = ConvNetAutoregressive2D(shape, depth, f, weights_normalization=False, precision="fp32", seed=1)
+    rng = np.random.default_rng(2)
+    s = torch.as_tensor(rng.choice([-1, 1], size=(100,) + shape).astype(np.int8)).cuda()
+    _, _, saved = m.forward(s, mode=_lib.FK_AR2D_SAVE)
+    local = Observable(Heisenberg(hilbert_state_shape=shape, pbc=True)).local_values(m, s)
+    opt = ComplexValuesStochasticReconfiguration(m, lr=0.05, diag_shift=1e-2, iterative_solver=False)
+    x = opt.direction(s, local, saved).cpu().numpy().astype(np.float64)
+    o = m.log_derivatives(s, saved).cpu().numpy().T.astype(np.complex128)
+    e = local[:, 0].cpu().numpy() + 1j * local[:, 1].cpu().numpy()
+    want = ref_sr.sr_real(o, e, 1e-2)
+    assert np.linalg.norm(x - want) / np.linalg.norm(want) < 1e-3
+
+
+def test_vmc_with_sr_lowers_energy(cuda):
+    from flowket_gb300.machines import ConvNetAutoregressive2D
+    from flowket_gb300.operators import Heisenberg
+    from flowket_gb300.optimization import VariationalMonteCarlo
+    from flowket_gb300.optimizers import ComplexValuesStochasticReconfiguration
+    from flowket_gb300.samplers import FastAutoregressiveSampler
+    shape = (4, 4)
+    m = ConvNetAutoregressive2D(shape, 3, 16, weights_normalization=True, precision="fp32", seed=0)
+    vmc = VariationalMonteCarlo(m, Heisenberg(hilbert_state_shape=shape, pbc=True),
+                                FastAutoregressiveSampler(m, 256, seed=3))
+    opt = ComplexValuesStochasticReconfiguration(m, lr=0.05, diag_shift=1e-3)
+    energies = []
+    for _ in range(30):
+        vmc.step(opt)
+        energies.append(vmc.current_energy.real)
+    assert np.mean(energies[-5:]) < np.mean(energies[:3]) - 1.0
