@@ -54,7 +54,33 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--fp32-steps", type=int, default=2)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--case", default="vmc", choices=["vmc", "forward"],
+                   help="forward: only the batched AR2D forward of the local-energy stage on --configs "
+                        "connected configurations (the small case used for ncu captures)")
+    p.add_argument("--configs", type=int, default=32768)
     return p.parse_args()
+
+
+def forward_case(args):
+    """The AR2D forward of the local-energy stage alone, on `configs`
+    configurations of the bench workload's network."""
+    from flowket_gb300.machines import ConvNetAutoregressive2D
+    m = ConvNetAutoregressive2D(SHAPE, DEPTH, CHANNELS, weights_normalization=True, precision="bf16", seed=0)
+    g = torch.Generator(device="cuda").manual_seed(0)
+    spins = (2 * torch.randint(0, 2, (args.configs,) + SHAPE, device="cuda", generator=g) - 1).to(torch.int8)
+    for _ in range(args.warmup):
+        m.forward(spins)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(args.steps):
+        m.forward(spins)
+    b.record()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / args.steps
+    fl = flops_per_sample_forward(SHAPE, DEPTH, CHANNELS) * args.configs
+    print(json.dumps({"case": "forward", "configs": args.configs, "ms_per_forward": ms,
+                      "tflops": fl / (ms / 1e3) / 1e12}), flush=True)
 
 
 def dist_init(n):
@@ -311,7 +337,9 @@ def ours_arm(args, rank, world):
 def main():
     args = parse()
     rank, world = dist_init(args.gpus)
-    if args.impl == "reference":
+    if args.case == "forward":
+        forward_case(args)
+    elif args.impl == "reference":
         reference_arm(args, rank, world)
     else:
         ours_arm(args, rank, world)

@@ -25,6 +25,7 @@
 #include "fk_ar2d.cuh"
 
 #include <math.h>
+#include <stdlib.h>
 #include <string.h>
 
 namespace fk {
@@ -767,6 +768,18 @@ static int launch_op(const OpArgs& a, int64_t tiles, int H, int W, int* err, cud
   return check_cuda(launched(), "op_row_kernel");
 }
 
+// FK_AR2D_ENGINE=rowwise selects the per-pixel engine for every op (the
+// pipelined engine computes bitwise the same values; the switch lets tests
+// compare the two).
+static bool use_pipe_engine() {
+  static int v = -1;
+  if (v < 0) {
+    const char* e = getenv("FK_AR2D_ENGINE");
+    v = (e && strcmp(e, "rowwise") == 0) ? 0 : 1;
+  }
+  return v == 1;
+}
+
 template <int F, bool TC>
 static int forward_impl(const NetLayout& L, const void* packed, const int8_t* spins, int64_t batch,
                         float* log_psi, float* cond, const Tensors& T, int mode, cudaStream_t s) {
@@ -781,7 +794,11 @@ static int forward_impl(const NetLayout& L, const void* packed, const int8_t* sp
       ops[2].cond = cond;
     }
     for (int k = 0; k < 3; ++k) {
-      int st = launch_op<F, TC>(ops[k], tiles, L.H, L.W, err, s);
+      int st;
+      if (TC && F <= 32 && !ops[k].first && use_pipe_engine())
+        st = launch_pipe_op(F, ops[k], tiles, L.H, L.W, err, s);
+      else
+        st = launch_op<F, TC>(ops[k], tiles, L.H, L.W, err, s);
       if (st != FK_OK) return st;
     }
   }

@@ -137,6 +137,9 @@ __device__ __forceinline__ float spin_at(const int8_t* spins, int64_t batch, int
 }
 
 int64_t tensor_bytes(const NetLayout& L, int64_t tiles, int channels);
+// Pipelined persistent tensor-core engine (fk_ar2d_pipe.cu) for the ops after
+// the first layer with F <= 32; FK_ERR_ARG when the op is not supported.
+int launch_pipe_op(int F, const OpArgs& a, int64_t tiles, int H, int W, int* err, cudaStream_t s);
 int64_t workspace_layout(const NetLayout& L, int64_t batch, int mode, char* base, Tensors* T);
 
 }  // namespace fk

@@ -126,3 +126,25 @@ def test_sampler_matches_exact_distribution(cuda, precision):
     y = np.bincount(exact.states_to_index(ref), minlength=512)
     z = ((np.square(x - y) - x - y) / (x + y + 1e-20)).sum()
     assert z <= np.sqrt(n), z
+
+
+@pytest.mark.parametrize("f", [16, 32])
+def test_pipelined_engine_equals_per_pixel_engine(cuda, f, tmp_path):
+    """The persistent pipelined tensor-core engine and the per-pixel engine
+    give bitwise the same log psi (same MMA sequence, same epilogue)."""
+    import subprocess
+    import sys
+    code = (
+        "import sys, numpy as np, torch; sys.path.insert(0, %r);"
+        "from flowket_gb300.machines import ConvNetAutoregressive2D;"
+        "m = ConvNetAutoregressive2D((5, 7), 4, %d, weights_normalization=True, precision='bf16', seed=3);"
+        "s = torch.as_tensor(np.random.default_rng(9).choice([-1, 1], size=(700, 5, 7)).astype(np.int8)).cuda();"
+        "np.save(%r, m.log_psi(s).cpu().numpy())"
+    ) % (str(__import__("os").path.dirname(__import__("os").path.dirname(__file__))), f, str(tmp_path / "a.npy"))
+    env = dict(__import__("os").environ, FK_AR2D_ENGINE="rowwise")
+    subprocess.run([sys.executable, "-c", code], check=True, env=env)
+    ref = np.load(tmp_path / "a.npy")
+    m = _machine((5, 7), 4, f, True, "bf16", seed=3)
+    s = torch.as_tensor(np.random.default_rng(9).choice([-1, 1], size=(700, 5, 7)).astype(np.int8)).cuda()
+    got = m.log_psi(s).cpu().numpy()
+    assert np.array_equal(got, ref)
