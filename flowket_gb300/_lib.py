@@ -49,6 +49,9 @@ _SIGNATURES = {
     "fk_ar2d_workspace_bytes": (c_i64, [c_p, c_i64, c_i32]),
     "fk_ar2d_forward": (c_i32, [c_p, c_p, c_p, c_i64, c_p, c_p, c_p, c_i64, c_i32, c_p]),
     "fk_ar2d_sample": (c_i32, [c_p, c_p, c_i64, c_u64, c_u64, c_p, c_p, c_p, c_i64, c_p]),
+    "fk_ar2d_connections_workspace_bytes": (c_i64, [c_p, c_i64, c_i64]),
+    "fk_ar2d_forward_connections": (c_i32, [c_p, c_p, c_p, c_p, c_p, c_i64, c_p, c_i64, c_i64, c_p, c_p, c_i64,
+                                            c_i64, c_p]),
     "fk_ar2d_backward_workspace_bytes": (c_i64, [c_p, c_i64]),
     "fk_ar2d_backward": (c_i32, [c_p, c_p, c_p, c_p, c_i64, c_p, c_p, c_i64, c_p, c_i64, c_p, c_p, c_p]),
     "fk_axpy": (c_i32, [c_i64, c_f32, c_p, c_p, c_p]),

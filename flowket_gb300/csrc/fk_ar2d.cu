@@ -616,8 +616,13 @@ __global__ void __launch_bounds__(128) op_row_kernel(const __grid_constant__ OpA
   using T = typename std::conditional<TC, __nv_bfloat16, float>::type;
   extern __shared__ __align__(1024) uint8_t smem[];
   const int P = H * W;
-  const int64_t tile = blockIdx.x / H;
-  const int r = blockIdx.x % H;
+  int64_t item = blockIdx.x;
+  if (a.items) {
+    if ((int)blockIdx.x >= *a.n_items) return;
+    item = a.items[blockIdx.x];
+  }
+  const int64_t tile = item / H;
+  const int r = (int)(item % H);
   TcSmem s;
   TcState st;
   if (TC) {
@@ -795,7 +800,7 @@ static int forward_impl(const NetLayout& L, const void* packed, const int8_t* sp
     }
     for (int k = 0; k < 3; ++k) {
       int st;
-      if (TC && F <= 32 && !ops[k].first && use_pipe_engine())
+      if (TC && pipe_supported(F, L.W) && !ops[k].first && use_pipe_engine())
         st = launch_pipe_op(F, ops[k], tiles, L.H, L.W, err, s);
       else
         st = launch_op<F, TC>(ops[k], tiles, L.H, L.W, err, s);
@@ -932,6 +937,234 @@ static int sample_impl(const NetLayout& L, const void* packed, int64_t batch, ui
   return check_cuda(launched(), "row_reduce_kernel");
 }
 
+
+// ============================================================== causal reuse
+// Connected configurations of a sample differ from it only at their flipped
+// sites. Every activation of the network at a pixel depends on spins at that
+// pixel's row and above (vertical stream) or earlier in raster order
+// (horizontal stream), so for a configuration whose first flipped site is on
+// row rk all rows < rk of every layer equal the base sample's. The
+// configurations are sorted by rk; a tile of 128 starting at rk evaluates rows
+// >= rk only, takes rows rk-2..rk of the tensors its 3-row taps read from the
+// base sample's saved activations, and sums the log psi partials of rows < rk
+// from the base. The result is bitwise that of a full forward.
+
+__global__ void conn_rk_kernel(const short2* __restrict__ cflips, int64_t n, int H, int W, int32_t* __restrict__ rk,
+                               int32_t* __restrict__ hist) {
+  int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  short2 f = cflips[j];
+  int r0 = f.x >= 0 ? f.x / W : H;
+  int r1 = f.y >= 0 ? f.y / W : H;
+  int r = r0 < r1 ? r0 : r1;
+  if (r >= H) r = 0;  // no flipped site: evaluate every row
+  rk[j] = r;
+  atomicAdd(&hist[r], 1);
+}
+
+__global__ void conn_bucket_kernel(const int32_t* __restrict__ hist, int H, int32_t* __restrict__ cursor) {
+  int run = 0;
+  for (int r = 0; r < H; ++r) {
+    cursor[r] = run;
+    run += hist[r];
+  }
+}
+
+__global__ void conn_scatter_kernel(const int32_t* __restrict__ rk, int64_t n, int32_t* __restrict__ cursor,
+                                    int32_t* __restrict__ perm, int32_t* __restrict__ srk) {
+  int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  int r = rk[j];
+  int pos = atomicAdd(&cursor[r], 1);
+  perm[pos] = (int32_t)j;
+  srk[pos] = r;
+}
+
+// chunk rows [j0, j0+n): configurations and owners in sorted order
+__global__ void conn_gather_configs_kernel(const int8_t* __restrict__ configs, const int32_t* __restrict__ owner,
+                                           const int32_t* __restrict__ perm, int64_t j0, int64_t n, int P,
+                                           int8_t* __restrict__ cfg, int32_t* __restrict__ cown) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * P) return;
+  int64_t j = t / P;
+  int k = (int)(t - j * P);
+  int64_t src = perm[j0 + j];
+  cfg[t] = configs[src * P + k];
+  if (k == 0) cown[j] = owner[src];
+}
+
+// Work list of the chunk: item = tile * H + r for r >= rk_start(tile).
+__global__ void conn_items_kernel(const int32_t* __restrict__ srk, int64_t j0, int64_t n, int H,
+                                  int32_t* __restrict__ rk_start, int32_t* __restrict__ items,
+                                  int32_t* __restrict__ n_items) {
+  __shared__ int32_t part[1024];
+  const int tiles = (int)((n + kTile - 1) / kTile);
+  const int per = (tiles + blockDim.x - 1) / blockDim.x;
+  const int lo = threadIdx.x * per, hi = lo + per < tiles ? lo + per : tiles;
+  int cnt = 0;
+  for (int t = lo; t < hi; ++t) {
+    int r = srk[j0 + (int64_t)t * kTile];
+    rk_start[t] = r;
+    cnt += H - r;
+  }
+  part[threadIdx.x] = cnt;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int run = 0;
+    for (int i = 0; i < (int)blockDim.x; ++i) {
+      int v = part[i];
+      part[i] = run;
+      run += v;
+    }
+    *n_items = run;
+  }
+  __syncthreads();
+  int off = part[threadIdx.x];
+  for (int t = lo; t < hi; ++t)
+    for (int r = rk_start[t]; r < H; ++r) items[off++] = t * H + r;
+}
+
+// Rows rk-2..rk-1 of the V stream and of Cat's X half, rows rk-2..rk of Cat's
+// Y half, copied from the owner's base activations. Grid: (tile, 3 rows, W).
+template <typename T>
+__global__ void conn_gather_rows_kernel(const int32_t* __restrict__ rk_start, const int32_t* __restrict__ cown,
+                                        int64_t n, int H, int W, int F, const T* __restrict__ base_v,
+                                        const T* __restrict__ base_cat, T* __restrict__ v_out, T* __restrict__ cat_out) {
+  const int64_t tile = blockIdx.x;
+  const int slot = blockIdx.y;  // 0, 1, 2 -> rows rk-2, rk-1, rk
+  const int c = blockIdx.z;
+  const int m = threadIdx.x;
+  const int rk = rk_start[tile];
+  const int r = rk - 2 + slot;
+  if (r < 0 || r >= H) return;
+  const int64_t j = tile * kTile + m;
+  if (j >= n) return;
+  const int64_t b = cown[j];
+  const int64_t tb = b / kTile;
+  const int lb = (int)(b % kTile);
+  const int P = H * W, pix = r * W + c;
+  const int G = F / 8;
+  const T* sv = base_v ? base_v + ((tb * P + pix) * (int64_t)F) * kTile : nullptr;
+  const T* sc = base_cat + ((tb * P + pix) * (int64_t)F) * kTile;
+  T* dv = v_out ? v_out + ((tile * P + pix) * (int64_t)F) * kTile : nullptr;
+  T* dc = cat_out + ((tile * P + pix) * (int64_t)F) * kTile;
+  constexpr int E = 16 / sizeof(T);  // elements per 16 bytes
+  for (int g = 0; g < G; ++g) {
+    const bool y_half = g >= G / 2;
+    for (int e = 0; e < 8; e += E) {
+      if (r < rk || y_half) {
+        *reinterpret_cast<uint4*>(dc + ((int64_t)g * kTile + m) * 8 + e) =
+            *reinterpret_cast<const uint4*>(sc + ((int64_t)g * kTile + lb) * 8 + e);
+      }
+      if (r < rk && dv) {
+        *reinterpret_cast<uint4*>(dv + ((int64_t)g * kTile + m) * 8 + e) =
+            *reinterpret_cast<const uint4*>(sv + ((int64_t)g * kTile + lb) * 8 + e);
+      }
+    }
+  }
+}
+
+__global__ void conn_reduce_kernel(const float2* __restrict__ part, const float2* __restrict__ base_part,
+                                   const int32_t* __restrict__ rk_start, const int32_t* __restrict__ cown,
+                                   const int32_t* __restrict__ perm, int64_t j0, int64_t n, int H,
+                                   float2* __restrict__ out) {
+  int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const int64_t tile = j / kTile;
+  const int m = (int)(j % kTile);
+  const int rk = rk_start[tile];
+  const int64_t b = cown[j];
+  const int64_t tb = b / kTile;
+  const int lb = (int)(b % kTile);
+  Kahan re, im;
+  for (int r = 0; r < H; ++r) {
+    float2 p = r < rk ? base_part[(tb * H + r) * kTile + lb] : part[(tile * H + r) * kTile + m];
+    re.add(p.x);
+    im.add(p.y);
+  }
+  out[perm[j0 + j]] = make_float2(re.s - re.c, im.s - im.c);
+}
+
+struct ConnScratch {
+  int32_t *rk, *perm, *srk, *hist, *cursor, *cown, *rk_start, *items, *n_items;
+  int8_t* cfg;
+  int64_t bytes;
+};
+
+static int64_t conn_layout(const NetLayout& L, int64_t max_rows, int64_t chunk, char* base, Tensors* T,
+                           ConnScratch* S) {
+  int64_t off = workspace_layout(L, chunk, FK_AR2D_INFER, base, T);
+  auto take = [&](int64_t bytes) -> char* {
+    char* p = base ? base + off : nullptr;
+    off += (bytes + 255) / 256 * 256;
+    return p;
+  };
+  ConnScratch tmp;
+  ConnScratch* s = S ? S : &tmp;
+  const int64_t tiles = (chunk + kTile - 1) / kTile;
+  s->rk = reinterpret_cast<int32_t*>(take(max_rows * 4));
+  s->perm = reinterpret_cast<int32_t*>(take(max_rows * 4));
+  s->srk = reinterpret_cast<int32_t*>(take(max_rows * 4));
+  s->hist = reinterpret_cast<int32_t*>(take((L.H + 1) * 4));
+  s->cursor = reinterpret_cast<int32_t*>(take((L.H + 1) * 4));
+  s->cown = reinterpret_cast<int32_t*>(take(chunk * 4));
+  s->rk_start = reinterpret_cast<int32_t*>(take(tiles * 4));
+  s->items = reinterpret_cast<int32_t*>(take(tiles * L.H * 4));
+  s->n_items = reinterpret_cast<int32_t*>(take(4));
+  s->cfg = reinterpret_cast<int8_t*>(take(chunk * L.P));
+  s->bytes = off;
+  return off;
+}
+
+template <int F, bool TC>
+static int connections_impl(const NetLayout& L, const void* packed, const int8_t* configs, const int32_t* owner,
+                            const int16_t* cflips, int64_t n_rows, const Tensors& B, float* log_psi,
+                            const Tensors& T, const ConnScratch& S, int64_t chunk, cudaStream_t s) {
+  using Tv = typename std::conditional<TC, __nv_bfloat16, float>::type;
+  int* err = device_error_word();
+  FK_CUDA(cudaMemsetAsync(S.hist, 0, (L.H + 1) * 4, s));
+  conn_rk_kernel<<<(unsigned)((n_rows + 255) / 256), 256, 0, s>>>(reinterpret_cast<const short2*>(cflips), n_rows,
+                                                                  L.H, L.W, S.rk, S.hist);
+  conn_bucket_kernel<<<1, 1, 0, s>>>(S.hist, L.H, S.cursor);
+  conn_scatter_kernel<<<(unsigned)((n_rows + 255) / 256), 256, 0, s>>>(S.rk, n_rows, S.cursor, S.perm, S.srk);
+  FK_CUDA(launched(3));
+  for (int64_t j0 = 0; j0 < n_rows; j0 += chunk) {
+    const int64_t n = n_rows - j0 < chunk ? n_rows - j0 : chunk;
+    const int64_t tiles = (n + kTile - 1) / kTile;
+    conn_gather_configs_kernel<<<(unsigned)((n * L.P + 255) / 256), 256, 0, s>>>(configs, owner, S.perm, j0, n,
+                                                                                 L.P, S.cfg, S.cown);
+    conn_items_kernel<<<1, 1024, 0, s>>>(S.srk, j0, n, L.H, S.rk_start, S.items, S.n_items);
+    FK_CUDA(launched(2));
+    for (int i = 0; i < L.n_cc; ++i) {
+      CCTensors x = cc_tensors(L, T, FK_AR2D_INFER, i);
+      const bool last = i == L.n_cc - 1;
+      dim3 g((unsigned)tiles, 3, (unsigned)L.W);
+      conn_gather_rows_kernel<Tv><<<g, kTile, 0, s>>>(
+          S.rk_start, S.cown, n, L.H, L.W, F, last ? nullptr : static_cast<const Tv*>(B.v[i]),
+          static_cast<const Tv*>(B.cat[i]), last ? nullptr : static_cast<Tv*>(x.vout), static_cast<Tv*>(x.cat));
+      FK_CUDA(launched());
+      OpArgs ops[3];
+      make_ops(L, packed, i, S.cfg, n, x.vin, x.hin, x.vres, x.hres, x.vout, x.hout, x.cat, nullptr, nullptr, ops);
+      for (int k = 0; k < 3; ++k) {
+        ops[k].items = S.items;
+        ops[k].n_items = S.n_items;
+        if (last && k == 2) ops[k].row_partial = T.row_partial;
+        int st;
+        if (TC && pipe_supported(F, L.W) && !ops[k].first && use_pipe_engine())
+          st = launch_pipe_op(F, ops[k], tiles, L.H, L.W, err, s);
+        else
+          st = launch_op<F, TC>(ops[k], tiles, L.H, L.W, err, s);
+        if (st != FK_OK) return st;
+      }
+    }
+    conn_reduce_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(T.row_partial, B.row_partial, S.rk_start, S.cown,
+                                                                  S.perm, j0, n, L.H,
+                                                                  reinterpret_cast<float2*>(log_psi));
+    FK_CUDA(launched());
+  }
+  return FK_OK;
+}
+
 }  // namespace fk
 
 using namespace fk;
@@ -1018,6 +1251,45 @@ int fk_ar2d_sample(const fk_ar2d_desc* desc, const void* packed, int64_t batch, 
                        : sample_impl<32, false>(L, packed, batch, seed, offset, spins, log_psi, T, s);
     default: return tc ? sample_impl<64, true>(L, packed, batch, seed, offset, spins, log_psi, T, s)
                        : sample_impl<64, false>(L, packed, batch, seed, offset, spins, log_psi, T, s);
+  }
+}
+
+
+int64_t fk_ar2d_connections_workspace_bytes(const fk_ar2d_desc* desc, int64_t max_rows, int64_t chunk) {
+  NetLayout L;
+  if (build_layout(desc, &L) != FK_OK || max_rows < 0 || chunk <= 0) return -1;
+  return conn_layout(L, max_rows, chunk, nullptr, nullptr, nullptr);
+}
+
+int fk_ar2d_forward_connections(const fk_ar2d_desc* desc, const void* packed, const int8_t* configs,
+                                const int32_t* owner, const int16_t* cflips, int64_t n_rows, const void* base_saved,
+                                int64_t base_saved_bytes, int64_t base_batch, float* log_psi, void* workspace,
+                                int64_t workspace_bytes, int64_t chunk, void* stream) {
+  NetLayout L;
+  int st = build_layout(desc, &L);
+  if (st != FK_OK) return st;
+  FK_CHECK_ARG(chunk > 0 && chunk % kTile == 0, "fk_ar2d_forward_connections: chunk must be a multiple of 128");
+  if (n_rows == 0) return FK_OK;
+  FK_CHECK_ARG(packed && configs && owner && cflips && base_saved && log_psi && n_rows > 0 && base_batch > 0,
+               "fk_ar2d_forward_connections: NULL buffer");
+  Tensors B;
+  int64_t need = workspace_layout(L, base_batch, FK_AR2D_SAVE, static_cast<char*>(const_cast<void*>(base_saved)), &B);
+  FK_CHECK_ARG(base_saved_bytes >= need, "fk_ar2d_forward_connections: base workspace %lld < %lld bytes",
+               (long long)base_saved_bytes, (long long)need);
+  Tensors T;
+  ConnScratch S;
+  int64_t wneed = conn_layout(L, n_rows, chunk, static_cast<char*>(workspace), &T, &S);
+  FK_CHECK_ARG(workspace && workspace_bytes >= wneed, "fk_ar2d_forward_connections: workspace %lld < %lld bytes",
+               (long long)workspace_bytes, (long long)wneed);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const bool tc = L.precision == FK_PRECISION_BF16;
+  switch (L.F) {
+    case 16: return tc ? connections_impl<16, true>(L, packed, configs, owner, cflips, n_rows, B, log_psi, T, S, chunk, s)
+                       : connections_impl<16, false>(L, packed, configs, owner, cflips, n_rows, B, log_psi, T, S, chunk, s);
+    case 32: return tc ? connections_impl<32, true>(L, packed, configs, owner, cflips, n_rows, B, log_psi, T, S, chunk, s)
+                       : connections_impl<32, false>(L, packed, configs, owner, cflips, n_rows, B, log_psi, T, S, chunk, s);
+    default: return tc ? connections_impl<64, true>(L, packed, configs, owner, cflips, n_rows, B, log_psi, T, S, chunk, s)
+                       : connections_impl<64, false>(L, packed, configs, owner, cflips, n_rows, B, log_psi, T, S, chunk, s);
   }
 }
 

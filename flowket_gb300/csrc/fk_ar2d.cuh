@@ -65,6 +65,10 @@ struct OpArgs {
   float2* row_partial;  // last C: [tiles][H][128] log psi partial per row
   float* cond;          // last C: [batch][P][4] normalised conditionals (optional)
   int64_t batch;
+  // Optional work list: item k = tile * H + row for k < *n_items (row-suffix
+  // evaluation of connected configurations); NULL = every (tile, row).
+  const int32_t* items;
+  const int32_t* n_items;
 };
 
 // Workspace tensors of one forward.
@@ -140,6 +144,7 @@ int64_t tensor_bytes(const NetLayout& L, int64_t tiles, int channels);
 // Pipelined persistent tensor-core engine (fk_ar2d_pipe.cu) for the ops after
 // the first layer with F <= 32; FK_ERR_ARG when the op is not supported.
 int launch_pipe_op(int F, const OpArgs& a, int64_t tiles, int H, int W, int* err, cudaStream_t s);
+bool pipe_supported(int F, int W);
 int64_t workspace_layout(const NetLayout& L, int64_t batch, int mode, char* base, Tensors* T);
 
 }  // namespace fk

@@ -34,16 +34,21 @@ __device__ __forceinline__ void store_g(float* t, int64_t tile, int P, int pix, 
   store_row(blk<float>(t, tile, P, pix, C), m, c0, n, v);
 }
 
-// acc[ci] += sum_n g[n] W[row0 + ci][n]  (W fp32 [K][N] row-major)
+// acc[ci] += sum_n g[n] W[row0 + ci][n]  (W fp32 [K][N] row-major, rows
+// 16-byte aligned: one vector load per four FMAs)
 template <int CI, int N>
 __device__ __forceinline__ void dot_rows(const float* __restrict__ W, int row0, const float* g, float* acc) {
 #pragma unroll 4
   for (int ci = 0; ci < CI; ++ci) {
-    const float* w = W + (int64_t)(row0 + ci) * N;
-    float s = 0.f;
+    const float4* w = reinterpret_cast<const float4*>(W + (int64_t)(row0 + ci) * N);
+    float s0 = 0.f, s1 = 0.f;
 #pragma unroll
-    for (int n = 0; n < N; ++n) s += g[n] * __ldg(w + n);
-    acc[ci] += s;
+    for (int n4 = 0; n4 < N / 4; ++n4) {
+      float4 v = __ldg(w + n4);
+      s0 += g[4 * n4] * v.x + g[4 * n4 + 2] * v.z;
+      s1 += g[4 * n4 + 1] * v.y + g[4 * n4 + 3] * v.w;
+    }
+    acc[ci] += s0 + s1;
   }
 }
 

@@ -5,15 +5,17 @@
 // row of 128 samples. Six warps:
 //   warp 0 (one thread): TMA producer. Loads the op's weights once, then every
 //       input column (the 3 rows r-2..r -- 1 row for the H op -- of one lattice
-//       column, one bulk copy per [F/8][128][8] block) into a 4-slot ring;
+//       column, one bulk copy per [F/8][128][8] block) into a 7-8 slot ring;
 //   warp 1 (one thread): MMA issuer. Per pixel, tcgen05.mma over the in-bounds
 //       taps (K = 16 steps) into one of two TMEM accumulators, commits the
 //       accumulator to the epilogue and every column whose last pixel this was
 //       back to the producer; then the chained 1x1 MMA of the previous pixel
 //       on the epilogue's staged bf16 activations;
-//   warps 2-5: epilogue (thread = sample, TMEM lane quarter = warp % 4):
-//       bias, relu, residual, stream store, chained-conv staging, and the
-//       second half after the chained MMA.
+//   warps 2-9: epilogue in two groups of four warps taking alternate pixels
+//       (thread = sample, TMEM lane quarter = warp % 4): bias, relu, residual
+//       (prefetched before the accumulator wait), stream store, chained-conv
+//       staging, and the second half after the chained MMA; the head's log psi
+//       partials are summed in pixel order through shared memory.
 // A pixel loads one new column instead of nine taps, and loads, MMAs and
 // epilogues of consecutive pixels overlap. The MMA sequence of a pixel (taps
 // ascending, K steps ascending) and the epilogue arithmetic are those of the
@@ -25,13 +27,20 @@ namespace fk {
 template <int F>
 struct PipeCfg {
   static constexpr int kBlk = kTile * F * 2;
-  static constexpr int kNcol = 4;
+  // Column ring depth: a column is requested when the column kNcol places
+  // earlier is released, i.e. kNcol - 2 pixels before its first use.
+  static constexpr int kNcol = F <= 16 ? 8 : 7;
   static constexpr int kRing = 3 * kNcol * kBlk;
   static constexpr int kW = 9 * F * F * 2;
   static constexpr int kCW = F * 32 * 2;
-  static constexpr int kCA = 2 * kTile * F * 2;
-  static constexpr int kBars = 256;
-  static constexpr int kSmem = kRing + kW + kCW + kCA + kBars;
+  static constexpr int kGroups = 2;                 // epilogue groups (alternate pixels)
+  static constexpr int kNB = kGroups;               // TMEM / staging buffers (one per group)
+  static constexpr int kCA = kNB * kTile * F * 2;   // staged chained-conv inputs
+  static constexpr int kBias = 64 * 4;              // main (F) + chained (<= 32) biases
+  static constexpr int kBars = 512;
+  static constexpr int kMaxW = 16;                  // head partials [W][128] float2
+  static constexpr int kSmemBase = kRing + kW + kCW + kCA + kBias + kBars;
+  static int head_bytes(int w) { return w * kTile * 8; }
 };
 
 __device__ __forceinline__ bool pwait(uint64_t* bar, uint32_t parity, int* err, bool& abort) {
@@ -51,26 +60,34 @@ __device__ __forceinline__ void tread(uint32_t taddr_lane, uint32_t col, float* 
 }
 
 template <int F>
-__global__ void __launch_bounds__(192, 1) op_pipe_kernel(const __grid_constant__ OpArgs a, int H, int W,
+__global__ void __launch_bounds__(320, 1) op_pipe_kernel(const __grid_constant__ OpArgs a, int H, int W,
                                                          int64_t n_items, int* err) {
+  // With a work list, n_items is an upper bound and the list's count is read
+  // on the device.
   using C = PipeCfg<F>;
   using T = __nv_bfloat16;
   constexpr int F2 = F / 2;
   constexpr int NC2 = F2 < 16 ? 16 : F2;
+  constexpr int NB = C::kNB;
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t* ring = smem;
   uint8_t* wsm = smem + C::kRing;
   uint8_t* cwsm = wsm + C::kW;
   uint8_t* casm = cwsm + C::kCW;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(casm + C::kCA);
+  float* bias_sm = reinterpret_cast<float*>(casm + C::kCA);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(casm + C::kCA + C::kBias);
+  constexpr int NR = C::kNcol;
   uint64_t* full = bars;
-  uint64_t* empty = bars + 4;
-  uint64_t* wbar = bars + 8;
-  uint64_t* accf = bars + 9;
-  uint64_t* acce = bars + 11;
-  uint64_t* caf = bars + 13;
-  uint64_t* cf = bars + 15;
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 17);
+  uint64_t* empty = bars + NR;
+  uint64_t* wbar = bars + 2 * NR;
+  uint64_t* accf = wbar + 1;
+  uint64_t* acce = accf + NB;
+  uint64_t* caf = acce + NB;
+  uint64_t* cf = caf + NB;
+  uint64_t* head_ready = cf + NB;
+  uint64_t* head_free = head_ready + 1;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(head_free + 1);
+  float2* head_sm = reinterpret_cast<float2*>(smem + C::kSmemBase);
 
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   const int P = H * W;
@@ -80,26 +97,32 @@ __global__ void __launch_bounds__(192, 1) op_pipe_kernel(const __grid_constant__
   const int dcmax = kind == kConvV ? 1 : 0;
   const int ntaps = kind == kConvH ? 3 : 9;
   const bool has_chain = !(kind == kConvC && !a.last);
+  const bool head = kind == kConvC && a.last;
   const int cnp = kind == kConvC ? 16 : NC2;
   const uint32_t chain_bytes = (uint32_t)(F * cnp * 2);
   const uint32_t wbytes = (uint32_t)(ntaps * F * F * 2);
 
   if (threadIdx.x == 0) {
-    for (int i = 0; i < 4; ++i) {
+    for (int i = 0; i < NR; ++i) {
       mbar_init(&full[i], 1);
       mbar_init(&empty[i], 1);
     }
     mbar_init(wbar, 1);
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < NB; ++i) {
       mbar_init(&accf[i], 1);
       mbar_init(&acce[i], 128);
       mbar_init(&caf[i], 128);
       mbar_init(&cf[i], 1);
     }
+    mbar_init(head_ready, 128);
+    mbar_init(head_free, 128);
     fence_mbar_init();
   }
+  for (int i = threadIdx.x; i < F; i += blockDim.x) bias_sm[i] = a.main.b[i];
+  if (has_chain)
+    for (int i = threadIdx.x; i < cnp; i += blockDim.x) bias_sm[32 + i] = a.chain.b[i];
   if (warp == 1) {
-    tmem_alloc(tslot, 128);
+    tmem_alloc(tslot, 256);
     tmem_relinquish();
   }
   tc_fence_before();
@@ -107,6 +130,8 @@ __global__ void __launch_bounds__(192, 1) op_pipe_kernel(const __grid_constant__
   tc_fence_after();
   const uint32_t tmem = *tslot;
   bool abort = false;
+  if (a.items) n_items = *a.n_items;
+  auto item_at = [&](int64_t k) -> int64_t { return a.items ? (int64_t)a.items[k] : k; };
 
   if (warp == 0) {
     if (lane == 0) {
@@ -115,12 +140,13 @@ __global__ void __launch_bounds__(192, 1) op_pipe_kernel(const __grid_constant__
       bulk_g2s(wsm, a.main.w, wbytes, wbar);
       if (has_chain) bulk_g2s(cwsm, a.chain.w, chain_bytes, wbar);
       uint32_t g = 0;
-      for (int64_t item = blockIdx.x; item < n_items && !abort; item += gridDim.x) {
+      for (int64_t it = blockIdx.x; it < n_items && !abort; it += gridDim.x) {
+        const int64_t item = item_at(it);
         const int64_t tile = item / H;
         const int r = (int)(item % H);
         for (int x = 0; x < W && !abort; ++x, ++g) {
-          const uint32_t slot = g % 4;
-          if (g >= 4 && !pwait(&empty[slot], ((g / 4) - 1) & 1, err, abort)) break;
+          const uint32_t slot = g % NR;
+          if (g >= NR && !pwait(&empty[slot], ((g / NR) - 1) & 1, err, abort)) break;
           uint32_t bytes = 0;
           for (int k = 0; k < nrows; ++k)
             if (r - (nrows - 1) + k >= 0) bytes += C::kBlk;
@@ -136,65 +162,90 @@ __global__ void __launch_bounds__(192, 1) op_pipe_kernel(const __grid_constant__
   } else if (warp == 1) {
     if (lane == 0) {
       // ---------------------------------------------------------------- MMA issuer
+      // The issuing thread is the critical resource (a 128x32x16 MMA costs ~48
+      // cycles, the same as a few dozen instructions), so descriptors are
+      // advanced by adding (byte offset >> 4) to base descriptors, and taps
+      // and ring slots are resolved without divisions.
       const uint32_t idesc = umma_idesc_bf16(128, F);
       const uint32_t idesc_c = umma_idesc_bf16(128, cnp);
-      const uint32_t ring_a = smem_u32(ring), w_a = smem_u32(wsm), cw_a = smem_u32(cwsm), ca_a = smem_u32(casm);
+      const uint64_t a0 = umma_sdesc(smem_u32(ring), 2048, 128);
+      const uint64_t w0 = umma_sdesc(smem_u32(wsm), F * 16, 128);
+      const uint64_t ca0 = umma_sdesc(smem_u32(casm), 2048, 128);
+      const uint64_t cw0 = umma_sdesc(smem_u32(cwsm), cnp * 16, 128);
+      constexpr uint32_t kBlk16 = C::kBlk >> 4;           // one ring block
+      constexpr uint32_t kTap16 = (F * F * 2) >> 4;       // one tap's weight slice
+      constexpr uint32_t kKs16 = (2 * 2048) >> 4;         // one K=16 step of A
+      constexpr uint32_t kKsW16 = (2 * F * 16) >> 4;      // one K=16 step of B
       pwait(wbar, 0, err, abort);
       uint32_t g_wait = 0, g_base = 0, p = 0, pc = 0;
       bool pending = false;
       auto issue_chain = [&](uint32_t q) {
-        const uint32_t b = q % 2;
-        if (!pwait(&caf[b], (q / 2) & 1, err, abort)) return;
+        const uint32_t b = q % NB;
+        if (!pwait(&caf[b], (q / NB) & 1, err, abort)) return;
         tc_fence_after();
 #pragma unroll
-        for (int ks = 0; ks < F / 16; ++ks) {
-          uint64_t ad = umma_sdesc(ca_a + b * (kTile * F * 2) + ks * 2 * 2048, 2048, 128);
-          uint64_t bd = umma_sdesc(cw_a + ks * 2 * cnp * 16, cnp * 16, 128);
-          umma_bf16(tmem + 64 + b * 32, ad, bd, idesc_c, ks > 0 ? 1u : 0u);
-        }
+        for (int ks = 0; ks < F / 16; ++ks)
+          umma_bf16(tmem + 128 + b * 32, ca0 + ((b * (kTile * F * 2) + ks * 2 * 2048) >> 4),
+                    cw0 + ((ks * 2 * cnp * 16) >> 4), idesc_c, ks > 0 ? 1u : 0u);
         umma_commit(&cf[b]);
       };
-      for (int64_t item = blockIdx.x; item < n_items && !abort; item += gridDim.x) {
+      // taps of this op as (dr, dc) with the weight slice index t = position
+      const int tdr0 = kind == kConvH ? 0 : -2;
+      const int tdc0 = kind == kConvV ? -1 : -2;
+      const int tnr = kind == kConvH ? 1 : 3;
+      for (int64_t it = blockIdx.x; it < n_items && !abort; it += gridDim.x) {
+        const int64_t item = item_at(it);
         const int r = (int)(item % H);
+        // ring slot of column 0 of this item
+        uint32_t slot_c = g_base % NR;
         for (int c = 0; c < W && !abort; ++c) {
           const int xmax = c + dcmax < W - 1 ? c + dcmax : W - 1;
           while (g_wait < g_base + (uint32_t)xmax + 1 && !abort) {
-            pwait(&full[g_wait % 4], (g_wait / 4) & 1, err, abort);
+            pwait(&full[g_wait % NR], (g_wait / NR) & 1, err, abort);
             ++g_wait;
           }
-          const uint32_t b = p % 2;
-          if (p >= 2) pwait(&acce[b], ((p / 2) - 1) & 1, err, abort);
+          const uint32_t b = p % NB;
+          if (p >= NB) pwait(&acce[b], ((p / NB) - 1) & 1, err, abort);
           if (abort) break;
           tc_fence_after();
-          bool first = true;
-          for (int t = 0; t < ntaps; ++t) {
-            int dr, dc;
-            tap_offset(kind, t, dr, dc);
-            const int rr = r + dr, x = c + dc;
-            if (rr < 0 || rr >= H || x < 0 || x >= W) continue;
-            const uint32_t slot = (g_base + x) % 4;
-            const int k = dr + (nrows - 1);
-            const uint32_t abase = ring_a + (slot * 3 + k) * C::kBlk;
-            const uint32_t wb = w_a + t * (F * F * 2);
+          const uint32_t d = tmem + b * 32;
+          uint32_t acc_flag = 0u;
+          // rows dr = tdr0 .. tdr0+tnr-1, columns dc = tdc0 .. tdc0+2; t = row*3 + col
 #pragma unroll
-            for (int ks = 0; ks < F / 16; ++ks) {
-              uint64_t ad = umma_sdesc(abase + ks * 2 * 2048, 2048, 128);
-              uint64_t bd = umma_sdesc(wb + ks * 2 * F * 16, F * 16, 128);
-              umma_bf16(tmem + b * F, ad, bd, idesc, first ? 0u : 1u);
-              first = false;
+          for (int i = 0; i < 3; ++i) {
+            if (i >= tnr) break;
+            const int rr = r + tdr0 + i;
+            if (rr < 0) continue;
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+              const int x = c + tdc0 + j;
+              if (x < 0 || x >= W) continue;
+              // slot of column x = slot_c + (tdc0 + j), wrapped into [0, NR)
+              int sx = (int)slot_c + tdc0 + j;
+              sx += sx < 0 ? NR : 0;
+              sx -= sx >= NR ? NR : 0;
+              const int krow = (tnr == 1) ? 0 : i;
+              const uint32_t aoff = ((uint32_t)sx * 3 + krow) * kBlk16;
+              const uint32_t woff = (uint32_t)(i * 3 + j) * kTap16;
+#pragma unroll
+              for (int ks = 0; ks < F / 16; ++ks) {
+                umma_bf16(d, a0 + aoff + ks * kKs16, w0 + woff + ks * kKsW16, idesc, acc_flag);
+                acc_flag = 1u;
+              }
             }
           }
           umma_commit(&accf[b]);
           const int xr = c + dcmin;
-          if (xr >= 0) umma_commit(&empty[(g_base + xr) % 4]);
+          if (xr >= 0) umma_commit(&empty[(g_base + xr) % NR]);
           if (c == W - 1) {
             for (int x = (W + dcmin > xr + 1 ? W + dcmin : xr + 1); x < W; ++x)
-              if (x >= 0) umma_commit(&empty[(g_base + x) % 4]);
+              if (x >= 0) umma_commit(&empty[(g_base + x) % NR]);
           }
           if (pending) issue_chain(pc);
           pending = has_chain;
           pc = p;
           ++p;
+          slot_c = slot_c + 1 == (uint32_t)NR ? 0 : slot_c + 1;
         }
         g_base += W;
       }
@@ -202,34 +253,40 @@ __global__ void __launch_bounds__(192, 1) op_pipe_kernel(const __grid_constant__
     }
   } else {
     // ---------------------------------------------------------------- epilogue
+    // Two groups of four warps take alternate pixels; within a group the TMEM
+    // lane quarter is warp % 4, so thread (warp, lane) owns sample m.
+    const int grp = (warp - 2) / 4;
     const int q4 = warp % 4;
     const int m = q4 * 32 + lane;
     const uint32_t tl = tmem + ((uint32_t)(q4 * 32) << 16);
-    const float* bm = a.main.b;
-    const float* bc = a.chain.b;
-    uint32_t p = 0;
-    for (int64_t item = blockIdx.x; item < n_items && !abort; item += gridDim.x) {
+    const float* bm = bias_sm;
+    const float* bc = bias_sm + 32;
+    const bool need_res = (kind == kConvV && a.stream_out && a.res) || (kind == kConvC && !a.last && a.res);
+    uint32_t p = 0, it_count = 0;
+    for (int64_t it = blockIdx.x; it < n_items && !abort; it += gridDim.x, ++it_count) {
+      const int64_t item = item_at(it);
       const int64_t tile = item / H;
       const int r = (int)(item % H);
       const int64_t sample = tile * kTile + m;
-      Kahan kre, kim;
+      if (head && grp == 1 && it_count > 0 && !pwait(head_free, (it_count - 1) & 1, err, abort)) break;
       for (int c = 0; c < W && !abort; ++c, ++p) {
-        const uint32_t b = p % 2;
+        if ((int)(p % C::kGroups) != grp) continue;
+        const uint32_t b = p % NB;
         const int pix = r * W + c;
-        if (!pwait(&accf[b], (p / 2) & 1, err, abort)) break;
+        float o[F];
+        if (need_res) load_row(blk<T>(a.res, tile, P, pix, F), m, 0, F, o);
+        if (!pwait(&accf[b], (p / NB) & 1, err, abort)) break;
         tc_fence_after();
         float acc[F];
-        tread<F>(tl, b * F, acc);
+        tread<F>(tl, b * 32, acc);
         tc_fence_before();
         mbar_arrive(&acce[b]);
         float cin[F];
         if (kind == kConvV) {
 #pragma unroll
-          for (int n = 0; n < F; ++n) acc[n] += __ldg(bm + n);
+          for (int n = 0; n < F; ++n) acc[n] += bm[n];
           if (a.stream_out) {
-            float o[F];
             if (a.res) {
-              load_row(blk<T>(a.res, tile, P, pix, F), m, 0, F, o);
 #pragma unroll
               for (int n = 0; n < F; ++n) o[n] = fmaxf(o[n] + acc[n], 0.f);
             } else {
@@ -243,15 +300,13 @@ __global__ void __launch_bounds__(192, 1) op_pipe_kernel(const __grid_constant__
           if (a.aux_out) store_row(blk<T>(a.aux_out, tile, P, pix, F), m, 0, F, cin);
         } else if (kind == kConvH) {
 #pragma unroll
-          for (int n = 0; n < F; ++n) cin[n] = fmaxf(acc[n] + __ldg(bm + n), 0.f);
+          for (int n = 0; n < F; ++n) cin[n] = fmaxf(acc[n] + bm[n], 0.f);
           if (a.aux_out) store_row(blk<T>(a.aux_out, tile, P, pix, F), m, 0, F, cin);
         } else {
 #pragma unroll
-          for (int n = 0; n < F; ++n) acc[n] += __ldg(bm + n);
+          for (int n = 0; n < F; ++n) acc[n] += bm[n];
           if (!a.last) {
-            float o[F];
             if (a.res) {
-              load_row(blk<T>(a.res, tile, P, pix, F), m, 0, F, o);
 #pragma unroll
               for (int n = 0; n < F; ++n) o[n] = fmaxf(o[n] + acc[n], 0.f);
             } else {
@@ -272,57 +327,69 @@ __global__ void __launch_bounds__(192, 1) op_pipe_kernel(const __grid_constant__
         for (int gq = 0; gq < F / 8; ++gq) st8(ca + ((int64_t)gq * kTile + m) * 8, cin + 8 * gq);
         fence_proxy_async_smem();
         mbar_arrive(&caf[b]);
-        if (!pwait(&cf[b], (p / 2) & 1, err, abort)) break;
+        if (!pwait(&cf[b], (p / NB) & 1, err, abort)) break;
         tc_fence_after();
         float out[32];
         if (kind == kConvC)
-          tread<16>(tl, 64 + b * 32, out);
+          tread<16>(tl, 128 + b * 32, out);
         else
-          tread<NC2>(tl, 64 + b * 32, out);
+          tread<NC2>(tl, 128 + b * 32, out);
         tc_fence_before();
         if (kind == kConvV) {
 #pragma unroll
-          for (int n = 0; n < F2; ++n) out[n] = fmaxf(out[n] + __ldg(bc + n), 0.f);
+          for (int n = 0; n < F2; ++n) out[n] = fmaxf(out[n] + bc[n], 0.f);
           if (r + 1 < H) store_row(blk<T>(a.cat, tile, P, pix + W, F), m, F2, F2, out);
           if (r == 0) {
 #pragma unroll
-            for (int n = 0; n < F2; ++n) out[n] = fmaxf(__ldg(bc + n), 0.f);
+            for (int n = 0; n < F2; ++n) out[n] = fmaxf(bc[n], 0.f);
             store_row(blk<T>(a.cat, tile, P, c, F), m, F2, F2, out);
           }
         } else if (kind == kConvH) {
 #pragma unroll
-          for (int n = 0; n < F2; ++n) out[n] = fmaxf(out[n] + __ldg(bc + n), 0.f);
+          for (int n = 0; n < F2; ++n) out[n] = fmaxf(out[n] + bc[n], 0.f);
           const int sh = a.last ? 1 : 0;
           if (c + sh < W) store_row(blk<T>(a.cat, tile, P, pix + sh, F), m, 0, F2, out);
           if (sh && c == 0) {
 #pragma unroll
-            for (int n = 0; n < F2; ++n) out[n] = fmaxf(__ldg(bc + n), 0.f);
+            for (int n = 0; n < F2; ++n) out[n] = fmaxf(bc[n], 0.f);
             store_row(blk<T>(a.cat, tile, P, pix, F), m, 0, F2, out);
           }
         } else {
 #pragma unroll
-          for (int n = 0; n < 4; ++n) out[n] += __ldg(bc + n);
+          for (int n = 0; n < 4; ++n) out[n] += bc[n];
           // abstract_machine.py:56-57 normalisation (same arithmetic as the per-pixel engine)
           float a2 = 2.f * out[0], b2 = 2.f * out[1];
           float mx = fmaxf(a2, b2);
           float lse = 0.5f * (mx + logf(expf(a2 - mx) + expf(b2 - mx)));
           float re0 = out[0] - lse, re1 = out[1] - lse;
           bool up = spin_at(a.spins, a.batch, P, sample, pix) > 0.f;
-          kre.add(up ? re0 : re1);
-          kim.add(up ? out[2] : out[3]);
+          head_sm[c * kTile + m] = make_float2(up ? re0 : re1, up ? out[2] : out[3]);
           if (a.cond && sample < a.batch)
             reinterpret_cast<float4*>(a.cond)[sample * P + pix] = make_float4(re0, re1, out[2], out[3]);
         }
       }
-      if (kind == kConvC && a.last && !abort)
-        a.row_partial[((int64_t)tile * H + r) * kTile + m] = make_float2(kre.s - kre.c, kim.s - kim.c);
+      if (head && !abort) {
+        // ordered compensated sum over the row's pixels (the per-pixel engine's order)
+        if (grp == 1) {
+          mbar_arrive(head_ready);
+        } else if (pwait(head_ready, it_count & 1, err, abort)) {
+          Kahan kre, kim;
+          for (int c = 0; c < W; ++c) {
+            float2 v = head_sm[c * kTile + m];
+            kre.add(v.x);
+            kim.add(v.y);
+          }
+          a.row_partial[((int64_t)tile * H + r) * kTile + m] = make_float2(kre.s - kre.c, kim.s - kim.c);
+          mbar_arrive(head_free);
+        }
+      }
     }
   }
   tc_fence_before();
   __syncthreads();
   if (warp == 1) {
     tc_fence_after();
-    tmem_dealloc(tmem, 128);
+    tmem_dealloc(tmem, 256);
   }
 }
 
@@ -335,16 +402,18 @@ static int launch_pipe(const OpArgs& a, int64_t tiles, int H, int W, int* err, c
     FK_CUDA(cudaGetDevice(&dev));
     FK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   }
+  const bool head = a.kind == kConvC && a.last;
+  if (head && W > PipeCfg<F>::kMaxW) return FK_ERR_ARG;
+  const int smem = PipeCfg<F>::kSmemBase + (head ? PipeCfg<F>::head_bytes(W) : 0);
   if (!attr) {
     FK_CUDA(cudaFuncSetAttribute(op_pipe_kernel<F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)PipeCfg<F>::kSmem));
+                                 PipeCfg<F>::kSmemBase + PipeCfg<F>::head_bytes(PipeCfg<F>::kMaxW)));
     attr = true;
   }
   const int64_t items = tiles * H;
-  const int per_sm = (227 * 1024) / PipeCfg<F>::kSmem > 0 ? (227 * 1024) / PipeCfg<F>::kSmem : 1;
-  int64_t grid = (int64_t)sms * per_sm;
+  int64_t grid = (int64_t)sms;  // one CTA per SM (256 TMEM columns, 320 threads)
   if (grid > items) grid = items;
-  op_pipe_kernel<F><<<(unsigned)grid, 192, PipeCfg<F>::kSmem, s>>>(a, H, W, items, err);
+  op_pipe_kernel<F><<<(unsigned)grid, 320, smem, s>>>(a, H, W, items, err);
   return check_cuda(launched(), "op_pipe_kernel");
 }
 
@@ -354,5 +423,10 @@ int launch_pipe_op(int F, const OpArgs& a, int64_t tiles, int H, int W, int* err
   if (F == 32) return launch_pipe<32>(a, tiles, H, W, err, s);
   return FK_ERR_ARG;
 }
+
+bool pipe_supported(int F, int W) { return (F == 16 || F == 32) && W <= PipeCfg<32>::kMaxW; }
+
+static_assert(PipeCfg<32>::kSmemBase + 16 * kTile * 8 <= 227 * 1024, "pipelined engine exceeds shared memory");
+static_assert(PipeCfg<16>::kSmemBase + 16 * kTile * 8 <= 227 * 1024, "pipelined engine exceeds shared memory");
 
 }  // namespace fk

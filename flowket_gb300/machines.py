@@ -348,3 +348,25 @@ class RBMSym(RBM):
         full = torch.cat([a, b, w.reshape(-1)])
         super().__init__(shape, alpha=alpha, device=device,
                          params=torch.view_as_real(full).reshape(-1).to(torch.float32))
+
+
+def _ar2d_forward_connections(machine, configs, owner, cflips, n_rows, base_saved, base_batch, chunk=1 << 17):
+    """log psi (n_rows, 2) of connected configurations with causal reuse of the
+    base samples' saved activations (fk_ar2d_forward_connections)."""
+    lib = _lib.load()
+    max_rows = configs.shape[0]
+    chunk = min(chunk, ((n_rows + 127) // 128) * 128) if n_rows else 128
+    nbytes = lib.fk_ar2d_connections_workspace_bytes(ctypes_ref(machine.desc), max_rows, chunk)
+    key = ("conn", max_rows, chunk)
+    ws = machine._ws.get(key)
+    if ws is None:
+        ws = torch.empty(nbytes, dtype=torch.uint8, device=machine.device)
+        machine._ws[key] = ws
+    out = torch.empty((max(n_rows, 1), 2), dtype=torch.float32, device=machine.device)
+    _lib.call("fk_ar2d_forward_connections", ctypes_ref(machine.desc), _lib.ptr(machine.packed()), _lib.ptr(configs),
+              _lib.ptr(owner), _lib.ptr(cflips), n_rows, _lib.ptr(base_saved), base_saved.numel(), base_batch,
+              _lib.ptr(out), _lib.ptr(ws), ws.numel(), chunk, _lib.stream_ptr())
+    return out
+
+
+ConvNetAutoregressive2D.forward_connections = _ar2d_forward_connections

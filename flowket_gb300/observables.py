@@ -67,21 +67,28 @@ class Observable(BaseObservable):
         rows = int(bf["nrows"].item())
         return spins, mel, bf, rows
 
-    def local_values(self, machine, configurations, log_psi=None):
+    def local_values(self, machine, configurations, log_psi=None, base_saved=None):
+        """E_loc per sample ((B, 2) float64). With `base_saved` (the sampler's
+        or a FK_AR2D_SAVE forward's workspace for these configurations) the
+        connected configurations reuse the base activations (causal reuse)."""
         spins, mel, bf, rows = self.connections(configurations)
         b = spins.shape[0]
         if log_psi is None:
             lp_self, _, _ = machine.forward(spins)
         else:
             lp_self = log_psi
-        lp_rows = torch.empty((max(rows, 1), 2), dtype=torch.float32, device=spins.device)
         if self.record_forward:
             ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
             ev[0].record()
-        for i in range(0, rows, self.evaluation_batch_size):
-            j = min(rows, i + self.evaluation_batch_size)
-            lp, _, _ = machine.forward(bf["configs"][i:j])
-            lp_rows[i:j] = lp
+        if base_saved is not None and hasattr(machine, "forward_connections"):
+            lp_rows = machine.forward_connections(bf["configs"], bf["owner"], bf["cflips"], rows, base_saved, b,
+                                                  chunk=self.evaluation_batch_size)
+        else:
+            lp_rows = torch.empty((max(rows, 1), 2), dtype=torch.float32, device=spins.device)
+            for i in range(0, rows, self.evaluation_batch_size):
+                j = min(rows, i + self.evaluation_batch_size)
+                lp, _, _ = machine.forward(bf["configs"][i:j])
+                lp_rows[i:j] = lp
         if self.record_forward:
             ev[1].record()
             self.forward_events.append(ev)

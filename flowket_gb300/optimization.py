@@ -66,6 +66,8 @@ class VariationalMonteCarlo(MiniBatchGenerator):
         self.current_energy = None
         self.current_local_energy_variance = None
         self.times = {}
+        # evaluate connected configurations from the sampler's saved activations
+        self.causal_reuse = True
 
     def _sample(self):
         out = self.sampler.sample()
@@ -73,7 +75,9 @@ class VariationalMonteCarlo(MiniBatchGenerator):
             return out
         return out, None, None
 
-    def _local_energy(self, spins, log_psi):
+    def _local_energy(self, spins, log_psi, saved=None):
+        if saved is not None:
+            return self.energy_observable.local_values(self.model, spins, log_psi=log_psi, base_saved=saved)
         return self.energy_observable.local_values(self.model, spins, log_psi=log_psi)
 
     def next_batch(self):
@@ -93,7 +97,7 @@ class VariationalMonteCarlo(MiniBatchGenerator):
         ev[0].record()
         spins, lp, saved = self._sample()
         ev[1].record()
-        local = self._local_energy(spins, lp)
+        local = self._local_energy(spins, lp, saved if self.causal_reuse else None)
         stats, w = energy_stats(local)
         ev[2].record()
         if hasattr(optimizer, "update"):

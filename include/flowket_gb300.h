@@ -125,6 +125,21 @@ int fk_ar2d_forward(const fk_ar2d_desc* desc, const void* packed, const int8_t* 
  * layout) for fk_ar2d_backward. */
 int fk_ar2d_sample(const fk_ar2d_desc* desc, const void* packed, int64_t batch, uint64_t seed, uint64_t offset,
                    int8_t* spins, float* log_psi, void* workspace, int64_t workspace_bytes, void* stream);
+/* log psi of connected configurations with causal reuse (the batched
+ * wave-function evaluation of observables/monte_carlo/operator.py:20-34).
+ * configs [n_rows][N], owner[row] = base sample, cflips[row][2] = flipped
+ * sites (the compact list of fk_compact_connections). base_saved is the
+ * FK_AR2D_SAVE workspace of the sampler/forward that evaluated the base_batch
+ * base samples with these weights. Rows are sorted by the row rk of their first
+ * flipped site; only lattice rows >= rk are evaluated, rows rk-2..rk of the
+ * tensors the causal taps read and the log psi of rows < rk come from the base.
+ * Bitwise equal to fk_ar2d_forward on the same configurations. log_psi [n_rows][2]
+ * in the input order. chunk (a multiple of 128) bounds the rows in flight. */
+int64_t fk_ar2d_connections_workspace_bytes(const fk_ar2d_desc* desc, int64_t max_rows, int64_t chunk);
+int fk_ar2d_forward_connections(const fk_ar2d_desc* desc, const void* packed, const int8_t* configs,
+                                const int32_t* owner, const int16_t* cflips, int64_t n_rows, const void* base_saved,
+                                int64_t base_saved_bytes, int64_t base_batch, float* log_psi, void* workspace,
+                                int64_t workspace_bytes, int64_t chunk, void* stream);
 /* Adjoint of log psi through the masked convolutions. Seeds w [B][2] weight
  * Re and Im log psi of each sample. grad [num_params] = d/dtheta sum_b
  * (w_re Re log psi_b + w_im Im log psi_b) (the Keras loss gradient of

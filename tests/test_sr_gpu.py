@@ -27,7 +27,8 @@ def test_gram_and_solve_match_numpy(cuda):
     ws = torch.empty(_lib.load().fk_sr_solve_workspace_bytes(n), dtype=torch.uint8, device="cuda")
     _lib.call("fk_sr_solve", _lib.ptr(gram), n, 1.0 / p, 0.05, _lib.ptr(rhs), 1e-12, 500, _lib.ptr(x),
               _lib.ptr(stats), _lib.ptr(ws), ws.numel(), _lib.stream_ptr())
-    ref = np.linalg.solve(want / p + 0.05 * np.eye(n), rhs.cpu().numpy())
+    # the solver against a dense FP64 solve of the same (GPU-built) matrix
+    ref = np.linalg.solve(gram.cpu().numpy() / p + 0.05 * np.eye(n), rhs.cpu().numpy())
     np.testing.assert_allclose(x.cpu().numpy(), ref, rtol=1e-8, atol=1e-10)
     assert 0 < stats[0].item() <= 500
 

@@ -60,3 +60,24 @@ def test_vmc_step_decreases_energy_heisenberg_4x4(cuda):
     assert last < first
     assert (last - e0) / abs(e0) < 0.1, (last, e0)
     assert set(vmc.times) == {"sampling", "local_energy", "gradient", "update"}
+
+
+@pytest.mark.parametrize("precision,which", [("bf16", 0), ("bf16", 1), ("fp32", 2), ("bf16", 2)])
+def test_causal_reuse_equals_full_forward(cuda, precision, which):
+    """Connected configurations evaluated from the base samples' saved
+    activations (rows >= first flipped row only) give bitwise the full forward."""
+    from flowket_gb300.machines import ConvNetAutoregressive2D
+    from flowket_gb300.observables import Observable
+    from flowket_gb300.samplers import FastAutoregressiveSampler
+    shape = (5, 6)
+    m = ConvNetAutoregressive2D(shape, 4, 16, weights_normalization=True, precision=precision, seed=2)
+    op = _ops(shape)[which][0]
+    spins, lp, saved = FastAutoregressiveSampler(m, 300, seed=8).sample()
+    obs = Observable(op, evaluation_batch_size=1024)
+    _, _, bf, rows = obs.connections(spins)
+    full = m.forward(bf["configs"][:rows])[0]
+    reuse = m.forward_connections(bf["configs"], bf["owner"], bf["cflips"], rows, saved, 300, chunk=1024)
+    assert torch.equal(full, reuse[:rows])
+    e_full = obs.local_values(m, spins, log_psi=lp).clone()
+    e_reuse = obs.local_values(m, spins, log_psi=lp, base_saved=saved)
+    assert torch.equal(e_full, e_reuse)
