@@ -319,4 +319,75 @@ int fk_sr_backmap(const float* o_re, const float* o_im, int64_t n_params, int64_
   return FK_OK;
 }
 
+
 }  // extern "C"
+
+// ---------------------------------------------------------------- no-allocation solve
+// Some hosts cannot hand this library a workspace: their device memory is
+// owned by another allocator (a framework that reserves nearly all of the GPU
+// at start-up, so a cudaMalloc would fail), or their policy forbids
+// cudaMalloc/cudaFree on the solve path because those calls synchronise the
+// device. fk_sr_solve_noalloc serves them with the scratch of the conjugate
+// gradients (three vectors of length n plus eight scalars) in a file-scope
+// device array of fixed size. The array exists once per device that loads the
+// library and stays reserved until the process exits.
+namespace fk {
+
+constexpr int64_t kNoAllocMaxN = 8192;  // largest n: 196,672 bytes of scratch
+static __device__ __align__(256) double g_sr_noalloc_scratch[3 * kNoAllocMaxN + 8];
+
+// Device address of the scratch array on the current device, looked up once
+// per device with that device current (the host-side name is not a device
+// pointer and must never be handed to a kernel).
+static double* noalloc_scratch() {
+  int dev = 0;
+  if (check_cuda(cudaGetDevice(&dev), "cudaGetDevice") != FK_OK) return nullptr;
+  static double* cached[64] = {nullptr};
+  if (dev < 0 || dev >= 64) {
+    set_error("fk_sr_solve_noalloc: device index %d out of range", dev);
+    return nullptr;
+  }
+  if (!cached[dev]) {
+    void* p = nullptr;
+    if (check_cuda(cudaGetSymbolAddress(&p, g_sr_noalloc_scratch), "cudaGetSymbolAddress") != FK_OK) return nullptr;
+    cached[dev] = static_cast<double*>(p);
+  }
+  return cached[dev];
+}
+
+}  // namespace fk
+
+extern "C" int fk_sr_solve_noalloc(const double* gram, int64_t n, double scale, double shift, const double* rhs,
+                                   double tol, int32_t max_iter, double* x, double* stats, void* stream) {
+  FK_CHECK_ARG(gram && rhs && x && n > 0 && max_iter > 0, "fk_sr_solve_noalloc: bad arguments");
+  FK_CHECK_ARG(n <= fk::kNoAllocMaxN,
+               "fk_sr_solve_noalloc: n = %lld exceeds the built-in scratch (n <= %lld); use fk_sr_solve with a "
+               "workspace",
+               (long long)n, (long long)fk::kNoAllocMaxN);
+  double* ws = fk::noalloc_scratch();
+  if (!ws) return FK_ERR_CUDA;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  double* r = ws;
+  double* p = r + n;
+  double* q = p + n;
+  double* sc = q + n;
+  // cg_init rewrites x, r, p and every scalar before any of them is read, so
+  // nothing left in the shared array by an earlier call is ever used.
+  fk::cg_init_kernel<<<1, 1024, 0, st>>>(rhs, n, x, r, p, sc, tol);
+  FK_CUDA(fk::launched());
+  const unsigned mv_blocks = (unsigned)((n * 32 + 255) / 256);
+  const unsigned vec_blocks = (unsigned)((n + 255) / 256 < 152 ? (n + 255) / 256 : 152);
+  for (int it = 0; it < max_iter; ++it) {
+    fk::cg_matvec_kernel<<<mv_blocks, 256, 0, st>>>(gram, n, scale, shift, p, q, sc);
+    fk::cg_update_kernel<<<vec_blocks, 256, 0, st>>>(n, x, r, p, q, sc);
+    fk::cg_direction_kernel<<<vec_blocks, 256, 0, st>>>(n, r, p, sc, 0);
+    fk::cg_roll_kernel<<<1, 1, 0, st>>>(sc);
+    FK_CUDA(fk::launched(4));
+  }
+  if (stats) {
+    FK_CUDA(cudaMemcpyAsync(stats, sc + 5, sizeof(double), cudaMemcpyDeviceToDevice, st));
+    FK_CUDA(cudaMemcpyAsync(stats + 1, sc + 0, sizeof(double), cudaMemcpyDeviceToDevice, st));
+    FK_CUDA(cudaMemcpyAsync(stats + 2, sc + 4, sizeof(double), cudaMemcpyDeviceToDevice, st));
+  }
+  return FK_OK;
+}

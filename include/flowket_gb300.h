@@ -212,6 +212,17 @@ int64_t fk_sr_solve_workspace_bytes(int64_t n);
 int fk_sr_solve(const double* gram, int64_t n, double scale, double shift, const double* rhs, double tol,
                 int32_t max_iter, double* x, double* stats, void* workspace, int64_t workspace_bytes,
                 void* stream);
+/* fk_sr_solve without a workspace, for callers that cannot allocate device
+ * memory (their GPU memory belongs to another allocator, or cudaMalloc is not
+ * allowed on their solve path). No counterpart in the reference. The CG
+ * scratch lives in a fixed device array inside the library, so n is limited to
+ * 8192; larger n is rejected with FK_ERR_ARG. The first call on a device looks
+ * the array up (cudaGetSymbolAddress) and should come before any stream
+ * capture. All calls share the array: calls that overlap on the GPU (other
+ * streams, other threads) race and must be serialised by the caller. Nothing
+ * from an earlier call is read; results equal fk_sr_solve's. */
+int fk_sr_solve_noalloc(const double* gram, int64_t n, double scale, double shift, const double* rhs, double tol,
+                        int32_t max_iter, double* x, double* stats, void* stream);
 /* x = scale * Y alpha (complex_values_optimizer.py:48-58 update direction);
  * params -= lr * x when params != NULL; x written to x_out when != NULL. */
 int fk_sr_backmap(const float* o_re, const float* o_im, int64_t n_params, int64_t n_samples, const double* alpha,
