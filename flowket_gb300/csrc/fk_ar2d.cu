@@ -77,6 +77,17 @@ int build_layout(const fk_ar2d_desc* d, NetLayout* L) {
     if (L->precision == FK_PRECISION_BF16) {
       w += ((int64_t)c.Kpad * c.Npad * 2 + 255) / 256 * 256;
     }
+    c.ws_off = -1;
+    c.wt_off = -1;
+    if (L->precision == FK_PRECISION_BF16 && kw == 3 && cin == F && F <= 32) {
+      c.ws_off = w;
+      w += ((int64_t)kh * cin * 3 * cout * 2 + 255) / 256 * 256;
+      c.wt_off = w;
+      w += ((int64_t)kh * cout * 3 * cin * 2 + 255) / 256 * 256;
+    } else if (L->precision == FK_PRECISION_BF16 && kh == 1 && kw == 1 && cin == F && cout == F / 2 && F <= 32) {
+      c.wt_off = w;
+      w += ((int64_t)cout * cin * 2 + 255) / 256 * 256;
+    }
     c.w32_off = w;
     w += ((int64_t)c.K * cout * 4 + 255) / 256 * 256;
     c.b_off = w;
@@ -181,6 +192,40 @@ __global__ void pack_kernel(const __grid_constant__ PackArgs a) {
       int k = kg * 8 + e;
       float x = (k < c.K && n < c.cout) ? v[(int64_t)k * c.cout + n] * scale[n] : 0.f;
       w[i] = __float2bfloat16_rn(x);
+    }
+  }
+  if (a.bf16 && c.ws_off >= 0) {
+    // column-scatter operand: element (kernel row i, k, n = s*cout + co) at
+    // ((i*(cin/8) + k/8)*3*cout + n)*8 + k%8, value W[i][2 - s][k][co]
+    __nv_bfloat16* w = reinterpret_cast<__nv_bfloat16*>(a.packed + c.ws_off);
+    const int n3 = 3 * c.cout;
+    const int total = c.kh * c.cin * n3;
+    for (int i = threadIdx.x; i < total; i += blockDim.x) {
+      const int e = i % 8;
+      const int n = (i / 8) % n3;
+      const int kg = i / (8 * n3);  // i*(cin/8) + k/8
+      const int row = kg / (c.cin / 8);
+      const int k = (kg % (c.cin / 8)) * 8 + e;
+      const int s = n / c.cout, co = n % c.cout;
+      const int t = row * c.kw + (2 - s);
+      w[i] = __float2bfloat16_rn(v[((int64_t)t * c.cin + k) * c.cout + co] * scale[co]);
+    }
+  }
+  if (a.bf16 && c.wt_off >= 0) {
+    // transposed operand: element (kernel row i, k = co, n = j*cin + ci) at
+    // ((i*(cout/8) + co/8)*kw*cin + n)*8 + co%8, value W[i][j][ci][co]
+    __nv_bfloat16* w = reinterpret_cast<__nv_bfloat16*>(a.packed + c.wt_off);
+    const int nn = c.kw * c.cin;
+    const int total = c.kh * c.cout * nn;
+    for (int i = threadIdx.x; i < total; i += blockDim.x) {
+      const int e = i % 8;
+      const int n = (i / 8) % nn;
+      const int kg = i / (8 * nn);  // i*(cout/8) + co/8
+      const int row = kg / (c.cout / 8);
+      const int co = (kg % (c.cout / 8)) * 8 + e;
+      const int j = n / c.cin, ci = n % c.cin;
+      const int t = row * c.kw + j;
+      w[i] = __float2bfloat16_rn(v[((int64_t)t * c.cin + ci) * c.cout + co] * scale[co]);
     }
   }
 }
@@ -392,11 +437,15 @@ __device__ void tc_main(const OpArgs& a, TcSmem& s, TcState& st, int64_t tile, i
     if (!tc_wait(s.bar_mma, st.ph_mma, st)) return;
     tc_fence_after();
   } else {
+    // Taps in column-major order (tap column, then tap row): the order in
+    // which the pipelined engine accumulates an output pixel, so that both
+    // engines and the sampler round identically.
     int taps[9];
     int pix[9];
     int nvalid = 0;
     const int nt = num_taps(a.kind);
-    for (int t = 0; t < nt; ++t) {
+    for (int q = 0; q < nt; ++q) {
+      const int t = tap_colmajor(a.kind, q);
       int dr, dc;
       tap_offset(a.kind, t, dr, dc);
       int rr = r + dr, cc = c + dc;
@@ -675,6 +724,8 @@ static ConvW convw(const NetLayout& L, const void* packed, int idx) {
   const ConvDesc& c = L.conv[idx];
   ConvW w;
   w.w = static_cast<const char*>(packed) + c.w_off;
+  w.ws = c.ws_off >= 0 ? static_cast<const char*>(packed) + c.ws_off : nullptr;
+  w.wt = c.wt_off >= 0 ? static_cast<const char*>(packed) + c.wt_off : nullptr;
   w.b = reinterpret_cast<const float*>(static_cast<const char*>(packed) + c.b_off);
   w.K = c.K;
   w.Npad = c.Npad;

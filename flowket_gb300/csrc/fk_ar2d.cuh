@@ -25,6 +25,8 @@ struct ConvDesc {
   int64_t p_kernel, p_bias, p_g;  // float offsets into the flat parameter vector (p_g < 0: none)
   int64_t w_off, b_off;           // byte offsets into the packed buffer (weights, fp32 bias)
   int64_t w32_off;                // byte offset of the fp32 [K][cout] effective kernel (== w_off on fp32)
+  int64_t ws_off;                 // byte offset of the column-scatter operand (-1: none), see below
+  int64_t wt_off;                 // byte offset of the transposed operand of the adjoint (-1: none)
   int kh, kw, cin, cout;
   int K, Kpad, Npad;              // GEMM K (taps*cin), padded K / N for the bf16 operand
 };
@@ -44,8 +46,23 @@ int build_layout(const fk_ar2d_desc* d, NetLayout* L);
 inline int conv_index(int cc, int kind) { return cc * 5 + kind; }
 
 // Packed weights as seen by one op.
+//
+// Column-scatter operand (bf16, convs with 3 kernel columns reading F <= 32
+// channels): per kernel row i a no-swizzle K-major block [cin/8][3*cout][8]
+// whose row n = s*cout + co holds W[i][2 - s][:, co]. One MMA of an input
+// column against kernel row i then yields the contributions to the three
+// output columns it feeds, output x + o + s in TMEM slot order (o = -1 for the
+// V op, 0 for the H and C ops).
+//
+// Transposed operand (bf16, adjoint on tensor cores): for the 3-column convs
+// per kernel row i a block [cout/8][3*cin][8] whose row n = j*cin + ci holds
+// W[i][j][ci][:] (K = output channel), so that one MMA of an output-gradient
+// column against kernel row i yields its contributions to three input-gradient
+// columns; for the 1x1 convs one block [cout/8][cin][8] holding W^T.
 struct ConvW {
   const void* w;    // fp32 [K][N] or bf16 [Kpad/8][Npad][8]
+  const void* ws;   // column-scatter operand or NULL
+  const void* wt;   // transposed operand of the adjoint or NULL
   const float* b;   // bias [N]
   int K, Npad;
 };
@@ -135,6 +152,8 @@ __device__ __forceinline__ void tap_offset(int kind, int t, int& dr, int& dc) {
   }
 }
 __device__ __forceinline__ int num_taps(int kind) { return kind == kConvH ? 3 : 9; }
+// q-th tap in column-major order (kernel column j outer, kernel row i inner).
+__device__ __forceinline__ int tap_colmajor(int kind, int q) { return kind == kConvH ? q : (q % 3) * 3 + q / 3; }
 
 __device__ __forceinline__ float spin_at(const int8_t* spins, int64_t batch, int P, int64_t sample, int pix) {
   return sample < batch ? (float)spins[sample * P + pix] : 1.f;

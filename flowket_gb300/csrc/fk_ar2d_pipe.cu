@@ -1,43 +1,52 @@
-// Pipelined tensor-core engine for the V/H/C ops of the AR2D forward
-// (causal convs after the first, F <= 32).
+// Pipelined column-scatter tensor-core engine for the V/H/C ops of the AR2D
+// forward (causal convs after the first, F <= 32).
 //
 // One persistent CTA per SM walks (tile, row) items; each item is one lattice
-// row of 128 samples. Six warps:
-//   warp 0 (one thread): TMA producer. Loads the op's weights once, then every
-//       input column (the 3 rows r-2..r -- 1 row for the H op -- of one lattice
-//       column, one bulk copy per [F/8][128][8] block) into a 7-8 slot ring;
-//   warp 1 (one thread): MMA issuer. Per pixel, tcgen05.mma over the in-bounds
-//       taps (K = 16 steps) into one of two TMEM accumulators, commits the
-//       accumulator to the epilogue and every column whose last pixel this was
-//       back to the producer; then the chained 1x1 MMA of the previous pixel
-//       on the epilogue's staged bf16 activations;
-//   warps 2-9: epilogue in two groups of four warps taking alternate pixels
+// row of 128 samples. Ten warps:
+//   warp 0 (one thread): TMA producer. Loads the op's column-scatter weights
+//       once, then every input column (the rows r-2..r -- only row r for the
+//       H op -- of one lattice column, one bulk copy per [F/8][128][8] block)
+//       into a ring of column slots;
+//   warp 1 (one thread): MMA issuer. Input column x is multiplied once per
+//       kernel row i by the three kernel columns stacked along N (N = 3F):
+//       the product holds x's contributions to the three output columns it
+//       feeds (x-1..x+1 for the V op, x..x+2 for the H and C ops), which
+//       accumulate in three consecutive TMEM slots of a ring. An output is
+//       committed to the epilogue after its last input column; the chained
+//       1x1 MMA of an output is issued one output later, on the epilogue's
+//       staged bf16 activations;
+//   warps 2-9: epilogue in two groups of four warps taking alternate outputs
 //       (thread = sample, TMEM lane quarter = warp % 4): bias, relu, residual
 //       (prefetched before the accumulator wait), stream store, chained-conv
 //       staging, and the second half after the chained MMA; the head's log psi
 //       partials are summed in pixel order through shared memory.
-// A pixel loads one new column instead of nine taps, and loads, MMAs and
-// epilogues of consecutive pixels overlap. The MMA sequence of a pixel (taps
-// ascending, K steps ascending) and the epilogue arithmetic are those of the
-// per-pixel engine in fk_ar2d.cu, so both engines give bitwise the same result.
+// Compared with gathering nine taps per output (18 MMAs of N = F per pixel)
+// this issues 6-7 MMAs of N = 3F per pixel: the single issuing thread, not the
+// tensor pipe, bounds small-N MMA streams.
+//
+// Each output accumulates its taps in column-major order (tap column outer,
+// tap row inner, K steps innermost), the order of the per-pixel engine in
+// fk_ar2d.cu, and the epilogue arithmetic is the same, so both engines give
+// bitwise the same result.
 #include "fk_ar2d.cuh"
 
 namespace fk {
 
 template <int F>
 struct PipeCfg {
-  static constexpr int kBlk = kTile * F * 2;
-  // Column ring depth: a column is requested when the column kNcol places
-  // earlier is released, i.e. kNcol - 2 pixels before its first use.
-  static constexpr int kNcol = F <= 16 ? 8 : 7;
+  static constexpr int kBlk = kTile * F * 2;        // one [F/8][128][8] bf16 block
+  static constexpr int kNcol = F <= 16 ? 8 : 6;     // input column slots
   static constexpr int kRing = 3 * kNcol * kBlk;
-  static constexpr int kW = 9 * F * F * 2;
+  static constexpr int kWRow = F * 3 * F * 2;       // one kernel row of the scatter operand
+  static constexpr int kW = 3 * kWRow;
   static constexpr int kCW = F * 32 * 2;
-  static constexpr int kGroups = 2;                 // epilogue groups (alternate pixels)
-  static constexpr int kNB = kGroups;               // TMEM / staging buffers (one per group)
-  static constexpr int kCA = kNB * kTile * F * 2;   // staged chained-conv inputs
+  static constexpr int kGroups = 2;                 // epilogue groups (alternate outputs)
+  static constexpr int kNB = kGroups;               // chained-conv staging buffers
+  static constexpr int kCA = kNB * kTile * F * 2;
   static constexpr int kBias = 64 * 4;              // main (F) + chained (<= 32) biases
-  static constexpr int kBars = 512;
+  static constexpr int kNS = 256 / F;               // TMEM accumulator slots (F columns each)
+  static constexpr uint32_t kChainCol = 256;        // chained accumulators: 256 + b * 32
+  static constexpr int kBars = 1024;
   static constexpr int kMaxW = 16;                  // head partials [W][128] float2
   static constexpr int kSmemBase = kRing + kW + kCW + kCA + kBias + kBars;
   static int head_bytes(int w) { return w * kTile * 8; }
@@ -69,6 +78,8 @@ __global__ void __launch_bounds__(320, 1) op_pipe_kernel(const __grid_constant__
   constexpr int F2 = F / 2;
   constexpr int NC2 = F2 < 16 ? 16 : F2;
   constexpr int NB = C::kNB;
+  constexpr int NS = C::kNS;
+  constexpr int NR = C::kNcol;
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t* ring = smem;
   uint8_t* wsm = smem + C::kRing;
@@ -76,13 +87,12 @@ __global__ void __launch_bounds__(320, 1) op_pipe_kernel(const __grid_constant__
   uint8_t* casm = cwsm + C::kCW;
   float* bias_sm = reinterpret_cast<float*>(casm + C::kCA);
   uint64_t* bars = reinterpret_cast<uint64_t*>(casm + C::kCA + C::kBias);
-  constexpr int NR = C::kNcol;
   uint64_t* full = bars;
   uint64_t* empty = bars + NR;
   uint64_t* wbar = bars + 2 * NR;
   uint64_t* accf = wbar + 1;
-  uint64_t* acce = accf + NB;
-  uint64_t* caf = acce + NB;
+  uint64_t* acce = accf + NS;
+  uint64_t* caf = acce + NS;
   uint64_t* cf = caf + NB;
   uint64_t* head_ready = cf + NB;
   uint64_t* head_free = head_ready + 1;
@@ -93,14 +103,11 @@ __global__ void __launch_bounds__(320, 1) op_pipe_kernel(const __grid_constant__
   const int P = H * W;
   const int kind = a.kind;
   const int nrows = kind == kConvH ? 1 : 3;
-  const int dcmin = kind == kConvV ? -1 : -2;
-  const int dcmax = kind == kConvV ? 1 : 0;
-  const int ntaps = kind == kConvH ? 3 : 9;
   const bool has_chain = !(kind == kConvC && !a.last);
   const bool head = kind == kConvC && a.last;
   const int cnp = kind == kConvC ? 16 : NC2;
   const uint32_t chain_bytes = (uint32_t)(F * cnp * 2);
-  const uint32_t wbytes = (uint32_t)(ntaps * F * F * 2);
+  const uint32_t wbytes = (uint32_t)(nrows * C::kWRow);
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < NR; ++i) {
@@ -108,9 +115,11 @@ __global__ void __launch_bounds__(320, 1) op_pipe_kernel(const __grid_constant__
       mbar_init(&empty[i], 1);
     }
     mbar_init(wbar, 1);
-    for (int i = 0; i < NB; ++i) {
+    for (int i = 0; i < NS; ++i) {
       mbar_init(&accf[i], 1);
       mbar_init(&acce[i], 128);
+    }
+    for (int i = 0; i < NB; ++i) {
       mbar_init(&caf[i], 128);
       mbar_init(&cf[i], 1);
     }
@@ -122,7 +131,7 @@ __global__ void __launch_bounds__(320, 1) op_pipe_kernel(const __grid_constant__
   if (has_chain)
     for (int i = threadIdx.x; i < cnp; i += blockDim.x) bias_sm[32 + i] = a.chain.b[i];
   if (warp == 1) {
-    tmem_alloc(tslot, 256);
+    tmem_alloc(tslot, 512);
     tmem_relinquish();
   }
   tc_fence_before();
@@ -137,7 +146,7 @@ __global__ void __launch_bounds__(320, 1) op_pipe_kernel(const __grid_constant__
     if (lane == 0) {
       // ---------------------------------------------------------------- producer
       mbar_arrive_expect_tx(wbar, wbytes + (has_chain ? chain_bytes : 0));
-      bulk_g2s(wsm, a.main.w, wbytes, wbar);
+      bulk_g2s(wsm, a.main.ws, wbytes, wbar);
       if (has_chain) bulk_g2s(cwsm, a.chain.w, chain_bytes, wbar);
       uint32_t g = 0;
       for (int64_t it = blockIdx.x; it < n_items && !abort; it += gridDim.x) {
@@ -162,98 +171,102 @@ __global__ void __launch_bounds__(320, 1) op_pipe_kernel(const __grid_constant__
   } else if (warp == 1) {
     if (lane == 0) {
       // ---------------------------------------------------------------- MMA issuer
-      // The issuing thread is the critical resource (a 128x32x16 MMA costs ~48
-      // cycles, the same as a few dozen instructions), so descriptors are
-      // advanced by adding (byte offset >> 4) to base descriptors, and taps
-      // and ring slots are resolved without divisions.
-      const uint32_t idesc = umma_idesc_bf16(128, F);
+      const uint32_t idesc1 = umma_idesc_bf16(128, F);
+      const uint32_t idesc2 = umma_idesc_bf16(128, 2 * F);
+      const uint32_t idesc3 = umma_idesc_bf16(128, 3 * F);
       const uint32_t idesc_c = umma_idesc_bf16(128, cnp);
       const uint64_t a0 = umma_sdesc(smem_u32(ring), 2048, 128);
-      const uint64_t w0 = umma_sdesc(smem_u32(wsm), F * 16, 128);
+      const uint64_t w0 = umma_sdesc(smem_u32(wsm), 3 * F * 16, 128);
       const uint64_t ca0 = umma_sdesc(smem_u32(casm), 2048, 128);
       const uint64_t cw0 = umma_sdesc(smem_u32(cwsm), cnp * 16, 128);
-      constexpr uint32_t kBlk16 = C::kBlk >> 4;           // one ring block
-      constexpr uint32_t kTap16 = (F * F * 2) >> 4;       // one tap's weight slice
-      constexpr uint32_t kKs16 = (2 * 2048) >> 4;         // one K=16 step of A
-      constexpr uint32_t kKsW16 = (2 * F * 16) >> 4;      // one K=16 step of B
+      constexpr uint32_t kBlk16 = C::kBlk >> 4;         // one ring block
+      constexpr uint32_t kRow16 = C::kWRow >> 4;        // one kernel row of the scatter operand
+      constexpr uint32_t kKs16 = (2 * 2048) >> 4;       // one K=16 step of A
+      constexpr uint32_t kKsW16 = (2 * 3 * F * 16) >> 4;  // one K=16 step of B
+      // outputs x + o0 .. x + o0 + 2 receive input column x; output c is
+      // complete after input column min(c + done_off, W - 1)
+      const int o0 = kind == kConvV ? -1 : 0;
+      const int done_off = kind == kConvV ? 1 : 0;
       pwait(wbar, 0, err, abort);
-      uint32_t g_wait = 0, g_base = 0, p = 0, pc = 0;
-      bool pending = false;
+      uint32_t gx = 0;       // input columns consumed (ring position)
+      uint32_t n_done = 0;   // outputs committed to the epilogue
+      uint32_t n_chain = 0;  // outputs whose chained MMA was issued
+      uint32_t gbase = 0;    // global index of output column 0 of the current item
       auto issue_chain = [&](uint32_t q) {
         const uint32_t b = q % NB;
         if (!pwait(&caf[b], (q / NB) & 1, err, abort)) return;
         tc_fence_after();
 #pragma unroll
         for (int ks = 0; ks < F / 16; ++ks)
-          umma_bf16(tmem + 128 + b * 32, ca0 + ((b * (kTile * F * 2) + ks * 2 * 2048) >> 4),
+          umma_bf16(tmem + C::kChainCol + b * 32, ca0 + ((b * (kTile * F * 2) + ks * 2 * 2048) >> 4),
                     cw0 + ((ks * 2 * cnp * 16) >> 4), idesc_c, ks > 0 ? 1u : 0u);
         umma_commit(&cf[b]);
       };
-      // taps of this op as (dr, dc) with the weight slice index t = position
-      const int tdr0 = kind == kConvH ? 0 : -2;
-      const int tdc0 = kind == kConvV ? -1 : -2;
-      const int tnr = kind == kConvH ? 1 : 3;
       for (int64_t it = blockIdx.x; it < n_items && !abort; it += gridDim.x) {
         const int64_t item = item_at(it);
         const int r = (int)(item % H);
-        // ring slot of column 0 of this item
-        uint32_t slot_c = g_base % NR;
-        for (int c = 0; c < W && !abort; ++c) {
-          const int xmax = c + dcmax < W - 1 ? c + dcmax : W - 1;
-          while (g_wait < g_base + (uint32_t)xmax + 1 && !abort) {
-            pwait(&full[g_wait % NR], (g_wait / NR) & 1, err, abort);
-            ++g_wait;
+        const int k0 = (nrows - 1) - r > 0 ? (nrows - 1) - r : 0;  // first in-lattice kernel row
+        for (int x = 0; x < W && !abort; ++x, ++gx) {
+          const uint32_t cs = gx % NR;
+          pwait(&full[cs], (gx / NR) & 1, err, abort);
+          const int c_lo = x + o0 < 0 ? 0 : x + o0;
+          const int c_hi = x + o0 + 2 < W - 1 ? x + o0 + 2 : W - 1;
+          // outputs first reached by this column, [c_f, c_hi]: all of them at
+          // x == 0, else output x + o0 + 2 if it exists
+          const int c_f = x == 0 ? c_lo : (x + o0 + 2 < c_hi + 1 ? x + o0 + 2 : c_hi + 1);
+          for (int c = c_f; c <= c_hi; ++c) {
+            const uint32_t p = gbase + (uint32_t)c;
+            if (p >= (uint32_t)NS) pwait(&acce[p % NS], ((p / NS) - 1) & 1, err, abort);
           }
-          const uint32_t b = p % NB;
-          if (p >= NB) pwait(&acce[b], ((p / NB) - 1) & 1, err, abort);
           if (abort) break;
           tc_fence_after();
-          const uint32_t d = tmem + b * 32;
-          uint32_t acc_flag = 0u;
-          // rows dr = tdr0 .. tdr0+tnr-1, columns dc = tdc0 .. tdc0+2; t = row*3 + col
+          // One MMA per (kernel row, K step) over outputs [ca, cb], split where
+          // the TMEM slot ring wraps.
+          auto mma = [&](int ca, int cb, uint32_t aoff, uint32_t boff, uint32_t acc) {
+            while (ca <= cb) {
+              const uint32_t s = (gbase + (uint32_t)ca) % NS;
+              int n = cb - ca + 1;
+              if (n > NS - (int)s) n = NS - (int)s;
+              const uint32_t id = n == 3 ? idesc3 : (n == 2 ? idesc2 : idesc1);
+              umma_bf16(tmem + s * F, a0 + aoff, w0 + boff + (uint32_t)((ca - x - o0) * F), id, acc);
+              ca += n;
+            }
+          };
+          bool first = true;
+          for (int k = k0; k < nrows; ++k) {
 #pragma unroll
-          for (int i = 0; i < 3; ++i) {
-            if (i >= tnr) break;
-            const int rr = r + tdr0 + i;
-            if (rr < 0) continue;
-#pragma unroll
-            for (int j = 0; j < 3; ++j) {
-              const int x = c + tdc0 + j;
-              if (x < 0 || x >= W) continue;
-              // slot of column x = slot_c + (tdc0 + j), wrapped into [0, NR)
-              int sx = (int)slot_c + tdc0 + j;
-              sx += sx < 0 ? NR : 0;
-              sx -= sx >= NR ? NR : 0;
-              const int krow = (tnr == 1) ? 0 : i;
-              const uint32_t aoff = ((uint32_t)sx * 3 + krow) * kBlk16;
-              const uint32_t woff = (uint32_t)(i * 3 + j) * kTap16;
-#pragma unroll
-              for (int ks = 0; ks < F / 16; ++ks) {
-                umma_bf16(d, a0 + aoff + ks * kKs16, w0 + woff + ks * kKsW16, idesc, acc_flag);
-                acc_flag = 1u;
+            for (int ks = 0; ks < F / 16; ++ks) {
+              const uint32_t aoff = (cs * 3 + (uint32_t)k) * kBlk16 + ks * kKs16;
+              const uint32_t boff = (uint32_t)k * kRow16 + ks * kKsW16;
+              if (first) {
+                if (c_f > c_lo) mma(c_lo, c_f - 1, aoff, boff, 1u);
+                mma(c_f, c_hi, aoff, boff, 0u);
+                first = false;
+              } else {
+                mma(c_lo, c_hi, aoff, boff, 1u);
               }
             }
           }
-          umma_commit(&accf[b]);
-          const int xr = c + dcmin;
-          if (xr >= 0) umma_commit(&empty[(g_base + xr) % NR]);
-          if (c == W - 1) {
-            for (int x = (W + dcmin > xr + 1 ? W + dcmin : xr + 1); x < W; ++x)
-              if (x >= 0) umma_commit(&empty[(g_base + x) % NR]);
+          umma_commit(&empty[cs]);
+          // outputs completed by this column
+          const int d_lo = x - done_off < 0 ? 0 : x - done_off;
+          const int d_hi = x == W - 1 ? W - 1 : x - done_off;
+          for (int c = d_lo; c <= d_hi; ++c) {
+            umma_commit(&accf[(gbase + (uint32_t)c) % NS]);
+            ++n_done;
           }
-          if (pending) issue_chain(pc);
-          pending = has_chain;
-          pc = p;
-          ++p;
-          slot_c = slot_c + 1 == (uint32_t)NR ? 0 : slot_c + 1;
+          // chained MMAs trail the committed outputs by one
+          if (has_chain)
+            while (n_chain + 1 < n_done && !abort) issue_chain(n_chain++);
         }
-        g_base += W;
+        gbase += (uint32_t)W;
       }
-      if (pending && !abort) issue_chain(pc);
+      if (has_chain)
+        while (n_chain < n_done && !abort) issue_chain(n_chain++);
     }
   } else {
     // ---------------------------------------------------------------- epilogue
-    // Two groups of four warps take alternate pixels; within a group the TMEM
+    // Two groups of four warps take alternate outputs; within a group the TMEM
     // lane quarter is warp % 4, so thread (warp, lane) owns sample m.
     const int grp = (warp - 2) / 4;
     const int q4 = warp % 4;
@@ -272,15 +285,16 @@ __global__ void __launch_bounds__(320, 1) op_pipe_kernel(const __grid_constant__
       for (int c = 0; c < W && !abort; ++c, ++p) {
         if ((int)(p % C::kGroups) != grp) continue;
         const uint32_t b = p % NB;
+        const uint32_t sl = p % NS;
         const int pix = r * W + c;
         float o[F];
         if (need_res) load_row(blk<T>(a.res, tile, P, pix, F), m, 0, F, o);
-        if (!pwait(&accf[b], (p / NB) & 1, err, abort)) break;
+        if (!pwait(&accf[sl], (p / NS) & 1, err, abort)) break;
         tc_fence_after();
         float acc[F];
-        tread<F>(tl, b * 32, acc);
+        tread<F>(tl, sl * F, acc);
         tc_fence_before();
-        mbar_arrive(&acce[b]);
+        mbar_arrive(&acce[sl]);
         float cin[F];
         if (kind == kConvV) {
 #pragma unroll
@@ -331,9 +345,9 @@ __global__ void __launch_bounds__(320, 1) op_pipe_kernel(const __grid_constant__
         tc_fence_after();
         float out[32];
         if (kind == kConvC)
-          tread<16>(tl, 128 + b * 32, out);
+          tread<16>(tl, C::kChainCol + b * 32, out);
         else
-          tread<NC2>(tl, 128 + b * 32, out);
+          tread<NC2>(tl, C::kChainCol + b * 32, out);
         tc_fence_before();
         if (kind == kConvV) {
 #pragma unroll
@@ -389,9 +403,11 @@ __global__ void __launch_bounds__(320, 1) op_pipe_kernel(const __grid_constant__
   __syncthreads();
   if (warp == 1) {
     tc_fence_after();
-    tmem_dealloc(tmem, 256);
+    tmem_dealloc(tmem, 512);
   }
 }
+
+constexpr int kMinSmem = 120 * 1024;
 
 template <int F>
 static int launch_pipe(const OpArgs& a, int64_t tiles, int H, int W, int* err, cudaStream_t s) {
@@ -404,14 +420,19 @@ static int launch_pipe(const OpArgs& a, int64_t tiles, int H, int W, int* err, c
   }
   const bool head = a.kind == kConvC && a.last;
   if (head && W > PipeCfg<F>::kMaxW) return FK_ERR_ARG;
-  const int smem = PipeCfg<F>::kSmemBase + (head ? PipeCfg<F>::head_bytes(W) : 0);
+  if (!a.main.ws) return FK_ERR_ARG;
+  // At least half of an SM's shared memory, so that one CTA (holding all 512
+  // TMEM columns) runs per SM.
+  int smem = PipeCfg<F>::kSmemBase + (head ? PipeCfg<F>::head_bytes(W) : 0);
+  if (smem < kMinSmem) smem = kMinSmem;
   if (!attr) {
+    const int most = PipeCfg<F>::kSmemBase + PipeCfg<F>::head_bytes(PipeCfg<F>::kMaxW);
     FK_CUDA(cudaFuncSetAttribute(op_pipe_kernel<F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 PipeCfg<F>::kSmemBase + PipeCfg<F>::head_bytes(PipeCfg<F>::kMaxW)));
+                                 most > kMinSmem ? most : kMinSmem));
     attr = true;
   }
   const int64_t items = tiles * H;
-  int64_t grid = (int64_t)sms;  // one CTA per SM (256 TMEM columns, 320 threads)
+  int64_t grid = (int64_t)sms;  // one CTA per SM (512 TMEM columns, 320 threads)
   if (grid > items) grid = items;
   op_pipe_kernel<F><<<(unsigned)grid, 320, smem, s>>>(a, H, W, items, err);
   return check_cuda(launched(), "op_pipe_kernel");
@@ -424,9 +445,10 @@ int launch_pipe_op(int F, const OpArgs& a, int64_t tiles, int H, int W, int* err
   return FK_ERR_ARG;
 }
 
-bool pipe_supported(int F, int W) { return (F == 16 || F == 32) && W <= PipeCfg<32>::kMaxW; }
+bool pipe_supported(int F, int W) { return (F == 16 || F == 32) && W >= 2 && W <= PipeCfg<32>::kMaxW; }
 
 static_assert(PipeCfg<32>::kSmemBase + 16 * kTile * 8 <= 227 * 1024, "pipelined engine exceeds shared memory");
 static_assert(PipeCfg<16>::kSmemBase + 16 * kTile * 8 <= 227 * 1024, "pipelined engine exceeds shared memory");
+static_assert(3 * 32 <= 256 && PipeCfg<16>::kNS * 16 <= 256, "TMEM layout");
 
 }  // namespace fk
