@@ -41,16 +41,18 @@ struct PipeCfg {
   static constexpr int kW = 3 * kWRow;
   static constexpr int kCW = F * 32 * 2;
   static constexpr int kGroups = 2;                 // epilogue groups (alternate outputs)
-  static constexpr int kNB = kGroups;               // chained-conv staging buffers
+  static constexpr int kNB = 2 * kGroups;           // chained-conv staging buffers / accumulators
   static constexpr int kCA = kNB * kTile * F * 2;
   static constexpr int kBias = 64 * 4;              // main (F) + chained (<= 32) biases
   static constexpr int kNS = 256 / F;               // TMEM accumulator slots (F columns each)
-  static constexpr uint32_t kChainCol = 256;        // chained accumulators: 256 + b * 32
+  static constexpr uint32_t kChainCol = 256;        // chained accumulators: 256 + b * 32 (b < kNB)
   static constexpr int kBars = 1024;
   static constexpr int kMaxW = 16;                  // head partials [W][128] float2
   static constexpr int kSmemBase = kRing + kW + kCW + kCA + kBias + kBars;
   static int head_bytes(int w) { return w * kTile * 8; }
 };
+
+constexpr int kPipeThreads = 384;  // 12 warps: producer, issuer, waiter, chain issuer, 8 epilogue
 
 __device__ __forceinline__ bool pwait(uint64_t* bar, uint32_t parity, int* err, bool& abort) {
   if (abort) return false;
@@ -68,9 +70,24 @@ __device__ __forceinline__ void tread(uint32_t taddr_lane, uint32_t col, float* 
   tmem_ld_wait();
 }
 
+// Barrier 1 of the CTA: rendezvous of the waiter warp and the issuer warp,
+// one per input column, returning the OR of both warps' abort flags.
+__device__ __forceinline__ bool step_rendezvous(bool abort) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.u32 p, %1, 0;\n\t"
+      "barrier.cta.red.or.pred q, 1, 64, p;\n\t"
+      "selp.u32 %0, 1, 0, q;\n\t}"
+      : "=r"(r)
+      : "r"((uint32_t)abort)
+      : "memory");
+  return r != 0;
+}
+
 template <int F>
-__global__ void __launch_bounds__(320, 1) op_pipe_kernel(const __grid_constant__ OpArgs a, int H, int W,
-                                                         int64_t n_items, int* err) {
+__global__ void __launch_bounds__(kPipeThreads, 1) op_pipe_kernel(const __grid_constant__ OpArgs a, int H, int W,
+                                                                  int64_t n_items, int* err) {
   // With a work list, n_items is an upper bound and the list's count is read
   // on the device.
   using C = PipeCfg<F>;
@@ -96,7 +113,8 @@ __global__ void __launch_bounds__(320, 1) op_pipe_kernel(const __grid_constant__
   uint64_t* cf = caf + NB;
   uint64_t* head_ready = cf + NB;
   uint64_t* head_free = head_ready + 1;
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(head_free + 1);
+  uint64_t* drain = head_free + 1;  // [2]: MMA completion before teardown (issuer, chain issuer)
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(drain + 2);
   float2* head_sm = reinterpret_cast<float2*>(smem + C::kSmemBase);
 
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
@@ -108,6 +126,9 @@ __global__ void __launch_bounds__(320, 1) op_pipe_kernel(const __grid_constant__
   const int cnp = kind == kConvC ? 16 : NC2;
   const uint32_t chain_bytes = (uint32_t)(F * cnp * 2);
   const uint32_t wbytes = (uint32_t)(nrows * C::kWRow);
+  // outputs x + o0 .. x + o0 + 2 receive input column x; output c is complete
+  // after input column min(c - o0, W - 1)
+  const int o0 = kind == kConvV ? -1 : 0;
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < NR; ++i) {
@@ -125,6 +146,8 @@ __global__ void __launch_bounds__(320, 1) op_pipe_kernel(const __grid_constant__
     }
     mbar_init(head_ready, 128);
     mbar_init(head_free, 128);
+    mbar_init(&drain[0], 1);
+    mbar_init(&drain[1], 1);
     fence_mbar_init();
   }
   for (int i = threadIdx.x; i < F; i += blockDim.x) bias_sm[i] = a.main.b[i];
@@ -169,57 +192,38 @@ __global__ void __launch_bounds__(320, 1) op_pipe_kernel(const __grid_constant__
       }
     }
   } else if (warp == 1) {
-    if (lane == 0) {
-      // ---------------------------------------------------------------- MMA issuer
-      const uint32_t idesc1 = umma_idesc_bf16(128, F);
-      const uint32_t idesc2 = umma_idesc_bf16(128, 2 * F);
-      const uint32_t idesc3 = umma_idesc_bf16(128, 3 * F);
-      const uint32_t idesc_c = umma_idesc_bf16(128, cnp);
-      const uint64_t a0 = umma_sdesc(smem_u32(ring), 2048, 128);
-      const uint64_t w0 = umma_sdesc(smem_u32(wsm), 3 * F * 16, 128);
-      const uint64_t ca0 = umma_sdesc(smem_u32(casm), 2048, 128);
-      const uint64_t cw0 = umma_sdesc(smem_u32(cwsm), cnp * 16, 128);
-      constexpr uint32_t kBlk16 = C::kBlk >> 4;         // one ring block
-      constexpr uint32_t kRow16 = C::kWRow >> 4;        // one kernel row of the scatter operand
-      constexpr uint32_t kKs16 = (2 * 2048) >> 4;       // one K=16 step of A
-      constexpr uint32_t kKsW16 = (2 * 3 * F * 16) >> 4;  // one K=16 step of B
-      // outputs x + o0 .. x + o0 + 2 receive input column x; output c is
-      // complete after input column min(c + done_off, W - 1)
-      const int o0 = kind == kConvV ? -1 : 0;
-      const int done_off = kind == kConvV ? 1 : 0;
-      pwait(wbar, 0, err, abort);
-      uint32_t gx = 0;       // input columns consumed (ring position)
-      uint32_t n_done = 0;   // outputs committed to the epilogue
-      uint32_t n_chain = 0;  // outputs whose chained MMA was issued
-      uint32_t gbase = 0;    // global index of output column 0 of the current item
-      auto issue_chain = [&](uint32_t q) {
-        const uint32_t b = q % NB;
-        if (!pwait(&caf[b], (q / NB) & 1, err, abort)) return;
+    // ------------------------------------------------------------------ MMA issuer
+    // The whole warp runs the loop and lane 0 issues. This thread performs no
+    // memory load while MMAs stream (a load, mbarrier waits included, stalls
+    // the tensor pipe for hundreds of cycles): the waiter warp observes every
+    // barrier and releases each input column through barrier 1.
+    const uint32_t idesc1 = umma_idesc_bf16(128, F);
+    const uint32_t idesc2 = umma_idesc_bf16(128, 2 * F);
+    const uint32_t idesc3 = umma_idesc_bf16(128, 3 * F);
+    const uint64_t a0 = umma_sdesc(smem_u32(ring), 2048, 128);
+    const uint64_t w0 = umma_sdesc(smem_u32(wsm), 3 * F * 16, 128);
+    constexpr uint32_t kBlk16 = C::kBlk >> 4;           // one ring block
+    constexpr uint32_t kRow16 = C::kWRow >> 4;          // one kernel row of the scatter operand
+    constexpr uint32_t kKs16 = (2 * 2048) >> 4;         // one K=16 step of A
+    constexpr uint32_t kKsW16 = (2 * 3 * F * 16) >> 4;  // one K=16 step of B
+    uint32_t gx = 0;     // input columns consumed (ring position)
+    uint32_t cs = 0;     // ring slot of column gx
+    uint32_t gbase = 0;  // global index of output column 0 of the current item
+    int64_t next_item = blockIdx.x < n_items ? item_at(blockIdx.x) : 0;
+    for (int64_t it = blockIdx.x; it < n_items && !abort; it += gridDim.x) {
+      const int r = (int)(next_item % H);
+      if (it + gridDim.x < n_items) next_item = item_at(it + gridDim.x);  // consumed one item later
+      const int k0 = (nrows - 1) - r > 0 ? (nrows - 1) - r : 0;        // first in-lattice kernel row
+      for (int x = 0; x < W; ++x, ++gx) {
+        abort = step_rendezvous(false);
+        if (abort) break;
         tc_fence_after();
-#pragma unroll
-        for (int ks = 0; ks < F / 16; ++ks)
-          umma_bf16(tmem + C::kChainCol + b * 32, ca0 + ((b * (kTile * F * 2) + ks * 2 * 2048) >> 4),
-                    cw0 + ((ks * 2 * cnp * 16) >> 4), idesc_c, ks > 0 ? 1u : 0u);
-        umma_commit(&cf[b]);
-      };
-      for (int64_t it = blockIdx.x; it < n_items && !abort; it += gridDim.x) {
-        const int64_t item = item_at(it);
-        const int r = (int)(item % H);
-        const int k0 = (nrows - 1) - r > 0 ? (nrows - 1) - r : 0;  // first in-lattice kernel row
-        for (int x = 0; x < W && !abort; ++x, ++gx) {
-          const uint32_t cs = gx % NR;
-          pwait(&full[cs], (gx / NR) & 1, err, abort);
-          const int c_lo = x + o0 < 0 ? 0 : x + o0;
-          const int c_hi = x + o0 + 2 < W - 1 ? x + o0 + 2 : W - 1;
-          // outputs first reached by this column, [c_f, c_hi]: all of them at
-          // x == 0, else output x + o0 + 2 if it exists
-          const int c_f = x == 0 ? c_lo : (x + o0 + 2 < c_hi + 1 ? x + o0 + 2 : c_hi + 1);
-          for (int c = c_f; c <= c_hi; ++c) {
-            const uint32_t p = gbase + (uint32_t)c;
-            if (p >= (uint32_t)NS) pwait(&acce[p % NS], ((p / NS) - 1) & 1, err, abort);
-          }
-          if (abort) break;
-          tc_fence_after();
+        const int c_lo = x + o0 < 0 ? 0 : x + o0;
+        const int c_hi = x + o0 + 2 < W - 1 ? x + o0 + 2 : W - 1;
+        // outputs first reached by this column, [c_f, c_hi]: all of them at
+        // x == 0, else output x + o0 + 2 if it exists
+        const int c_f = x == 0 ? c_lo : (x + o0 + 2 < c_hi + 1 ? x + o0 + 2 : c_hi + 1);
+        if (lane == 0) {
           // One MMA per (kernel row, K step) over outputs [ca, cb], split where
           // the TMEM slot ring wraps.
           auto mma = [&](int ca, int cb, uint32_t aoff, uint32_t boff, uint32_t acc) {
@@ -249,38 +253,136 @@ __global__ void __launch_bounds__(320, 1) op_pipe_kernel(const __grid_constant__
           }
           umma_commit(&empty[cs]);
           // outputs completed by this column
-          const int d_lo = x - done_off < 0 ? 0 : x - done_off;
-          const int d_hi = x == W - 1 ? W - 1 : x - done_off;
-          for (int c = d_lo; c <= d_hi; ++c) {
-            umma_commit(&accf[(gbase + (uint32_t)c) % NS]);
-            ++n_done;
-          }
-          // chained MMAs trail the committed outputs by one
-          if (has_chain)
-            while (n_chain + 1 < n_done && !abort) issue_chain(n_chain++);
+          const int d_lo = x + o0 < 0 ? 0 : x + o0;
+          const int d_hi = x == W - 1 ? W - 1 : x + o0;
+          for (int c = d_lo; c <= d_hi; ++c) umma_commit(&accf[(gbase + (uint32_t)c) % NS]);
         }
-        gbase += (uint32_t)W;
+        __syncwarp();
+        cs = cs + 1 == (uint32_t)NR ? 0 : cs + 1;
       }
-      if (has_chain)
-        while (n_chain < n_done && !abort) issue_chain(n_chain++);
+      gbase += (uint32_t)W;
+    }
+    if (lane == 0) {
+      umma_commit(&drain[0]);
+      mbar_wait(&drain[0], 0, err);
+    }
+  } else if (warp == 2) {
+    // ------------------------------------------------------------------ waiter
+    // Observes the barriers each input column needs (column loaded, TMEM slots
+    // of the outputs it starts released by the epilogue), then releases the
+    // column to the issuer through barrier 1.
+    pwait(wbar, 0, err, abort);
+    uint32_t gx = 0, gbase = 0;
+    bool stop = false;
+    for (int64_t it = blockIdx.x; it < n_items && !stop; it += gridDim.x) {
+      for (int x = 0; x < W; ++x, ++gx) {
+        pwait(&full[gx % NR], (gx / NR) & 1, err, abort);
+        const int c_hi = x + o0 + 2 < W - 1 ? x + o0 + 2 : W - 1;
+        const int c_f = x == 0 ? (x + o0 < 0 ? 0 : x + o0) : (x + o0 + 2 < c_hi + 1 ? x + o0 + 2 : c_hi + 1);
+        for (int c = c_f; c <= c_hi; ++c) {
+          const uint32_t p = gbase + (uint32_t)c;
+          if (p >= (uint32_t)NS) pwait(&acce[p % NS], ((p / NS) - 1) & 1, err, abort);
+        }
+        stop = step_rendezvous(abort);
+        if (stop) break;
+      }
+      gbase += (uint32_t)W;
+    }
+    abort = stop;
+  } else if (warp == 3) {
+    // ------------------------------------------------------------------ chain issuer
+    // The chained 1x1 MMA of each output, on the epilogue's staged bf16
+    // activations, into one of NB chained accumulators.
+    if (has_chain && lane == 0) {
+      const uint32_t idesc_c = umma_idesc_bf16(128, cnp);
+      const uint64_t ca0 = umma_sdesc(smem_u32(casm), 2048, 128);
+      const uint64_t cw0 = umma_sdesc(smem_u32(cwsm), cnp * 16, 128);
+      pwait(wbar, 0, err, abort);
+      uint32_t q = 0;
+      for (int64_t it = blockIdx.x; it < n_items && !abort; it += gridDim.x) {
+        for (int c = 0; c < W && !abort; ++c, ++q) {
+          const uint32_t b = q % NB;
+          if (!pwait(&caf[b], (q / NB) & 1, err, abort)) break;
+          tc_fence_after();
+#pragma unroll
+          for (int ks = 0; ks < F / 16; ++ks)
+            umma_bf16(tmem + C::kChainCol + b * 32, ca0 + ((b * (kTile * F * 2) + ks * 2 * 2048) >> 4),
+                      cw0 + ((ks * 2 * cnp * 16) >> 4), idesc_c, ks > 0 ? 1u : 0u);
+          umma_commit(&cf[b]);
+        }
+      }
+      umma_commit(&drain[1]);
+      mbar_wait(&drain[1], 0, err);
     }
   } else {
     // ---------------------------------------------------------------- epilogue
     // Two groups of four warps take alternate outputs; within a group the TMEM
-    // lane quarter is warp % 4, so thread (warp, lane) owns sample m.
-    const int grp = (warp - 2) / 4;
+    // lane quarter is warp % 4, so thread (warp, lane) owns sample m. The part
+    // after the chained MMA of an output runs after the first part of the
+    // group's next output, which hides the chained MMA's round trip.
+    const int grp = (warp - 4) / 4;
     const int q4 = warp % 4;
     const int m = q4 * 32 + lane;
     const uint32_t tl = tmem + ((uint32_t)(q4 * 32) << 16);
     const float* bm = bias_sm;
     const float* bc = bias_sm + 32;
     const bool need_res = (kind == kConvV && a.stream_out && a.res) || (kind == kConvC && !a.last && a.res);
+    // deferred second half: output index, tile, row, column
+    bool pend = false;
+    uint32_t pq = 0;
+    int64_t ptile = 0;
+    int pr = 0, pc = 0;
+    auto second_half = [&]() {
+      const uint32_t b = pq % NB;
+      pend = false;
+      if (!pwait(&cf[b], (pq / NB) & 1, err, abort)) return;
+      tc_fence_after();
+      float out[32];
+      if (kind == kConvC)
+        tread<16>(tl, C::kChainCol + b * 32, out);
+      else
+        tread<NC2>(tl, C::kChainCol + b * 32, out);
+      tc_fence_before();
+      const int pix = pr * W + pc;
+      if (kind == kConvV) {
+#pragma unroll
+        for (int n = 0; n < F2; ++n) out[n] = fmaxf(out[n] + bc[n], 0.f);
+        if (pr + 1 < H) store_row(blk<T>(a.cat, ptile, P, pix + W, F), m, F2, F2, out);
+        if (pr == 0) {
+#pragma unroll
+          for (int n = 0; n < F2; ++n) out[n] = fmaxf(bc[n], 0.f);
+          store_row(blk<T>(a.cat, ptile, P, pc, F), m, F2, F2, out);
+        }
+      } else if (kind == kConvH) {
+#pragma unroll
+        for (int n = 0; n < F2; ++n) out[n] = fmaxf(out[n] + bc[n], 0.f);
+        const int sh = a.last ? 1 : 0;
+        if (pc + sh < W) store_row(blk<T>(a.cat, ptile, P, pix + sh, F), m, 0, F2, out);
+        if (sh && pc == 0) {
+#pragma unroll
+          for (int n = 0; n < F2; ++n) out[n] = fmaxf(bc[n], 0.f);
+          store_row(blk<T>(a.cat, ptile, P, pix, F), m, 0, F2, out);
+        }
+      } else {
+#pragma unroll
+        for (int n = 0; n < 4; ++n) out[n] += bc[n];
+        // abstract_machine.py:56-57 normalisation (same arithmetic as the per-pixel engine)
+        float a2 = 2.f * out[0], b2 = 2.f * out[1];
+        float mx = fmaxf(a2, b2);
+        float lse = 0.5f * (mx + logf(expf(a2 - mx) + expf(b2 - mx)));
+        float re0 = out[0] - lse, re1 = out[1] - lse;
+        const int64_t sample = ptile * kTile + m;
+        bool up = spin_at(a.spins, a.batch, P, sample, pix) > 0.f;
+        head_sm[pc * kTile + m] = make_float2(up ? re0 : re1, up ? out[2] : out[3]);
+        if (a.cond && sample < a.batch)
+          reinterpret_cast<float4*>(a.cond)[sample * P + pix] = make_float4(re0, re1, out[2], out[3]);
+      }
+    };
     uint32_t p = 0, it_count = 0;
     for (int64_t it = blockIdx.x; it < n_items && !abort; it += gridDim.x, ++it_count) {
       const int64_t item = item_at(it);
       const int64_t tile = item / H;
       const int r = (int)(item % H);
-      const int64_t sample = tile * kTile + m;
       if (head && grp == 1 && it_count > 0 && !pwait(head_free, (it_count - 1) & 1, err, abort)) break;
       for (int c = 0; c < W && !abort; ++c, ++p) {
         if ((int)(p % C::kGroups) != grp) continue;
@@ -341,48 +443,15 @@ __global__ void __launch_bounds__(320, 1) op_pipe_kernel(const __grid_constant__
         for (int gq = 0; gq < F / 8; ++gq) st8(ca + ((int64_t)gq * kTile + m) * 8, cin + 8 * gq);
         fence_proxy_async_smem();
         mbar_arrive(&caf[b]);
-        if (!pwait(&cf[b], (p / NB) & 1, err, abort)) break;
-        tc_fence_after();
-        float out[32];
-        if (kind == kConvC)
-          tread<16>(tl, C::kChainCol + b * 32, out);
-        else
-          tread<NC2>(tl, C::kChainCol + b * 32, out);
-        tc_fence_before();
-        if (kind == kConvV) {
-#pragma unroll
-          for (int n = 0; n < F2; ++n) out[n] = fmaxf(out[n] + bc[n], 0.f);
-          if (r + 1 < H) store_row(blk<T>(a.cat, tile, P, pix + W, F), m, F2, F2, out);
-          if (r == 0) {
-#pragma unroll
-            for (int n = 0; n < F2; ++n) out[n] = fmaxf(bc[n], 0.f);
-            store_row(blk<T>(a.cat, tile, P, c, F), m, F2, F2, out);
-          }
-        } else if (kind == kConvH) {
-#pragma unroll
-          for (int n = 0; n < F2; ++n) out[n] = fmaxf(out[n] + bc[n], 0.f);
-          const int sh = a.last ? 1 : 0;
-          if (c + sh < W) store_row(blk<T>(a.cat, tile, P, pix + sh, F), m, 0, F2, out);
-          if (sh && c == 0) {
-#pragma unroll
-            for (int n = 0; n < F2; ++n) out[n] = fmaxf(bc[n], 0.f);
-            store_row(blk<T>(a.cat, tile, P, pix, F), m, 0, F2, out);
-          }
-        } else {
-#pragma unroll
-          for (int n = 0; n < 4; ++n) out[n] += bc[n];
-          // abstract_machine.py:56-57 normalisation (same arithmetic as the per-pixel engine)
-          float a2 = 2.f * out[0], b2 = 2.f * out[1];
-          float mx = fmaxf(a2, b2);
-          float lse = 0.5f * (mx + logf(expf(a2 - mx) + expf(b2 - mx)));
-          float re0 = out[0] - lse, re1 = out[1] - lse;
-          bool up = spin_at(a.spins, a.batch, P, sample, pix) > 0.f;
-          head_sm[c * kTile + m] = make_float2(up ? re0 : re1, up ? out[2] : out[3]);
-          if (a.cond && sample < a.batch)
-            reinterpret_cast<float4*>(a.cond)[sample * P + pix] = make_float4(re0, re1, out[2], out[3]);
-        }
+        if (pend) second_half();
+        pend = true;
+        pq = p;
+        ptile = tile;
+        pr = r;
+        pc = c;
       }
       if (head && !abort) {
+        if (pend) second_half();
         // ordered compensated sum over the row's pixels (the per-pixel engine's order)
         if (grp == 1) {
           mbar_arrive(head_ready);
@@ -398,6 +467,7 @@ __global__ void __launch_bounds__(320, 1) op_pipe_kernel(const __grid_constant__
         }
       }
     }
+    if (pend && !abort) second_half();
   }
   tc_fence_before();
   __syncthreads();
@@ -432,9 +502,9 @@ static int launch_pipe(const OpArgs& a, int64_t tiles, int H, int W, int* err, c
     attr = true;
   }
   const int64_t items = tiles * H;
-  int64_t grid = (int64_t)sms;  // one CTA per SM (512 TMEM columns, 320 threads)
+  int64_t grid = (int64_t)sms;  // one CTA per SM (512 TMEM columns)
   if (grid > items) grid = items;
-  op_pipe_kernel<F><<<(unsigned)grid, 320, smem, s>>>(a, H, W, items, err);
+  op_pipe_kernel<F><<<(unsigned)grid, kPipeThreads, smem, s>>>(a, H, W, items, err);
   return check_cuda(launched(), "op_pipe_kernel");
 }
 
