@@ -138,6 +138,18 @@ __device__ __forceinline__ void load_row(const T* block, int m, int c0, int n, f
   for (int g = 0; g < n / 8; ++g) ld8(block + ((int64_t)((c0 / 8) + g) * kTile + m) * 8, v + 8 * g);
 }
 
+// Raw 16-byte chunks of thread row m's n channels (bf16), unpacked later.
+template <int N>
+__device__ __forceinline__ void load_raw(const __nv_bfloat16* block, int m, uint4* r) {
+#pragma unroll
+  for (int g = 0; g < N / 8; ++g) r[g] = *reinterpret_cast<const uint4*>(block + ((int64_t)g * kTile + m) * 8);
+}
+template <int N>
+__device__ __forceinline__ void unpack_raw(const uint4* r, float* v) {
+#pragma unroll
+  for (int g = 0; g < N / 8; ++g) unpack_bf16x8(r[g], v + 8 * g);
+}
+
 // Tap offsets of the three ops (kernel element t = i*kw + j).
 __device__ __forceinline__ void tap_offset(int kind, int t, int& dr, int& dc) {
   if (kind == kConvV) {
@@ -165,5 +177,49 @@ int64_t tensor_bytes(const NetLayout& L, int64_t tiles, int channels);
 int launch_pipe_op(int F, const OpArgs& a, int64_t tiles, int H, int W, int* err, cudaStream_t s);
 bool pipe_supported(int F, int W);
 int64_t workspace_layout(const NetLayout& L, int64_t batch, int mode, char* base, Tensors* T);
+
+// ---------------------------------------------------------------- adjoint on tensor cores (F = 32)
+enum BwdKind { kBwdC = 0, kBwdV = 1, kBwdH = 2 };
+
+struct BwdOpArgs {
+  int kind;
+  const void* in;        // input gradient: gHp (C^T), gVp (V^T), gT (H^T)
+  const void* wt;        // transposed scatter operand of the conv
+  const void* wx;        // C^T: transposed operand of the x conv ([F/16][F][8])
+  const void* wy;        // C^T: transposed operand of the y conv
+  const void* cat;       // C^T: saved Cat (mask)
+  const void* t;         // C^T: saved T (mask of gT)
+  const void* rv;        // C^T: saved relu(Vp) (mask of gVp)
+  const void* gvs;       // C^T: stream gradient of V added into gVp (NULL on the final conv)
+  int shift;             // C^T: 1 on the final conv
+  void* gcatm;           // C^T out
+  void* gt;              // C^T out
+  void* gvp;             // C^T out
+  const void* res;       // V^T / H^T: residual gradient (NULL: none)
+  const void* prev;      // V^T / H^T: saved V_{i-1} / H_{i-1} (mask)
+  void* out;             // V^T / H^T out
+};
+
+struct WgTcArgs {
+  const void* X;      // activations (bf16 blocked, F channels)
+  int x_rows;         // ring rows of X: 3 (rows r-2..r) or 1
+  int x_row0;         // X row of ring row 0 relative to the item row
+  const void* G;      // output gradient (bf16 blocked, F channels)
+  int g0;             // first gradient channel used (multiple of 8)
+  int n;              // output channels of the conv (16 or 32)
+  int ntc;            // kernel columns: 3 or 1
+  int dc0;            // column offset of kernel column 0
+  float* part;        // [gridDim.x][x_rows * 32][ntc * n] per-CTA partial dW
+};
+
+int launch_bwd_op(const BwdOpArgs& a, int64_t tiles, int H, int W, int* err, cudaStream_t s);
+int64_t wgrad_tc_part_floats(int64_t tiles, int H);
+// dW: raw kernel gradient of the conv ([kh*kw*32][n]); kcol0: first kernel
+// column the launch covers (1x1 convs: 0).
+int launch_wgrad_tc(const WgTcArgs& a, int kw, int kcol0, float* dW, int64_t tiles, int H, int W, int* err,
+                    cudaStream_t s);
+// part: >= tiles * n floats of scratch
+int launch_bias_sum(const void* G, int64_t tiles, int P, int g0, int n, int64_t batch, float* part, float* db,
+                    cudaStream_t s);
 
 }  // namespace fk

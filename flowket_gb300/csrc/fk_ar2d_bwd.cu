@@ -21,6 +21,7 @@
 // gradients are fp32 throughout.
 #include "fk_ar2d.cuh"
 
+#include <stdlib.h>
 #include <string.h>
 
 namespace fk {
@@ -60,10 +61,10 @@ struct HeadBwdArgs {
   const float2* seeds;   // [batch]
   int64_t batch;
   float* gL;             // [tiles][P][8ch] fp32 (4 used)
-  float* ghp;            // [tiles][P][F] fp32
+  void* ghp;             // [tiles][P][F] (gradient type)
 };
 
-template <int F, typename T>
+template <int F, typename T, typename TG>
 __global__ void __launch_bounds__(128) head_bwd_kernel(const __grid_constant__ HeadBwdArgs a, int H, int W) {
   const int P = H * W;
   const int64_t tile = blockIdx.x / H;
@@ -97,7 +98,7 @@ __global__ void __launch_bounds__(128) head_bwd_kernel(const __grid_constant__ H
       for (int j = 0; j < 4; ++j) s += __ldg(a.wo + k * 4 + j) * gl[j];
       gh[k] = g[k] > 0.f ? s : 0.f;
     }
-    store_g(a.ghp, tile, P, pix, F, m, 0, F, gh);
+    store_row(blk<TG>(a.ghp, tile, P, pix, F), m, 0, F, gh);
   }
 }
 
@@ -260,7 +261,7 @@ struct WgArgs {
   const void* X;        // activations (act type), cin channels; NULL -> spins
   const int8_t* spins;
   int cin;
-  const float* G;       // fp32 blocked, gC channels; uses [g0, g0 + N)
+  const void* G;        // blocked (gradient type), gC channels; uses [g0, g0 + N)
   int gC, g0, N;
   float* dW;            // summed raw kernel gradient [ntaps*cin][N]
   float* dB;            // summed bias gradient [N]
@@ -272,7 +273,7 @@ struct WgArgs {
 
 constexpr int kItemsPerCta = 4;
 
-template <typename T>
+template <typename T, typename TG>
 __global__ void __launch_bounds__(128) wgrad_kernel(const __grid_constant__ WgArgs a, int H, int W) {
   __shared__ float red[4][64];
   const int P = H * W;
@@ -297,7 +298,7 @@ __global__ void __launch_bounds__(128) wgrad_kernel(const __grid_constant__ WgAr
     for (int r = 0; r < H; ++r) {
       for (int c = 0; c < W; ++c) {
         float g[8];
-        load_row(blk<float>(a.G, tile, P, r * W + c, a.gC), m, a.g0 + nc * 8, 8, g);
+        load_row(blk<TG>(a.G, tile, P, r * W + c, a.gC), m, a.g0 + nc * 8, 8, g);
         if (with_bias) {
 #pragma unroll
           for (int j = 0; j < 8; ++j) gb[j] += g[j];
@@ -472,7 +473,7 @@ static void tap_list(int kind, WgArgs& w) {
   }
 }
 
-template <typename T>
+template <typename T, typename TG = float>
 static int launch_wgrad(const NetLayout& L, WgArgs& w, const ConvDesc& cd, float* grad, float* O, int64_t batch,
                         cudaStream_t s) {
   int64_t tiles = (batch + kTile - 1) / kTile;
@@ -487,7 +488,7 @@ static int launch_wgrad(const NetLayout& L, WgArgs& w, const ConvDesc& cd, float
     w.dB = grad + cd.p_bias;
   }
   dim3 grid((unsigned)tiles, (unsigned)((w.items + kItemsPerCta - 1) / kItemsPerCta));
-  wgrad_kernel<T><<<grid, 128, 0, s>>>(w, L.H, L.W);
+  wgrad_kernel<T, TG><<<grid, 128, 0, s>>>(w, L.H, L.W);
   return check_cuda(launched(), "wgrad_kernel");
 }
 
@@ -513,7 +514,7 @@ static int backward_impl(const NetLayout& L, const void* packed, const float* pa
     h.batch = batch;
     h.gL = G.gl;
     h.ghp = G.ghp[last];
-    head_bwd_kernel<F, T><<<rows, 128, 0, s>>>(h, L.H, L.W);
+    head_bwd_kernel<F, T, float><<<rows, 128, 0, s>>>(h, L.H, L.W);
     FK_CUDA(launched());
     WgArgs w;
     memset(&w, 0, sizeof(w));
@@ -628,6 +629,197 @@ static int backward_impl(const NetLayout& L, const void* packed, const float* pa
   return FK_OK;
 }
 
+// ---------------------------------------------------------------- adjoint on tensor cores
+// Workspace of the tensor-core adjoint (BF16, F = 32, summed gradient): bf16
+// gradient tensors, the head gradient gL, and scratch for the per-CTA weight
+// gradient partials and the per-tile bias partials.
+struct TcBwdTensors {
+  void* gvs[40];   // masked stream gradient of V_i
+  void* ghp[40];   // masked gradient of Hp_i
+  void* gcatm;
+  void* gt;
+  void* gvp;
+  float* gl;
+  float* part;
+  float* bpart;
+  int64_t bytes;
+};
+
+static int64_t tc_bwd_layout(const NetLayout& L, int64_t batch, char* base, TcBwdTensors* T) {
+  const int64_t tiles = (batch + kTile - 1) / kTile;
+  const int64_t tb = tiles * L.P * (int64_t)kTile * L.F * 2;
+  int64_t off = 0;
+  auto take = [&](int64_t bytes) -> char* {
+    char* p = base ? base + off : nullptr;
+    off += (bytes + 255) / 256 * 256;
+    return p;
+  };
+  TcBwdTensors tmp;
+  TcBwdTensors* t = T ? T : &tmp;
+  memset(t, 0, sizeof(*t));
+  for (int i = 0; i < L.n_cc; ++i) {
+    t->gvs[i] = take(tb);
+    t->ghp[i] = take(tb);
+  }
+  t->gcatm = take(tb);
+  t->gt = take(tb);
+  t->gvp = take(tb);
+  t->gl = reinterpret_cast<float*>(take(tiles * L.P * (int64_t)kTile * 8 * 4));
+  t->part = reinterpret_cast<float*>(take(wgrad_tc_part_floats(tiles, L.H) * 4));
+  t->bpart = reinterpret_cast<float*>(take(tiles * 32 * 4));
+  t->bytes = off;
+  return off;
+}
+
+// FK_AR2D_ENGINE=rowwise also selects the CUDA-core adjoint (for comparisons).
+static bool use_tc_adjoint(const NetLayout& L) {
+  static int v = -1;
+  if (v < 0) {
+    const char* e = getenv("FK_AR2D_ENGINE");
+    v = (e && strcmp(e, "rowwise") == 0) ? 0 : 1;
+  }
+  return v == 1 && L.precision == FK_PRECISION_BF16 && L.F == 32 && pipe_supported(L.F, L.W);
+}
+
+static int backward_tc(const NetLayout& L, const void* packed, const float* params, const int8_t* spins,
+                       int64_t batch, const float* seeds, const Tensors& A, const TcBwdTensors& G, float* grad,
+                       cudaStream_t s) {
+  using T = __nv_bfloat16;
+  constexpr int F = 32;
+  const int64_t tiles = (batch + kTile - 1) / kTile;
+  const unsigned rows = (unsigned)(tiles * L.H);
+  const int last = L.n_cc - 1;
+  int* err = device_error_word();
+  int st;
+  auto wt = [&](int idx) { return static_cast<const char*>(packed) + L.conv[idx].wt_off; };
+  FK_CUDA(cudaMemsetAsync(grad, 0, (size_t)L.num_params * sizeof(float), s));
+  {
+    HeadBwdArgs h;
+    const int io = L.n_convs - 1;
+    h.hlast = A.h[last];
+    h.wo = w32(L, packed, io);
+    h.bo = reinterpret_cast<const float*>(static_cast<const char*>(packed) + L.conv[io].b_off);
+    h.spins = spins;
+    h.seeds = reinterpret_cast<const float2*>(seeds);
+    h.batch = batch;
+    h.gL = G.gl;
+    h.ghp = G.ghp[last];
+    head_bwd_kernel<F, T, T><<<rows, 128, 0, s>>>(h, L.H, L.W);
+    FK_CUDA(launched());
+    WgArgs w;
+    memset(&w, 0, sizeof(w));
+    w.ntaps = 1;
+    w.X = A.h[last];
+    w.cin = F;
+    w.G = G.gl;
+    w.gC = 8;
+    w.N = 4;
+    w.spins = spins;
+    if ((st = launch_wgrad<T, float>(L, w, L.conv[io], grad, nullptr, batch, s)) != FK_OK) return st;
+  }
+  auto wg = [&](const void* X, int x_rows, int x_row0, const void* Gt, int g0, int n, int ntc, int dc0,
+                const ConvDesc& cd) -> int {
+    WgTcArgs a;
+    a.X = X;
+    a.x_rows = x_rows;
+    a.x_row0 = x_row0;
+    a.G = Gt;
+    a.g0 = g0;
+    a.n = n;
+    a.ntc = ntc;
+    a.dc0 = dc0;
+    a.part = G.part;
+    int r = launch_wgrad_tc(a, cd.kw, 0, grad + cd.p_kernel, tiles, L.H, L.W, err, s);
+    if (r != FK_OK) return r;
+    return launch_bias_sum(Gt, tiles, L.P, g0, n, batch, G.bpart, grad + cd.p_bias, s);
+  };
+  for (int i = last; i >= 0; --i) {
+    const ConvDesc& cv = L.conv[conv_index(i, kConvV)];
+    const ConvDesc& ch = L.conv[conv_index(i, kConvH)];
+    const ConvDesc& cx = L.conv[conv_index(i, kConvX)];
+    const ConvDesc& cy = L.conv[conv_index(i, kConvY)];
+    const ConvDesc& cc = L.conv[conv_index(i, kConvC)];
+    const int shift = (i == last) ? 1 : 0;
+    {
+      BwdOpArgs b;
+      memset(&b, 0, sizeof(b));
+      b.kind = kBwdC;
+      b.in = G.ghp[i];
+      b.wt = wt(conv_index(i, kConvC));
+      b.wx = wt(conv_index(i, kConvX));
+      b.wy = wt(conv_index(i, kConvY));
+      b.cat = A.cat[i];
+      b.t = A.t[i];
+      b.rv = A.rv[i];
+      b.gvs = (i == last) ? nullptr : G.gvs[i];
+      b.shift = shift;
+      b.gcatm = G.gcatm;
+      b.gt = G.gt;
+      b.gvp = G.gvp;
+      if ((st = launch_bwd_op(b, tiles, L.H, L.W, err, s)) != FK_OK) return st;
+    }
+    // weight and bias gradients of the five convs of causal conv i
+    if ((st = wg(A.cat[i], 3, -2, G.ghp[i], 0, F, 3, -2, cc)) != FK_OK) return st;
+    if ((st = wg(A.t[i], 1, 0, G.gcatm, 0, F / 2, 1, -shift, cx)) != FK_OK) return st;
+    if ((st = wg(A.rv[i], 1, -1, G.gcatm, F / 2, F / 2, 1, 0, cy)) != FK_OK) return st;
+    if (i > 0) {
+      if ((st = wg(A.h[i - 1], 1, 0, G.gt, 0, F, 3, -2, ch)) != FK_OK) return st;
+      if ((st = wg(A.v[i - 1], 3, -2, G.gvp, 0, F, 3, -1, cv)) != FK_OK) return st;
+      // cc i = 2b+1 is the first conv of a block whose second conv (2b+2) adds
+      // the block input S_{2b} = S_{i-1} as residual
+      const bool block_first = (i % 2 == 1) && (i + 1 < last);
+      BwdOpArgs b;
+      memset(&b, 0, sizeof(b));
+      b.kind = kBwdV;
+      b.in = G.gvp;
+      b.wt = wt(conv_index(i, kConvV));
+      b.res = block_first ? G.gvs[i + 1] : nullptr;
+      b.prev = A.v[i - 1];
+      b.out = G.gvs[i - 1];
+      if ((st = launch_bwd_op(b, tiles, L.H, L.W, err, s)) != FK_OK) return st;
+      b.kind = kBwdH;
+      b.in = G.gt;
+      b.wt = wt(conv_index(i, kConvH));
+      b.res = block_first ? G.ghp[i + 1] : nullptr;
+      b.prev = A.h[i - 1];
+      b.out = G.ghp[i - 1];
+      if ((st = launch_bwd_op(b, tiles, L.H, L.W, err, s)) != FK_OK) return st;
+    } else {
+      // first causal conv: cin = 1 (spins), CUDA cores
+      WgArgs w;
+      memset(&w, 0, sizeof(w));
+      w.spins = spins;
+      tap_list(kConvH, w);
+      w.X = nullptr;
+      w.cin = 1;
+      w.G = G.gt;
+      w.gC = F;
+      w.N = F;
+      if ((st = launch_wgrad<T, T>(L, w, ch, grad, nullptr, batch, s)) != FK_OK) return st;
+      tap_list(kConvV, w);
+      w.G = G.gvp;
+      if ((st = launch_wgrad<T, T>(L, w, cv, grad, nullptr, batch, s)) != FK_OK) return st;
+    }
+  }
+  if (L.wn) {
+    for (int k = 0; k < L.n_convs - 1; ++k) {
+      const ConvDesc& cd = L.conv[k];
+      WnArgs a;
+      a.params = params;
+      a.p_kernel = cd.p_kernel;
+      a.p_g = cd.p_g;
+      a.K = cd.K;
+      a.N = cd.cout;
+      a.grad = grad;
+      a.O = nullptr;
+      a.batch = batch;
+      wn_kernel<<<(unsigned)((cd.cout + 127) / 128), 128, 0, s>>>(a);
+      FK_CUDA(launched());
+    }
+  }
+  return FK_OK;
+}
+
 }  // namespace fk
 
 using namespace fk;
@@ -637,7 +829,9 @@ extern "C" {
 int64_t fk_ar2d_backward_workspace_bytes(const fk_ar2d_desc* desc, int64_t batch) {
   NetLayout L;
   if (build_layout(desc, &L) != FK_OK || batch < 0) return -1;
-  return bwd_layout(L, batch, nullptr, nullptr);
+  const int64_t b = bwd_layout(L, batch, nullptr, nullptr);
+  const int64_t t = (L.precision == FK_PRECISION_BF16 && L.F == 32) ? tc_bwd_layout(L, batch, nullptr, nullptr) : 0;
+  return b > t ? b : t;
 }
 
 int fk_ar2d_backward(const fk_ar2d_desc* desc, const void* packed, const float* params, const int8_t* spins,
@@ -653,11 +847,18 @@ int fk_ar2d_backward(const fk_ar2d_desc* desc, const void* packed, const float* 
   int64_t need = workspace_layout(L, batch, FK_AR2D_SAVE, static_cast<char*>(const_cast<void*>(saved)), &A);
   FK_CHECK_ARG(saved_bytes >= need, "fk_ar2d_backward: saved workspace %lld < %lld bytes", (long long)saved_bytes,
                (long long)need);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!per_sample && use_tc_adjoint(L)) {
+    TcBwdTensors TG;
+    int64_t tneed = tc_bwd_layout(L, batch, static_cast<char*>(workspace), &TG);
+    FK_CHECK_ARG(workspace && workspace_bytes >= tneed, "fk_ar2d_backward: workspace %lld < %lld bytes",
+                 (long long)workspace_bytes, (long long)tneed);
+    return backward_tc(L, packed, params, spins, batch, w, A, TG, grad, s);
+  }
   BwdTensors G;
   int64_t gneed = bwd_layout(L, batch, static_cast<char*>(workspace), &G);
   FK_CHECK_ARG(workspace && workspace_bytes >= gneed, "fk_ar2d_backward: workspace %lld < %lld bytes",
                (long long)workspace_bytes, (long long)gneed);
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
   float* O = per_sample;
   float* g = per_sample ? nullptr : grad;
   const bool bf = L.precision == FK_PRECISION_BF16;

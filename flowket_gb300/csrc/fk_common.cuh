@@ -147,6 +147,12 @@ __host__ __device__ constexpr uint32_t umma_idesc_bf16(int m, int n) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
 
+// Same with both operands MN-major: A element (m, k) at (m/8)*sbo + (k/8)*lbo +
+// (k%8)*16B + (m%8)*2B, i.e. 8 consecutive M (or N) elements per 16 bytes.
+__host__ __device__ constexpr uint32_t umma_idesc_bf16_mn(int m, int n) {
+  return umma_idesc_bf16(m, n) | (1u << 15) | (1u << 16);
+}
+
 // Shared-memory matrix descriptor, no swizzle, K-major "interleaved" layout:
 // element (row, k) at start + (row/8)*sbo + (row%8)*16B + (k/8)*lbo + (k%8)*2B.
 __device__ __forceinline__ uint64_t umma_sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
@@ -172,6 +178,16 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// Stores 16 zero columns [taddr, taddr+16) of this thread's lane.
+__device__ __forceinline__ void tmem_zero16(uint32_t taddr) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+      "{%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1};" ::"r"(taddr),
+      "r"(0u)
+      : "memory");
+}
+__device__ __forceinline__ void tmem_st_wait() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 // ---------------------------------------------------------------- bf16 packing
 __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {

@@ -1,0 +1,248 @@
+// Column-scatter pipeline shared by the AR2D forward ops (fk_ar2d_pipe.cu)
+// and the data-gradient ops of the adjoint (fk_ar2d_bwd_tc.cu).
+//
+// One persistent CTA per SM walks (tile, row) items; each item is one lattice
+// row of 128 samples. Input column x of an item (nrows lattice rows, one
+// [F/8][128][8] bf16 block each) is multiplied once per kernel row by the
+// three kernel columns stacked along N (N = 3F): the product holds x's
+// contributions to the three output columns x + o0 .. x + o0 + 2, which
+// accumulate in three consecutive F-column slots of a TMEM ring. Output c is
+// complete after input column min(c - o0, W - 1).
+//
+// Roles (warps of the CTA):
+//   producer (one thread): bulk copies of the weights once, then of every
+//       input column into a ring of column slots;
+//   waiter (whole warp): observes the barriers each column needs (column
+//       loaded, TMEM slots of the outputs it starts released by the
+//       epilogue), then releases the column to the issuer through named
+//       barrier 1, which also carries an abort flag;
+//   issuer (whole warp, lane 0 issues): tcgen05.mma over the column and
+//       commits. This thread performs no memory load while MMAs stream: a
+//       load in the issuing thread -- an mbarrier wait included -- stalls the
+//       tensor pipe for hundreds of cycles.
+// The accumulation order of an output is: input columns ascending, kernel
+// rows ascending in ring order, K steps ascending.
+#pragma once
+
+#include "fk_ar2d.cuh"
+
+namespace fk {
+
+template <int F>
+struct PipeCfg {
+  static constexpr int kBlk = kTile * F * 2;        // one [F/8][128][8] bf16 block
+  static constexpr int kNcol = F <= 16 ? 8 : 6;     // input column slots
+  static constexpr int kRing = 3 * kNcol * kBlk;
+  static constexpr int kWRow = F * 3 * F * 2;       // one kernel row of the scatter operand
+  static constexpr int kW = 3 * kWRow;
+  static constexpr int kGroups = 2;                 // epilogue groups (alternate outputs)
+  static constexpr int kNB = 2 * kGroups;           // chained-conv staging buffers
+  static constexpr int kCA = kNB * kTile * F * 2;
+  static constexpr int kNS = 256 / F;               // TMEM accumulator slots (F columns each)
+  static constexpr uint32_t kChainCol = 256;        // chained accumulators start here
+  static constexpr int kBars = 1024;
+};
+
+constexpr int kPipeThreads = 384;  // 12 warps: producer, issuer, waiter, chain issuer, 8 epilogue
+
+// Geometry of one op: ring row k of an item at lattice row r holds input row
+// r + row0 + k (k < nrows); its kernel row is k, or nrows - 1 - k when rev.
+struct PipeGeom {
+  int H, W;
+  int nrows, row0, o0;
+  int rev;
+};
+
+__device__ __forceinline__ bool pwait(uint64_t* bar, uint32_t parity, int* err, bool& abort) {
+  if (abort) return false;
+  if (!mbar_wait(bar, parity, err)) {
+    abort = true;
+    return false;
+  }
+  return true;
+}
+
+template <int N>
+__device__ __forceinline__ void tread(uint32_t taddr_lane, uint32_t col, float* v) {
+#pragma unroll
+  for (int q = 0; q < N / 16; ++q) tmem_ld16(taddr_lane + col + q * 16, v + q * 16);
+  tmem_ld_wait();
+}
+
+// Barrier 1 of the CTA: rendezvous of the waiter warp and the issuer warp,
+// one per input column, returning the OR of both warps' abort flags.
+__device__ __forceinline__ bool step_rendezvous(bool abort) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.u32 p, %1, 0;\n\t"
+      "barrier.cta.red.or.pred q, 1, 64, p;\n\t"
+      "selp.u32 %0, 1, 0, q;\n\t}"
+      : "=r"(r)
+      : "r"((uint32_t)abort)
+      : "memory");
+  return r != 0;
+}
+
+struct PipeItems {
+  const int32_t* items;  // work list (NULL: item k = k)
+  int64_t n;
+  __device__ __forceinline__ int64_t at(int64_t k) const { return items ? (int64_t)items[k] : k; }
+};
+
+// In-lattice ring rows [k_lo, k_hi] of an item at row r.
+__device__ __forceinline__ void ring_rows(const PipeGeom& g, int r, int& k_lo, int& k_hi) {
+  k_lo = -(r + g.row0) > 0 ? -(r + g.row0) : 0;
+  k_hi = g.H - 1 - r - g.row0 < g.nrows - 1 ? g.H - 1 - r - g.row0 : g.nrows - 1;
+}
+
+// A weight region copied once into shared memory.
+struct WeightCopy {
+  uint8_t* dst;
+  const void* src;
+  uint32_t bytes;  // 0: none
+};
+
+// Producer (one thread): up to three weight regions once, then every input
+// column of every item into the ring.
+template <int F>
+__device__ void pipe_producer(const PipeGeom& g, const PipeItems& items, const void* in, uint8_t* ring,
+                              uint64_t* full, uint64_t* empty, uint64_t* wbar, WeightCopy w1, WeightCopy w2,
+                              WeightCopy w3, int* err, bool& abort) {
+  using C = PipeCfg<F>;
+  constexpr int NR = C::kNcol;
+  mbar_arrive_expect_tx(wbar, w1.bytes + w2.bytes + w3.bytes);
+  if (w1.bytes) bulk_g2s(w1.dst, w1.src, w1.bytes, wbar);
+  if (w2.bytes) bulk_g2s(w2.dst, w2.src, w2.bytes, wbar);
+  if (w3.bytes) bulk_g2s(w3.dst, w3.src, w3.bytes, wbar);
+  const int P = g.H * g.W;
+  uint32_t gc = 0;
+  for (int64_t it = blockIdx.x; it < items.n && !abort; it += gridDim.x) {
+    const int64_t item = items.at(it);
+    const int64_t tile = item / g.H;
+    const int r = (int)(item % g.H);
+    int k_lo, k_hi;
+    ring_rows(g, r, k_lo, k_hi);
+    for (int x = 0; x < g.W && !abort; ++x, ++gc) {
+      const uint32_t slot = gc % NR;
+      if (gc >= NR && !pwait(&empty[slot], ((gc / NR) - 1) & 1, err, abort)) break;
+      mbar_arrive_expect_tx(&full[slot], (uint32_t)(k_hi - k_lo + 1) * C::kBlk);
+      for (int k = k_lo; k <= k_hi; ++k)
+        bulk_g2s(ring + (slot * 3 + k) * C::kBlk,
+                 blk<__nv_bfloat16>(in, tile, P, (r + g.row0 + k) * g.W + x, F), C::kBlk, &full[slot]);
+    }
+  }
+}
+
+// Waiter (whole warp).
+template <int F>
+__device__ void pipe_waiter(const PipeGeom& g, const PipeItems& items, uint64_t* full, uint64_t* wbar,
+                            uint64_t* acce, int* err, bool& abort) {
+  using C = PipeCfg<F>;
+  constexpr int NR = C::kNcol;
+  constexpr int NS = C::kNS;
+  pwait(wbar, 0, err, abort);
+  uint32_t gx = 0, gbase = 0;
+  bool stop = false;
+  for (int64_t it = blockIdx.x; it < items.n && !stop; it += gridDim.x) {
+    for (int x = 0; x < g.W; ++x, ++gx) {
+      pwait(&full[gx % NR], (gx / NR) & 1, err, abort);
+      const int c_lo = x + g.o0 < 0 ? 0 : x + g.o0;
+      const int c_hi = x + g.o0 + 2 < g.W - 1 ? x + g.o0 + 2 : g.W - 1;
+      const int c_f = x == 0 ? c_lo : (x + g.o0 + 2 < c_hi + 1 ? x + g.o0 + 2 : c_hi + 1);
+      for (int c = c_f; c <= c_hi; ++c) {
+        const uint32_t p = gbase + (uint32_t)c;
+        if (p >= (uint32_t)NS) pwait(&acce[p % NS], ((p / NS) - 1) & 1, err, abort);
+      }
+      stop = step_rendezvous(abort);
+      if (stop) break;
+    }
+    gbase += (uint32_t)g.W;
+  }
+  abort = stop || abort;
+}
+
+// Issuer (whole warp; lane 0 issues). `w0` is the descriptor of kernel row 0
+// of the scatter operand ([F/8][3F][8] per kernel row).
+template <int F>
+__device__ void pipe_issuer(const PipeGeom& g, const PipeItems& items, uint8_t* ring, uint8_t* wsm,
+                            uint32_t tmem, uint64_t* empty, uint64_t* accf, uint64_t* drain, int* err,
+                            bool& abort) {
+  using C = PipeCfg<F>;
+  constexpr int NR = C::kNcol;
+  constexpr int NS = C::kNS;
+  const int lane = threadIdx.x % 32;
+  const uint32_t idesc1 = umma_idesc_bf16(128, F);
+  const uint32_t idesc2 = umma_idesc_bf16(128, 2 * F);
+  const uint32_t idesc3 = umma_idesc_bf16(128, 3 * F);
+  const uint64_t a0 = umma_sdesc(smem_u32(ring), 2048, 128);
+  const uint64_t w0 = umma_sdesc(smem_u32(wsm), 3 * F * 16, 128);
+  constexpr uint32_t kBlk16 = C::kBlk >> 4;           // one ring block
+  constexpr uint32_t kRow16 = C::kWRow >> 4;          // one kernel row of the scatter operand
+  constexpr uint32_t kKs16 = (2 * 2048) >> 4;         // one K=16 step of A
+  constexpr uint32_t kKsW16 = (2 * 3 * F * 16) >> 4;  // one K=16 step of B
+  const int W = g.W, o0 = g.o0;
+  uint32_t cs = 0;     // ring slot of the current column
+  uint32_t gbase = 0;  // global index of output column 0 of the current item
+  int64_t next_item = blockIdx.x < items.n ? items.at(blockIdx.x) : 0;
+  for (int64_t it = blockIdx.x; it < items.n && !abort; it += gridDim.x) {
+    const int r = (int)(next_item % g.H);
+    if (it + gridDim.x < items.n) next_item = items.at(it + gridDim.x);  // used one item later
+    int k_lo, k_hi;
+    ring_rows(g, r, k_lo, k_hi);
+    for (int x = 0; x < W; ++x) {
+      abort = step_rendezvous(false);
+      if (abort) break;
+      tc_fence_after();
+      const int c_lo = x + o0 < 0 ? 0 : x + o0;
+      const int c_hi = x + o0 + 2 < W - 1 ? x + o0 + 2 : W - 1;
+      // outputs first reached by this column, [c_f, c_hi]: all of them at
+      // x == 0, else output x + o0 + 2 if it exists
+      const int c_f = x == 0 ? c_lo : (x + o0 + 2 < c_hi + 1 ? x + o0 + 2 : c_hi + 1);
+      if (lane == 0) {
+        // one MMA per (ring row, K step) over outputs [ca, cb], split where
+        // the TMEM slot ring wraps
+        auto mma = [&](int ca, int cb, uint32_t aoff, uint32_t boff, uint32_t acc) {
+          while (ca <= cb) {
+            const uint32_t s = (gbase + (uint32_t)ca) % NS;
+            int n = cb - ca + 1;
+            if (n > NS - (int)s) n = NS - (int)s;
+            const uint32_t id = n == 3 ? idesc3 : (n == 2 ? idesc2 : idesc1);
+            umma_bf16(tmem + s * F, a0 + aoff, w0 + boff + (uint32_t)((ca - x - o0) * F), id, acc);
+            ca += n;
+          }
+        };
+        bool first = true;
+        for (int k = k_lo; k <= k_hi; ++k) {
+          const uint32_t krow = g.rev ? (uint32_t)(g.nrows - 1 - k) : (uint32_t)k;
+#pragma unroll
+          for (int ks = 0; ks < F / 16; ++ks) {
+            const uint32_t aoff = (cs * 3 + (uint32_t)k) * kBlk16 + ks * kKs16;
+            const uint32_t boff = krow * kRow16 + ks * kKsW16;
+            if (first) {
+              if (c_f > c_lo) mma(c_lo, c_f - 1, aoff, boff, 1u);
+              mma(c_f, c_hi, aoff, boff, 0u);
+              first = false;
+            } else {
+              mma(c_lo, c_hi, aoff, boff, 1u);
+            }
+          }
+        }
+        umma_commit(&empty[cs]);
+        // outputs completed by this column
+        const int d_lo = x + o0 < 0 ? 0 : x + o0;
+        const int d_hi = x == W - 1 ? W - 1 : x + o0;
+        for (int c = d_lo; c <= d_hi; ++c) umma_commit(&accf[(gbase + (uint32_t)c) % NS]);
+      }
+      __syncwarp();
+      cs = cs + 1 == (uint32_t)NR ? 0 : cs + 1;
+    }
+    gbase += (uint32_t)W;
+  }
+  if (lane == 0) {
+    umma_commit(drain);
+    mbar_wait(drain, 0, err);
+  }
+}
+
+}  // namespace fk

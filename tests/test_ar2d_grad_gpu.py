@@ -1,10 +1,17 @@
 """Adjoint kernel: gradients against the oracle's autograd (float64).
 
 Tolerances: FP32 path ||g - g_ref|| / ||g_ref|| < 1e-4. BF16 path (bf16
-activations from the tensor-core forward, fp32 weights and gradients): the
-stated bound is ||g - g_ref|| / ||g_ref|| < 1e-1 with cosine similarity
-> 0.995, for random +-seeds (which maximise cancellation between samples).
+activations from the tensor-core forward, fp32 weights and gradients; with
+F = 32 the adjoint itself runs on tensor cores with bf16 gradients between
+its ops): the stated bound is ||g - g_ref|| / ||g_ref|| < 1e-1 with cosine
+similarity > 0.995, for random +-seeds (which maximise cancellation between
+samples). The tensor-core adjoint against the CUDA-core adjoint on the same
+bf16 activations: relative difference < 3e-2, cosine > 0.999.
 """
+import os
+import subprocess
+import sys
+
 import numpy as np
 import pytest
 import torch
@@ -41,7 +48,10 @@ def test_gradient_fp32_matches_autograd(cuda, shape, depth, f, wn):
     assert rel < 1e-4, rel
 
 
-@pytest.mark.parametrize("shape,depth,f,wn", CASES[:2])
+BF16_CASES = CASES[:2] + [((10, 10), 10, 32, True), ((1, 12), 4, 32, True), ((6, 3), 5, 32, True)]
+
+
+@pytest.mark.parametrize("shape,depth,f,wn", BF16_CASES)
 def test_gradient_bf16_within_bound(cuda, shape, depth, f, wn):
     m, s, sc, w, saved = _setup(shape, depth, f, wn, "bf16")
     got = m.backward(sc, w, saved).cpu().numpy().astype(np.float64)
@@ -80,3 +90,41 @@ def test_sampler_activations_feed_the_adjoint(cuda, precision):
     _, _, saved2 = m.forward(spins, mode=_lib.FK_AR2D_SAVE)
     g2 = m.backward(spins, w, saved2)
     assert torch.equal(g1, g2)
+
+
+@pytest.mark.parametrize("shape,depth", [((5, 7), 4), ((10, 10), 10)])
+def test_tensor_core_adjoint_matches_cuda_core_adjoint(cuda, tmp_path, shape, depth):
+    """F = 32, BF16: the tcgen05 adjoint (bf16 gradients between ops,
+    deterministic sums) against the CUDA-core adjoint on the same saved
+    activations (FK_AR2D_ENGINE=rowwise selects the CUDA-core adjoint and the
+    per-pixel forward, which computes bitwise the same activations)."""
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = (
+        "import sys; sys.path.insert(0, %r);"
+        "import numpy as np, torch;"
+        "from flowket_gb300 import _lib;"
+        "from flowket_gb300.machines import ConvNetAutoregressive2D;"
+        "m = ConvNetAutoregressive2D(%r, %d, 32, weights_normalization=True, precision='bf16', seed=5);"
+        "rng = np.random.default_rng(6);"
+        "s = torch.as_tensor(rng.choice([-1, 1], size=(300,) + %r).astype(np.int8)).cuda();"
+        "w = torch.as_tensor(rng.normal(size=(300, 2)).astype(np.float32)).cuda();"
+        "_, _, saved = m.forward(s, mode=_lib.FK_AR2D_SAVE);"
+        "np.save(%r, m.backward(s, w, saved).cpu().numpy())"
+    ) % (root, shape, depth, shape, str(tmp_path / "g.npy"))
+    env = dict(os.environ, FK_AR2D_ENGINE="rowwise")
+    subprocess.run([sys.executable, "-c", code], check=True, env=env)
+    ref = np.load(tmp_path / "g.npy").astype(np.float64)
+    from flowket_gb300 import _lib
+    from flowket_gb300.machines import ConvNetAutoregressive2D
+    m = ConvNetAutoregressive2D(shape, depth, 32, weights_normalization=True, precision="bf16", seed=5)
+    rng = np.random.default_rng(6)
+    s = torch.as_tensor(rng.choice([-1, 1], size=(300,) + shape).astype(np.int8)).cuda()
+    w = torch.as_tensor(rng.normal(size=(300, 2)).astype(np.float32)).cuda()
+    _, _, saved = m.forward(s, mode=_lib.FK_AR2D_SAVE)
+    g1 = m.backward(s, w, saved).clone()
+    g2 = m.backward(s, w, saved)
+    assert torch.equal(g1, g2)  # fixed-order sums: deterministic
+    got = g1.cpu().numpy().astype(np.float64)
+    rel = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+    cos = got @ ref / (np.linalg.norm(got) * np.linalg.norm(ref))
+    assert rel < 3e-2 and cos > 0.999, (rel, cos)
