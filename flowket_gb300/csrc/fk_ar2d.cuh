@@ -210,16 +210,20 @@ struct WgTcArgs {
   int ntc;            // kernel columns: 3 or 1
   int dc0;            // column offset of kernel column 0
   float* part;        // [gridDim.x][x_rows * 32][ntc * n] per-CTA partial dW
+  int bias_jpos;      // column block whose ones-row sum is the bias gradient (-1: none)
+  float* part_bias;   // [gridDim.x][n] per-CTA partial bias gradient
 };
 
 int launch_bwd_op(const BwdOpArgs& a, int64_t tiles, int H, int W, int* err, cudaStream_t s);
-int64_t wgrad_tc_part_floats(int64_t tiles, int H);
+int64_t wgrad_tc_grid(int64_t tiles, int H);        // CTAs (and partials) of a weight-gradient launch
+int64_t wgrad_tc_part_floats(int64_t tiles, int H);  // partial dW (3*32*96 per CTA) then partial bias (32 per CTA)
 // dW: raw kernel gradient of the conv ([kh*kw*32][n]); kcol0: first kernel
 // column the launch covers (1x1 convs: 0).
-int launch_wgrad_tc(const WgTcArgs& a, int kw, int kcol0, float* dW, int64_t tiles, int H, int W, int* err,
-                    cudaStream_t s);
-// part: >= tiles * n floats of scratch
-int launch_bias_sum(const void* G, int64_t tiles, int P, int g0, int n, int64_t batch, float* part, float* db,
+// db: bias gradient when a.bias_jpos >= 0.
+int launch_wgrad_tc(const WgTcArgs& a, int kw, int kcol0, float* dW, float* db, int64_t tiles, int H, int W,
+                    int* err, cudaStream_t s);
+// part: >= tiles * H * n floats of scratch
+int launch_bias_sum(const void* G, int64_t tiles, int H, int W, int g0, int n, int64_t batch, float* part, float* db,
                     cudaStream_t s);
 
 }  // namespace fk

@@ -375,41 +375,63 @@ __global__ void __launch_bounds__(128) wgrad_kernel(const __grid_constant__ WgAr
   }
 }
 
-// Weight-normalisation chain rule for one conv. Summed: one thread per output
-// channel. Per-sample: one thread per (output channel, sample) on the O rows.
+// Weight-normalisation chain rule, all weight-normalised convs in one launch
+// (blockIdx.y = conv). Summed: one thread per output channel. Per-sample: one
+// thread per (output channel, sample) on the O rows.
 struct WnArgs {
   const float* params;
-  int64_t p_kernel, p_g;
-  int K, N;
-  float* grad;     // summed: flat gradient (kernel slot holds dW on entry)
-  float* O;        // per-sample rows (kernel slot holds dW on entry)
+  float* grad;     // summed: flat gradient (kernel slots hold dW on entry)
+  float* O;        // per-sample rows (kernel slots hold dW on entry)
   int64_t batch;
+  ConvDesc conv[kMaxConvs];
 };
 
 __global__ void wn_kernel(const __grid_constant__ WnArgs a) {
+  const ConvDesc& cd = a.conv[blockIdx.y];
+  const int N = cd.cout, K = cd.K;
+  const int64_t p_kernel = cd.p_kernel, p_g = cd.p_g;
   int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  int64_t cols = a.O ? (int64_t)a.N * a.batch : a.N;
+  int64_t cols = a.O ? (int64_t)N * a.batch : N;
   if (idx >= cols) return;
-  int n = (int)(idx % a.N);
-  int64_t b = idx / a.N;
-  const float* v = a.params + a.p_kernel;
+  int n = (int)(idx % N);
+  int64_t b = idx / N;
+  const float* v = a.params + p_kernel;
   float sq = 0.f;
-  for (int k = 0; k < a.K; ++k) sq += v[(int64_t)k * a.N + n] * v[(int64_t)k * a.N + n];
+  for (int k = 0; k < K; ++k) sq += v[(int64_t)k * N + n] * v[(int64_t)k * N + n];
   float inv = rsqrtf(fmaxf(sq, 1e-12f));
-  float eg = expf(a.params[a.p_g + n]);
+  float eg = expf(a.params[p_g + n]);
   auto at = [&](int k) -> float& {
-    return a.O ? a.O[(a.p_kernel + (int64_t)k * a.N + n) * a.batch + b] : a.grad[a.p_kernel + (int64_t)k * a.N + n];
+    return a.O ? a.O[(p_kernel + (int64_t)k * N + n) * a.batch + b] : a.grad[p_kernel + (int64_t)k * N + n];
   };
   float dot = 0.f;
-  for (int k = 0; k < a.K; ++k) dot += at(k) * v[(int64_t)k * a.N + n] * inv;
-  for (int k = 0; k < a.K; ++k) {
-    float u = v[(int64_t)k * a.N + n] * inv;
+  for (int k = 0; k < K; ++k) dot += at(k) * v[(int64_t)k * N + n] * inv;
+  for (int k = 0; k < K; ++k) {
+    float u = v[(int64_t)k * N + n] * inv;
     at(k) = eg * inv * (at(k) - u * dot);
   }
   if (a.O)
-    a.O[(a.p_g + n) * a.batch + b] = eg * dot;
+    a.O[(p_g + n) * a.batch + b] = eg * dot;
   else
-    a.grad[a.p_g + n] = eg * dot;
+    a.grad[p_g + n] = eg * dot;
+}
+
+// Every conv but the head (not weight-normalised).
+static int launch_wn(const NetLayout& L, const float* params, float* grad, float* O, int64_t batch, cudaStream_t s) {
+  WnArgs* a = new WnArgs;
+  a->params = params;
+  a->grad = grad;
+  a->O = O;
+  a->batch = batch;
+  int maxc = 0;
+  for (int k = 0; k < L.n_convs - 1; ++k) {
+    a->conv[k] = L.conv[k];
+    maxc = maxc > L.conv[k].cout ? maxc : L.conv[k].cout;
+  }
+  const int64_t cols = O ? (int64_t)maxc * batch : maxc;
+  dim3 grid((unsigned)((cols + 127) / 128), (unsigned)(L.n_convs - 1));
+  wn_kernel<<<grid, 128, 0, s>>>(*a);
+  delete a;
+  return check_cuda(launched(), "wn_kernel");
 }
 
 // ---------------------------------------------------------------- driver
@@ -609,23 +631,7 @@ static int backward_impl(const NetLayout& L, const void* packed, const float* pa
       FK_CUDA(launched());
     }
   }
-  if (L.wn) {
-    for (int k = 0; k < L.n_convs - 1; ++k) {
-      const ConvDesc& cd = L.conv[k];
-      WnArgs a;
-      a.params = params;
-      a.p_kernel = cd.p_kernel;
-      a.p_g = cd.p_g;
-      a.K = cd.K;
-      a.N = cd.cout;
-      a.grad = grad;
-      a.O = O;
-      a.batch = batch;
-      int64_t cols = O ? (int64_t)cd.cout * batch : cd.cout;
-      wn_kernel<<<(unsigned)((cols + 127) / 128), 128, 0, s>>>(a);
-      FK_CUDA(launched());
-    }
-  }
+  if (L.wn) return launch_wn(L, params, grad, O, batch, s);
   return FK_OK;
 }
 
@@ -666,7 +672,7 @@ static int64_t tc_bwd_layout(const NetLayout& L, int64_t batch, char* base, TcBw
   t->gvp = take(tb);
   t->gl = reinterpret_cast<float*>(take(tiles * L.P * (int64_t)kTile * 8 * 4));
   t->part = reinterpret_cast<float*>(take(wgrad_tc_part_floats(tiles, L.H) * 4));
-  t->bpart = reinterpret_cast<float*>(take(tiles * 32 * 4));
+  t->bpart = reinterpret_cast<float*>(take(tiles * L.H * 32 * 4));
   t->bytes = off;
   return off;
 }
@@ -729,9 +735,12 @@ static int backward_tc(const NetLayout& L, const void* packed, const float* para
     a.ntc = ntc;
     a.dc0 = dc0;
     a.part = G.part;
-    int r = launch_wgrad_tc(a, cd.kw, 0, grad + cd.p_kernel, tiles, L.H, L.W, err, s);
-    if (r != FK_OK) return r;
-    return launch_bias_sum(Gt, tiles, L.P, g0, n, batch, G.bpart, grad + cd.p_bias, s);
+    // the G column block that meets every output column once, at x = its column
+    a.bias_jpos = dc0 + ntc - 1;
+    a.part_bias = G.part + wgrad_tc_grid(tiles, L.H) * (3 * 32 * 96);
+    int r = launch_wgrad_tc(a, cd.kw, 0, grad + cd.p_kernel, grad + cd.p_bias, tiles, L.H, L.W, err, s);
+    if (r != FK_OK || a.bias_jpos >= 0) return r;
+    return launch_bias_sum(Gt, tiles, L.H, L.W, g0, n, batch, G.bpart, grad + cd.p_bias, s);
   };
   for (int i = last; i >= 0; --i) {
     const ConvDesc& cv = L.conv[conv_index(i, kConvV)];
@@ -801,22 +810,7 @@ static int backward_tc(const NetLayout& L, const void* packed, const float* para
       if ((st = launch_wgrad<T, T>(L, w, cv, grad, nullptr, batch, s)) != FK_OK) return st;
     }
   }
-  if (L.wn) {
-    for (int k = 0; k < L.n_convs - 1; ++k) {
-      const ConvDesc& cd = L.conv[k];
-      WnArgs a;
-      a.params = params;
-      a.p_kernel = cd.p_kernel;
-      a.p_g = cd.p_g;
-      a.K = cd.K;
-      a.N = cd.cout;
-      a.grad = grad;
-      a.O = nullptr;
-      a.batch = batch;
-      wn_kernel<<<(unsigned)((cd.cout + 127) / 128), 128, 0, s>>>(a);
-      FK_CUDA(launched());
-    }
-  }
+  if (L.wn) return launch_wn(L, params, grad, nullptr, batch, s);
   return FK_OK;
 }
 

@@ -317,11 +317,19 @@ __global__ void __launch_bounds__(kWgThreads, 1) wgrad_tc_kernel(const __grid_co
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tslot;
-  // zero the accumulator (rows = lanes, 96 columns)
+  // zero the accumulator (rows = lanes, 96 columns); the spare fourth block
+  // of every X slot holds ones, so accumulator rows 96..127 collect the
+  // column sums of G over the samples: the bias gradient (see a.bias).
   if (warp >= 4) {
     const uint32_t tl = tmem + ((uint32_t)((warp % 4) * 32) << 16);
     for (int c0 = 0; c0 < 96; c0 += 16) tmem_zero16(tl + c0);
     tmem_st_wait();
+    const uint4 one8 = make_uint4(0x3F803F80u, 0x3F803F80u, 0x3F803F80u, 0x3F803F80u);  // bf16 1.0 x 8
+    for (int i = threadIdx.x - 128; i < C::kNX * (C::kBlk / 16); i += 128) {
+      const int slot = i / (C::kBlk / 16), e = i % (C::kBlk / 16);
+      reinterpret_cast<uint4*>(xr + (slot * 4 + 3) * C::kBlk)[e] = one8;
+    }
+    fence_proxy_async_smem();
   }
   tc_fence_before();
   __syncthreads();
@@ -420,8 +428,8 @@ __global__ void __launch_bounds__(kWgThreads, 1) wgrad_tc_kernel(const __grid_co
     const int q4 = warp % 4;  // lane quarter = stacked row block = kernel row of ring row q4
     pwait(done, 0, err, abort);
     tc_fence_after();
+    const uint32_t tl = tmem + ((uint32_t)(q4 * 32) << 16);
     if (!abort && q4 < a.x_rows) {
-      const uint32_t tl = tmem + ((uint32_t)(q4 * 32) << 16);
       float* dst = a.part + ((int64_t)blockIdx.x * a.x_rows * 32 + q4 * 32 + lane) * (ntc * n);
       for (int c0 = 0; c0 < ntc * n; c0 += 16) {
         float v[16];
@@ -429,6 +437,19 @@ __global__ void __launch_bounds__(kWgThreads, 1) wgrad_tc_kernel(const __grid_co
         tmem_ld_wait();
 #pragma unroll
         for (int j = 0; j < 16; ++j) dst[c0 + j] = v[j];
+      }
+    }
+    if (!abort && q4 == 3 && a.bias_jpos >= 0) {
+      // row 96 (all rows of the ones block are equal): column block bias_jpos
+      // meets every G column exactly once, at input column x = its column
+      float* dst = a.part_bias + (int64_t)blockIdx.x * n;
+      for (int c0 = 0; c0 < n; c0 += 16) {
+        float v[16];
+        tmem_ld16(tl + a.bias_jpos * n + c0, v);
+        tmem_ld_wait();
+        if (lane == 0)
+#pragma unroll
+          for (int j = 0; j < 16; ++j) dst[c0 + j] = v[j];
       }
     }
   }
@@ -443,10 +464,17 @@ __global__ void __launch_bounds__(kWgThreads, 1) wgrad_tc_kernel(const __grid_co
 // Sums the per-CTA partials in CTA order into the raw kernel gradient
 // dW[((i*kw + j)*cin + ci)*n + co] (i = kernel row, j = kernel column).
 __global__ void wgrad_reduce_kernel(const float* part, int parts, int x_rows, int ntc, int n, int kw, int kcol0,
-                                    float* dW) {
+                                    float* dW, const float* part_bias, float* db) {
   const int per = x_rows * 32 * ntc * n;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= per) return;
+  if (e >= per) {
+    if (db && e < per + n) {
+      float s = 0.f;
+      for (int b = 0; b < parts; ++b) s += part_bias[(int64_t)b * n + (e - per)];
+      db[e - per] = s;
+    }
+    return;
+  }
   float s = 0.f;
   for (int b = 0; b < parts; ++b) s += part[(int64_t)b * per + e];
   const int row = e / (ntc * n), col = e % (ntc * n);
@@ -459,17 +487,19 @@ __global__ void wgrad_reduce_kernel(const float* part, int parts, int x_rows, in
 // Bias gradient, step 1: per tile (one CTA, thread = sample) the sum over
 // pixels of G[.., g0 + co], reduced over the tile's samples; step 2 sums the
 // tiles in order.
-__global__ void __launch_bounds__(128) bias_tile_kernel(const __nv_bfloat16* G, int P, int g0, int n, int64_t batch,
-                                                        float* part) {
+__global__ void __launch_bounds__(128) bias_tile_kernel(const __nv_bfloat16* G, int P, int W, int g0, int n,
+                                                        int64_t batch, float* part) {
   constexpr int F = 32;
   __shared__ float red[4][32];
-  const int64_t tile = blockIdx.x;
+  const int H = P / W;
+  const int64_t tile = blockIdx.x / H;
+  const int r = (int)(blockIdx.x % H);
   const int m = threadIdx.x;
   float s[F];
 #pragma unroll
   for (int c = 0; c < F; ++c) s[c] = 0.f;
   if (tile * kTile + m < batch) {
-    for (int pix = 0; pix < P; ++pix) {
+    for (int pix = r * W; pix < (r + 1) * W; ++pix) {
       float v[F];
       load_row(blk<__nv_bfloat16>(G, tile, P, pix, F), m, 0, F, v);
 #pragma unroll
@@ -488,7 +518,7 @@ __global__ void __launch_bounds__(128) bias_tile_kernel(const __nv_bfloat16* G, 
 #pragma unroll
     for (int c = 0; c < F; ++c) red[warp][c] = s[c];
   __syncthreads();
-  if (m < n) part[tile * n + m] = red[0][g0 + m] + red[1][g0 + m] + red[2][g0 + m] + red[3][g0 + m];
+  if (m < n) part[(int64_t)blockIdx.x * n + m] = red[0][g0 + m] + red[1][g0 + m] + red[2][g0 + m] + red[3][g0 + m];
 }
 
 __global__ void bias_reduce_kernel(const float* part, int64_t tiles, int n, float* db) {
@@ -531,14 +561,15 @@ int launch_bwd_op(const BwdOpArgs& a, int64_t tiles, int H, int W, int* err, cud
   return check_cuda(launched(), "bwd_op_kernel");
 }
 
-int64_t wgrad_tc_part_floats(int64_t tiles, int H) {
+int64_t wgrad_tc_grid(int64_t tiles, int H) {
   int64_t grid = sm_count();
-  if (grid > tiles * H) grid = tiles * H;
-  return grid * 3 * 32 * 96;
+  return grid < tiles * H ? grid : tiles * H;
 }
 
-int launch_wgrad_tc(const WgTcArgs& a, int kw, int kcol0, float* dW, int64_t tiles, int H, int W, int* err,
-                    cudaStream_t s) {
+int64_t wgrad_tc_part_floats(int64_t tiles, int H) { return wgrad_tc_grid(tiles, H) * (3 * 32 * 96 + 32); }
+
+int launch_wgrad_tc(const WgTcArgs& a, int kw, int kcol0, float* dW, float* db, int64_t tiles, int H, int W,
+                    int* err, cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
     int st = set_smem<32>((const void*)wgrad_tc_kernel<32>, WgCfg<32>::kSmem);
@@ -546,20 +577,21 @@ int launch_wgrad_tc(const WgTcArgs& a, int kw, int kcol0, float* dW, int64_t til
     attr = true;
   }
   const int64_t items = tiles * H;
-  int64_t grid = sm_count();
-  if (grid > items) grid = items;
+  const int64_t grid = wgrad_tc_grid(tiles, H);
   wgrad_tc_kernel<32><<<(unsigned)grid, kWgThreads, WgCfg<32>::kSmem, s>>>(a, H, W, items, err);
   FK_CUDA(launched());
-  const int per = a.x_rows * 32 * a.ntc * a.n;
-  wgrad_reduce_kernel<<<(per + 255) / 256, 256, 0, s>>>(a.part, (int)grid, a.x_rows, a.ntc, a.n, kw, kcol0, dW);
+  const int per = a.x_rows * 32 * a.ntc * a.n + (a.bias_jpos >= 0 ? a.n : 0);
+  wgrad_reduce_kernel<<<(per + 255) / 256, 256, 0, s>>>(a.part, (int)grid, a.x_rows, a.ntc, a.n, kw, kcol0, dW,
+                                                        a.part_bias, a.bias_jpos >= 0 ? db : nullptr);
   return check_cuda(launched(), "wgrad_reduce_kernel");
 }
 
-int launch_bias_sum(const void* G, int64_t tiles, int P, int g0, int n, int64_t batch, float* part, float* db,
+int launch_bias_sum(const void* G, int64_t tiles, int H, int W, int g0, int n, int64_t batch, float* part, float* db,
                     cudaStream_t s) {
-  bias_tile_kernel<<<(unsigned)tiles, 128, 0, s>>>(static_cast<const __nv_bfloat16*>(G), P, g0, n, batch, part);
+  bias_tile_kernel<<<(unsigned)(tiles * H), 128, 0, s>>>(static_cast<const __nv_bfloat16*>(G), H * W, W, g0, n, batch,
+                                                         part);
   FK_CUDA(launched());
-  bias_reduce_kernel<<<1, 32, 0, s>>>(part, tiles, n, db);
+  bias_reduce_kernel<<<1, 32, 0, s>>>(part, tiles * H, n, db);
   return check_cuda(launched(), "bias_reduce_kernel");
 }
 
