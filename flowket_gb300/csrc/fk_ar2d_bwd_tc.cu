@@ -81,10 +81,10 @@ __global__ void __launch_bounds__(kPipeThreads, 1) bwd_op_kernel(const __grid_co
     mbar_init(wbar, 1);
     for (int i = 0; i < NS; ++i) {
       mbar_init(&accf[i], 1);
-      mbar_init(&acce[i], 128);
+      mbar_init(&acce[i], 4);  // one arrival per epilogue warp
     }
     for (int i = 0; i < NB; ++i) {
-      mbar_init(&caf[i], 128);
+      mbar_init(&caf[i], 4);
       mbar_init(&cf[i], 1);
     }
     mbar_init(&drain[0], 1);
@@ -160,7 +160,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) bwd_op_kernel(const __grid_co
         load_raw<F>(blk<T>(a.rv, ptile, P, (pr - 1) * W + pc, F), m, rvr);
         if (a.gvs) load_raw<F>(blk<T>(a.gvs, ptile, P, (pr - 1) * W + pc, F), m, gsr);
       }
-      if (!pwait(&cf[b], (pq / NB) & 1, err, abort)) return;
+      if (!uwait(&cf[b], (pq / NB) & 1, err, abort)) return;
       tc_fence_after();
       float gx[F];
       tread<F>(tl, C::kChainCol + b * 2 * F, gx);
@@ -218,12 +218,12 @@ __global__ void __launch_bounds__(kPipeThreads, 1) bwd_op_kernel(const __grid_co
           load_row(blk<T>(a.prev, tile, P, pix, F), m, 0, F, mk);
           if (a.res) load_row(blk<T>(a.res, tile, P, pix, F), m, 0, F, rs);
         }
-        if (!pwait(&accf[sl], (p / NS) & 1, err, abort)) break;
+        if (!uwait(&accf[sl], (p / NS) & 1, err, abort)) break;
         tc_fence_after();
         float g[F];
         tread<F>(tl, sl * F, g);
         tc_fence_before();
-        mbar_arrive(&acce[sl]);
+        warp_arrive(&acce[sl]);
         if (!chain) {
           if (a.res) {
 #pragma unroll
@@ -242,7 +242,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) bwd_op_kernel(const __grid_co
 #pragma unroll
         for (int gq = 0; gq < F / 8; ++gq) st8(ca + ((int64_t)gq * kTile + m) * 8, g + 8 * gq);
         fence_proxy_async_smem();
-        mbar_arrive(&caf[b]);
+        warp_arrive(&caf[b]);
         if (pend) second_half();
         pend = true;
         pq = p;
@@ -426,7 +426,7 @@ __global__ void __launch_bounds__(kWgThreads, 1) wgrad_tc_kernel(const __grid_co
   } else if (warp >= 4) {
     // ------------------------------------------------------------------ readers
     const int q4 = warp % 4;  // lane quarter = stacked row block = kernel row of ring row q4
-    pwait(done, 0, err, abort);
+    uwait(done, 0, err, abort);
     tc_fence_after();
     const uint32_t tl = tmem + ((uint32_t)(q4 * 32) << 16);
     if (!abort && q4 < a.x_rows) {

@@ -88,14 +88,14 @@ __global__ void __launch_bounds__(kPipeThreads, 1) op_pipe_kernel(const __grid_c
     mbar_init(wbar, 1);
     for (int i = 0; i < NS; ++i) {
       mbar_init(&accf[i], 1);
-      mbar_init(&acce[i], 128);
+      mbar_init(&acce[i], 4);  // one arrival per epilogue warp
     }
     for (int i = 0; i < NB; ++i) {
-      mbar_init(&caf[i], 128);
+      mbar_init(&caf[i], 4);
       mbar_init(&cf[i], 1);
     }
-    mbar_init(head_ready, 128);
-    mbar_init(head_free, 128);
+    mbar_init(head_ready, 4);
+    mbar_init(head_free, 4);
     mbar_init(&drain[0], 1);
     mbar_init(&drain[1], 1);
     fence_mbar_init();
@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) op_pipe_kernel(const __grid_c
     auto second_half = [&]() {
       const uint32_t b = pq % NB;
       pend = false;
-      if (!pwait(&cf[b], (pq / NB) & 1, err, abort)) return;
+      if (!uwait(&cf[b], (pq / NB) & 1, err, abort)) return;
       tc_fence_after();
       float out[32];
       if (kind == kConvC)
@@ -220,7 +220,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) op_pipe_kernel(const __grid_c
       const int64_t item = item_at(it);
       const int64_t tile = item / H;
       const int r = (int)(item % H);
-      if (head && grp == 1 && it_count > 0 && !pwait(head_free, (it_count - 1) & 1, err, abort)) break;
+      if (head && grp == 1 && it_count > 0 && !uwait(head_free, (it_count - 1) & 1, err, abort)) break;
       for (int c = 0; c < W && !abort; ++c, ++p) {
         if ((int)(p % C::kGroups) != grp) continue;
         const uint32_t b = p % NB;
@@ -228,12 +228,12 @@ __global__ void __launch_bounds__(kPipeThreads, 1) op_pipe_kernel(const __grid_c
         const int pix = r * W + c;
         float o[F];
         if (need_res) load_row(blk<T>(a.res, tile, P, pix, F), m, 0, F, o);
-        if (!pwait(&accf[sl], (p / NS) & 1, err, abort)) break;
+        if (!uwait(&accf[sl], (p / NS) & 1, err, abort)) break;
         tc_fence_after();
         float acc[F];
         tread<F>(tl, sl * F, acc);
         tc_fence_before();
-        mbar_arrive(&acce[sl]);
+        warp_arrive(&acce[sl]);
         float cin[F];
         if (kind == kConvV) {
 #pragma unroll
@@ -279,7 +279,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) op_pipe_kernel(const __grid_c
 #pragma unroll
         for (int gq = 0; gq < F / 8; ++gq) st8(ca + ((int64_t)gq * kTile + m) * 8, cin + 8 * gq);
         fence_proxy_async_smem();
-        mbar_arrive(&caf[b]);
+        warp_arrive(&caf[b]);
         if (pend) second_half();
         pend = true;
         pq = p;
@@ -291,8 +291,8 @@ __global__ void __launch_bounds__(kPipeThreads, 1) op_pipe_kernel(const __grid_c
         if (pend) second_half();
         // ordered compensated sum over the row's pixels (the per-pixel engine's order)
         if (grp == 1) {
-          mbar_arrive(head_ready);
-        } else if (pwait(head_ready, it_count & 1, err, abort)) {
+          warp_arrive(head_ready);
+        } else if (uwait(head_ready, it_count & 1, err, abort)) {
           Kahan kre, kim;
           for (int c = 0; c < W; ++c) {
             float2 v = head_sm[c * kTile + m];
@@ -300,7 +300,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) op_pipe_kernel(const __grid_c
             kim.add(v.y);
           }
           a.row_partial[((int64_t)tile * H + r) * kTile + m] = make_float2(kre.s - kre.c, kim.s - kim.c);
-          mbar_arrive(head_free);
+          warp_arrive(head_free);
         }
       }
     }

@@ -62,6 +62,22 @@ __device__ __forceinline__ bool pwait(uint64_t* bar, uint32_t parity, int* err, 
   return true;
 }
 
+// pwait for code that all 32 lanes run converged (barrier counts of one
+// arrival per warp, named barriers): a timeout on any lane aborts the whole
+// warp, so the lanes never part at a later warp-wide step.
+__device__ __forceinline__ bool uwait(uint64_t* bar, uint32_t parity, int* err, bool& abort) {
+  pwait(bar, parity, err, abort);
+  abort = __any_sync(0xffffffffu, abort);
+  return !abort;
+}
+
+// Warp-wide arrival (one arrival per warp): the warp synchronisation orders
+// every lane's earlier accesses before lane 0's release.
+__device__ __forceinline__ void warp_arrive(uint64_t* bar) {
+  __syncwarp();
+  if ((threadIdx.x & 31) == 0) mbar_arrive(bar);
+}
+
 template <int N>
 __device__ __forceinline__ void tread(uint32_t taddr_lane, uint32_t col, float* v) {
 #pragma unroll
@@ -199,9 +215,57 @@ __device__ void pipe_issuer(const PipeGeom& g, const PipeItems& items, uint8_t* 
       // outputs first reached by this column, [c_f, c_hi]: all of them at
       // x == 0, else output x + o0 + 2 if it exists
       const int c_f = x == 0 ? c_lo : (x + o0 + 2 < c_hi + 1 ? x + o0 + 2 : c_hi + 1);
-      if (lane == 0) {
-        // one MMA per (ring row, K step) over outputs [ca, cb], split where
-        // the TMEM slot ring wraps
+      // common column: every kernel row in the lattice and no wrap of the
+      // TMEM slot ring -- straight-line MMAs on descriptors computed here,
+      // so that the issuing thread does little besides issuing
+      const uint32_t s_lo = (gbase + (uint32_t)c_lo) % NS;
+      const int n_tot = c_hi - c_lo + 1, n_live = c_f - c_lo;
+      if (k_lo == 0 && k_hi == g.nrows - 1 && (int)s_lo + n_tot <= NS) {
+        const uint32_t d_live = tmem + s_lo * F;
+        const uint32_t d_fresh = d_live + (uint32_t)(n_live * F);
+        const uint32_t id_tot = n_tot == 3 ? idesc3 : (n_tot == 2 ? idesc2 : idesc1);
+        const uint32_t id_live = n_live == 2 ? idesc2 : idesc1;
+        const uint32_t id_fresh = n_tot - n_live == 3 ? idesc3 : (n_tot - n_live == 2 ? idesc2 : idesc1);
+        const uint64_t a_col = a0 + cs * 3 * kBlk16;
+        const uint64_t b_live = w0 + (uint32_t)((c_lo - x - o0) * F);
+        const uint64_t b_fresh = w0 + (uint32_t)((c_f - x - o0) * F);
+        if (lane == 0) {
+          if (g.nrows == 3) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+#pragma unroll
+              for (int ks = 0; ks < F / 16; ++ks) {
+                const uint32_t aoff = (uint32_t)k * kBlk16 + ks * kKs16;
+                const uint32_t boff = (g.rev ? (uint32_t)(2 - k) : (uint32_t)k) * kRow16 + ks * kKsW16;
+                if (k == 0 && ks == 0) {
+                  if (n_live > 0) umma_bf16(d_live, a_col + aoff, b_live + boff, id_live, 1u);
+                  if (n_tot > n_live) umma_bf16(d_fresh, a_col + aoff, b_fresh + boff, id_fresh, 0u);
+                } else {
+                  umma_bf16(d_live, a_col + aoff, b_live + boff, id_tot, 1u);
+                }
+              }
+            }
+          } else {
+#pragma unroll
+            for (int ks = 0; ks < F / 16; ++ks) {
+              const uint32_t aoff = ks * kKs16;
+              const uint32_t boff = ks * kKsW16;
+              if (ks == 0) {
+                if (n_live > 0) umma_bf16(d_live, a_col + aoff, b_live + boff, id_live, 1u);
+                if (n_tot > n_live) umma_bf16(d_fresh, a_col + aoff, b_fresh + boff, id_fresh, 0u);
+              } else {
+                umma_bf16(d_live, a_col + aoff, b_live + boff, id_tot, 1u);
+              }
+            }
+          }
+          umma_commit(&empty[cs]);
+          const int d_lo = x + o0 < 0 ? 0 : x + o0;
+          const int d_hi = x == W - 1 ? W - 1 : x + o0;
+          for (int c = d_lo; c <= d_hi; ++c) umma_commit(&accf[(gbase + (uint32_t)c) % NS]);
+        }
+      } else if (lane == 0) {
+        // general column: one MMA per (ring row, K step) over outputs [ca, cb],
+        // split where the TMEM slot ring wraps
         auto mma = [&](int ca, int cb, uint32_t aoff, uint32_t boff, uint32_t acc) {
           while (ca <= cb) {
             const uint32_t s = (gbase + (uint32_t)ca) % NS;
