@@ -178,6 +178,59 @@ __device__ void pipe_waiter(const PipeGeom& g, const PipeItems& items, uint64_t*
   abort = stop || abort;
 }
 
+// Lane 0's MMAs of a column without TMEM ring wrap, ring rows KLO..KHI:
+// operands computed by the whole warp before the branch that selects lane 0,
+// compile-time offsets inside, so that the issuing thread only issues.
+template <int F, int KLO, int KHI>
+__device__ __forceinline__ void issue_plain(uint64_t a_col, uint64_t b_live, uint64_t b_fresh, uint32_t d_live,
+                                            uint32_t d_fresh, uint32_t id_tot, uint32_t id_live, uint32_t id_fresh,
+                                            int n_live, int n_tot, int rev) {
+  constexpr uint32_t kBlk16 = PipeCfg<F>::kBlk >> 4;
+  constexpr uint32_t kRow16 = PipeCfg<F>::kWRow >> 4;
+  constexpr uint32_t kKs16 = (2 * 2048) >> 4;
+  constexpr uint32_t kKsW16 = (2 * 3 * F * 16) >> 4;
+#pragma unroll
+  for (int k = KLO; k <= KHI; ++k) {
+#pragma unroll
+    for (int ks = 0; ks < F / 16; ++ks) {
+      const uint32_t aoff = (uint32_t)k * kBlk16 + ks * kKs16;
+      const uint32_t boff = (rev ? (uint32_t)(KHI - k + KLO) : (uint32_t)k) * kRow16 + ks * kKsW16;
+      if (k == KLO && ks == 0) {
+        if (n_live > 0) umma_bf16(d_live, a_col + aoff, b_live + boff, id_live, 1u);
+        if (n_tot > n_live) umma_bf16(d_fresh, a_col + aoff, b_fresh + boff, id_fresh, 0u);
+      } else {
+        umma_bf16(d_live, a_col + aoff, b_live + boff, id_tot, 1u);
+      }
+    }
+  }
+}
+
+// Reversed (adjoint) op near the bottom edge: ring rows 0..KHI, kernel row
+// 2 - k.
+template <int F, int KHI>
+__device__ __forceinline__ void issue_rev_partial(uint64_t a_col, uint64_t b_live, uint64_t b_fresh, uint32_t d_live,
+                                                  uint32_t d_fresh, uint32_t id_tot, uint32_t id_live,
+                                                  uint32_t id_fresh, int n_live, int n_tot) {
+  constexpr uint32_t kBlk16 = PipeCfg<F>::kBlk >> 4;
+  constexpr uint32_t kRow16 = PipeCfg<F>::kWRow >> 4;
+  constexpr uint32_t kKs16 = (2 * 2048) >> 4;
+  constexpr uint32_t kKsW16 = (2 * 3 * F * 16) >> 4;
+#pragma unroll
+  for (int k = 0; k <= KHI; ++k) {
+#pragma unroll
+    for (int ks = 0; ks < F / 16; ++ks) {
+      const uint32_t aoff = (uint32_t)k * kBlk16 + ks * kKs16;
+      const uint32_t boff = (uint32_t)(2 - k) * kRow16 + ks * kKsW16;
+      if (k == 0 && ks == 0) {
+        if (n_live > 0) umma_bf16(d_live, a_col + aoff, b_live + boff, id_live, 1u);
+        if (n_tot > n_live) umma_bf16(d_fresh, a_col + aoff, b_fresh + boff, id_fresh, 0u);
+      } else {
+        umma_bf16(d_live, a_col + aoff, b_live + boff, id_tot, 1u);
+      }
+    }
+  }
+}
+
 // Issuer (whole warp; lane 0 issues). `w0` is the descriptor of kernel row 0
 // of the scatter operand ([F/8][3F][8] per kernel row).
 template <int F>
@@ -215,12 +268,11 @@ __device__ void pipe_issuer(const PipeGeom& g, const PipeItems& items, uint8_t* 
       // outputs first reached by this column, [c_f, c_hi]: all of them at
       // x == 0, else output x + o0 + 2 if it exists
       const int c_f = x == 0 ? c_lo : (x + o0 + 2 < c_hi + 1 ? x + o0 + 2 : c_hi + 1);
-      // common column: every kernel row in the lattice and no wrap of the
-      // TMEM slot ring -- straight-line MMAs on descriptors computed here,
-      // so that the issuing thread does little besides issuing
+      // column without wrap of the TMEM slot ring: straight-line MMAs on
+      // operands computed here, so that the issuing thread only issues
       const uint32_t s_lo = (gbase + (uint32_t)c_lo) % NS;
       const int n_tot = c_hi - c_lo + 1, n_live = c_f - c_lo;
-      if (k_lo == 0 && k_hi == g.nrows - 1 && (int)s_lo + n_tot <= NS) {
+      if ((int)s_lo + n_tot <= NS) {
         const uint32_t d_live = tmem + s_lo * F;
         const uint32_t d_fresh = d_live + (uint32_t)(n_live * F);
         const uint32_t id_tot = n_tot == 3 ? idesc3 : (n_tot == 2 ? idesc2 : idesc1);
@@ -230,34 +282,22 @@ __device__ void pipe_issuer(const PipeGeom& g, const PipeItems& items, uint8_t* 
         const uint64_t b_live = w0 + (uint32_t)((c_lo - x - o0) * F);
         const uint64_t b_fresh = w0 + (uint32_t)((c_f - x - o0) * F);
         if (lane == 0) {
-          if (g.nrows == 3) {
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-#pragma unroll
-              for (int ks = 0; ks < F / 16; ++ks) {
-                const uint32_t aoff = (uint32_t)k * kBlk16 + ks * kKs16;
-                const uint32_t boff = (g.rev ? (uint32_t)(2 - k) : (uint32_t)k) * kRow16 + ks * kKsW16;
-                if (k == 0 && ks == 0) {
-                  if (n_live > 0) umma_bf16(d_live, a_col + aoff, b_live + boff, id_live, 1u);
-                  if (n_tot > n_live) umma_bf16(d_fresh, a_col + aoff, b_fresh + boff, id_fresh, 0u);
-                } else {
-                  umma_bf16(d_live, a_col + aoff, b_live + boff, id_tot, 1u);
-                }
-              }
-            }
-          } else {
-#pragma unroll
-            for (int ks = 0; ks < F / 16; ++ks) {
-              const uint32_t aoff = ks * kKs16;
-              const uint32_t boff = ks * kKsW16;
-              if (ks == 0) {
-                if (n_live > 0) umma_bf16(d_live, a_col + aoff, b_live + boff, id_live, 1u);
-                if (n_tot > n_live) umma_bf16(d_fresh, a_col + aoff, b_fresh + boff, id_fresh, 0u);
-              } else {
-                umma_bf16(d_live, a_col + aoff, b_live + boff, id_tot, 1u);
-              }
-            }
-          }
+          // in-lattice ring rows: all (k_lo, k_hi) = (0, 2); forward ops near
+          // the top edge (1, 2), (2, 2); reversed ops near the bottom edge
+          // (0, 1), (0, 0); 1-row ops (0, 0)
+          if (g.nrows == 1)
+            issue_plain<F, 0, 0>(a_col, b_live, b_fresh, d_live, d_fresh, id_tot, id_live, id_fresh, n_live, n_tot, 0);
+          else if (k_lo == 0 && k_hi == 2)
+            issue_plain<F, 0, 2>(a_col, b_live, b_fresh, d_live, d_fresh, id_tot, id_live, id_fresh, n_live, n_tot,
+                                 g.rev);
+          else if (!g.rev && k_lo == 1)
+            issue_plain<F, 1, 2>(a_col, b_live, b_fresh, d_live, d_fresh, id_tot, id_live, id_fresh, n_live, n_tot, 0);
+          else if (!g.rev)
+            issue_plain<F, 2, 2>(a_col, b_live, b_fresh, d_live, d_fresh, id_tot, id_live, id_fresh, n_live, n_tot, 0);
+          else if (k_hi == 1)
+            issue_rev_partial<F, 1>(a_col, b_live, b_fresh, d_live, d_fresh, id_tot, id_live, id_fresh, n_live, n_tot);
+          else
+            issue_rev_partial<F, 0>(a_col, b_live, b_fresh, d_live, d_fresh, id_tot, id_live, id_fresh, n_live, n_tot);
           umma_commit(&empty[cs]);
           const int d_lo = x + o0 < 0 ? 0 : x + o0;
           const int d_hi = x == W - 1 ? W - 1 : x + o0;
