@@ -269,6 +269,10 @@ struct WgArgs {
   int64_t o_kernel, o_bias;
   int64_t batch;
   int items;            // work items = ntaps * ceil(cin/8) * ceil(N/8)
+  // Fixed-order mode: each tile writes its sums to part[tile][ntaps*cin*N + N]
+  // (kernel then bias) instead of adding them atomically; the tiles are then
+  // summed in order (wgrad_part_reduce_kernel).
+  float* part;
 };
 
 constexpr int kItemsPerCta = 4;
@@ -354,7 +358,13 @@ __global__ void __launch_bounds__(128) wgrad_kernel(const __grid_constant__ WgAr
       if (m < 64) {
         int i = m / 8, j = m % 8;
         float v = red[0][m] + red[1][m] + red[2][m] + red[3][m];
-        if (i < kmax && j < nmax) atomicAdd(&a.dW[(int64_t)(t * a.cin + kc * 8 + i) * a.N + nc * 8 + j], v);
+        if (i < kmax && j < nmax) {
+          const int64_t e = (int64_t)(t * a.cin + kc * 8 + i) * a.N + nc * 8 + j;
+          if (a.part)
+            a.part[tile * ((int64_t)a.ntaps * a.cin * a.N + a.N) + e] = v;
+          else
+            atomicAdd(&a.dW[e], v);
+        }
       }
       __syncthreads();
       if (with_bias) {
@@ -368,7 +378,13 @@ __global__ void __launch_bounds__(128) wgrad_kernel(const __grid_constant__ WgAr
         if (lane == 0)
           for (int j = 0; j < 8; ++j) red[warp][j] = gb[j];
         __syncthreads();
-        if (m < nmax) atomicAdd(&a.dB[nc * 8 + m], red[0][m] + red[1][m] + red[2][m] + red[3][m]);
+        if (m < nmax) {
+          const float v = red[0][m] + red[1][m] + red[2][m] + red[3][m];
+          if (a.part)
+            a.part[tile * ((int64_t)a.ntaps * a.cin * a.N + a.N) + (int64_t)a.ntaps * a.cin * a.N + nc * 8 + m] = v;
+          else
+            atomicAdd(&a.dB[nc * 8 + m], v);
+        }
         __syncthreads();
       }
     }
@@ -495,6 +511,18 @@ static void tap_list(int kind, WgArgs& w) {
   }
 }
 
+// Sums the per-tile partials of the fixed-order mode in tile order.
+__global__ void wgrad_part_reduce_kernel(const float* part, int64_t tiles, int kn, int n, float* dW, float* dB) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= kn + n) return;
+  float s = 0.f;
+  for (int64_t t = 0; t < tiles; ++t) s += part[t * (kn + n) + e];
+  if (e < kn)
+    dW[e] = s;
+  else
+    dB[e - kn] = s;
+}
+
 template <typename T, typename TG = float>
 static int launch_wgrad(const NetLayout& L, WgArgs& w, const ConvDesc& cd, float* grad, float* O, int64_t batch,
                         cudaStream_t s) {
@@ -511,7 +539,11 @@ static int launch_wgrad(const NetLayout& L, WgArgs& w, const ConvDesc& cd, float
   }
   dim3 grid((unsigned)tiles, (unsigned)((w.items + kItemsPerCta - 1) / kItemsPerCta));
   wgrad_kernel<T, TG><<<grid, 128, 0, s>>>(w, L.H, L.W);
-  return check_cuda(launched(), "wgrad_kernel");
+  if (!w.part || O) return check_cuda(launched(), "wgrad_kernel");
+  FK_CUDA(launched());
+  const int kn = w.ntaps * w.cin * w.N;
+  wgrad_part_reduce_kernel<<<(kn + w.N + 127) / 128, 128, 0, s>>>(w.part, tiles, kn, w.N, w.dW, w.dB);
+  return check_cuda(launched(), "wgrad_part_reduce_kernel");
 }
 
 template <int F, typename T>
@@ -671,7 +703,11 @@ static int64_t tc_bwd_layout(const NetLayout& L, int64_t batch, char* base, TcBw
   t->gt = take(tb);
   t->gvp = take(tb);
   t->gl = reinterpret_cast<float*>(take(tiles * L.P * (int64_t)kTile * 8 * 4));
-  t->part = reinterpret_cast<float*>(take(wgrad_tc_part_floats(tiles, L.H) * 4));
+  // weight-gradient partials: the tensor-core launches' per-CTA sums, or the
+  // CUDA-core launches' per-tile sums (head, first causal conv: <= 9*1*32+32
+  // or 32*4+4 per tile)
+  const int64_t pf = wgrad_tc_part_floats(tiles, L.H);
+  t->part = reinterpret_cast<float*>(take((pf > tiles * 320 ? pf : tiles * 320) * 4));
   t->bpart = reinterpret_cast<float*>(take(tiles * L.H * 32 * 4));
   t->bytes = off;
   return off;
@@ -721,6 +757,7 @@ static int backward_tc(const NetLayout& L, const void* packed, const float* para
     w.gC = 8;
     w.N = 4;
     w.spins = spins;
+    w.part = G.part;
     if ((st = launch_wgrad<T, float>(L, w, L.conv[io], grad, nullptr, batch, s)) != FK_OK) return st;
   }
   auto wg = [&](const void* X, int x_rows, int x_row0, const void* Gt, int g0, int n, int ntc, int dc0,
@@ -804,6 +841,7 @@ static int backward_tc(const NetLayout& L, const void* packed, const float* para
       w.G = G.gt;
       w.gC = F;
       w.N = F;
+      w.part = G.part;
       if ((st = launch_wgrad<T, T>(L, w, ch, grad, nullptr, batch, s)) != FK_OK) return st;
       tap_list(kConvV, w);
       w.G = G.gvp;

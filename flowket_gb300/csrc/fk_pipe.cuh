@@ -268,19 +268,26 @@ __device__ void pipe_issuer(const PipeGeom& g, const PipeItems& items, uint8_t* 
       // outputs first reached by this column, [c_f, c_hi]: all of them at
       // x == 0, else output x + o0 + 2 if it exists
       const int c_f = x == 0 ? c_lo : (x + o0 + 2 < c_hi + 1 ? x + o0 + 2 : c_hi + 1);
-      // column without wrap of the TMEM slot ring: straight-line MMAs on
-      // operands computed here, so that the issuing thread only issues
+      // The column's outputs [c_lo, c_hi] in one part, or in two where the
+      // TMEM slot ring wraps ([c_lo, c_s) at slot s_lo.., [c_s, c_hi] at
+      // slot 0..); each part is issued as straight-line MMAs on operands
+      // computed here by the whole warp, so that the issuing thread only
+      // issues. An output lies in one part, so its accumulation order is
+      // unchanged by the split.
       const uint32_t s_lo = (gbase + (uint32_t)c_lo) % NS;
-      const int n_tot = c_hi - c_lo + 1, n_live = c_f - c_lo;
-      if ((int)s_lo + n_tot <= NS) {
-        const uint32_t d_live = tmem + s_lo * F;
+      const int c_s = c_lo + (NS - (int)s_lo) < c_hi + 1 ? c_lo + (NS - (int)s_lo) : c_hi + 1;
+      const uint64_t a_col = a0 + cs * 3 * kBlk16;
+      auto part = [&](int pa, int pb, uint32_t slot) {  // outputs [pa, pb], pa at TMEM slot `slot`
+        const int n_tot = pb - pa + 1;
+        const int f0 = c_f > pa ? c_f : pa;                       // first fresh output of the part
+        const int n_live = (f0 < pb + 1 ? f0 : pb + 1) - pa;
+        const uint32_t d_live = tmem + slot * F;
         const uint32_t d_fresh = d_live + (uint32_t)(n_live * F);
         const uint32_t id_tot = n_tot == 3 ? idesc3 : (n_tot == 2 ? idesc2 : idesc1);
         const uint32_t id_live = n_live == 2 ? idesc2 : idesc1;
         const uint32_t id_fresh = n_tot - n_live == 3 ? idesc3 : (n_tot - n_live == 2 ? idesc2 : idesc1);
-        const uint64_t a_col = a0 + cs * 3 * kBlk16;
-        const uint64_t b_live = w0 + (uint32_t)((c_lo - x - o0) * F);
-        const uint64_t b_fresh = w0 + (uint32_t)((c_f - x - o0) * F);
+        const uint64_t b_live = w0 + (uint32_t)((pa - x - o0) * F);
+        const uint64_t b_fresh = w0 + (uint32_t)((f0 - x - o0) * F);
         if (lane == 0) {
           // in-lattice ring rows: all (k_lo, k_hi) = (0, 2); forward ops near
           // the top edge (1, 2), (2, 2); reversed ops near the bottom edge
@@ -298,40 +305,11 @@ __device__ void pipe_issuer(const PipeGeom& g, const PipeItems& items, uint8_t* 
             issue_rev_partial<F, 1>(a_col, b_live, b_fresh, d_live, d_fresh, id_tot, id_live, id_fresh, n_live, n_tot);
           else
             issue_rev_partial<F, 0>(a_col, b_live, b_fresh, d_live, d_fresh, id_tot, id_live, id_fresh, n_live, n_tot);
-          umma_commit(&empty[cs]);
-          const int d_lo = x + o0 < 0 ? 0 : x + o0;
-          const int d_hi = x == W - 1 ? W - 1 : x + o0;
-          for (int c = d_lo; c <= d_hi; ++c) umma_commit(&accf[(gbase + (uint32_t)c) % NS]);
         }
-      } else if (lane == 0) {
-        // general column: one MMA per (ring row, K step) over outputs [ca, cb],
-        // split where the TMEM slot ring wraps
-        auto mma = [&](int ca, int cb, uint32_t aoff, uint32_t boff, uint32_t acc) {
-          while (ca <= cb) {
-            const uint32_t s = (gbase + (uint32_t)ca) % NS;
-            int n = cb - ca + 1;
-            if (n > NS - (int)s) n = NS - (int)s;
-            const uint32_t id = n == 3 ? idesc3 : (n == 2 ? idesc2 : idesc1);
-            umma_bf16(tmem + s * F, a0 + aoff, w0 + boff + (uint32_t)((ca - x - o0) * F), id, acc);
-            ca += n;
-          }
-        };
-        bool first = true;
-        for (int k = k_lo; k <= k_hi; ++k) {
-          const uint32_t krow = g.rev ? (uint32_t)(g.nrows - 1 - k) : (uint32_t)k;
-#pragma unroll
-          for (int ks = 0; ks < F / 16; ++ks) {
-            const uint32_t aoff = (cs * 3 + (uint32_t)k) * kBlk16 + ks * kKs16;
-            const uint32_t boff = krow * kRow16 + ks * kKsW16;
-            if (first) {
-              if (c_f > c_lo) mma(c_lo, c_f - 1, aoff, boff, 1u);
-              mma(c_f, c_hi, aoff, boff, 0u);
-              first = false;
-            } else {
-              mma(c_lo, c_hi, aoff, boff, 1u);
-            }
-          }
-        }
+      };
+      part(c_lo, c_s - 1, s_lo);
+      if (c_s <= c_hi) part(c_s, c_hi, 0u);
+      if (lane == 0) {
         umma_commit(&empty[cs]);
         // outputs completed by this column
         const int d_lo = x + o0 < 0 ? 0 : x + o0;
