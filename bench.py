@@ -235,6 +235,22 @@ def timed_steps(vmc, opt, k):
     return start.elapsed_time(stop), fwd_ms, rows
 
 
+def evaluated_row_fraction(vmc):
+    """Mean fraction of lattice rows the local-energy forward evaluates per
+    connected configuration: causal reuse recomputes rows >= the first
+    flipped row only (rows above come from the sampled configuration's saved
+    activations), so the algorithmic FLOPs of a connection are this fraction
+    of a full forward's."""
+    obs = vmc.energy_observable
+    _, _, bf, rows = obs.connections(vmc.current_batch)
+    f = bf["cflips"][:rows].to(torch.int64)
+    h, w = SHAPE
+    r = torch.where(f >= 0, torch.div(f, w, rounding_mode="floor"), torch.full_like(f, h))
+    rk = r.min(dim=1).values
+    rk = torch.where(rk >= h, torch.zeros_like(rk), rk)
+    return float(((h - rk).double() / h).mean())
+
+
 def ours_arm(args, rank, world):
     from flowket_gb300 import _lib
     lib = _lib.load()
@@ -243,6 +259,7 @@ def ours_arm(args, rank, world):
     obs.record_forward = True
     for _ in range(args.warmup):
         vmc.step(opt)
+    row_frac = evaluated_row_fraction(vmc)
     obs.forward_events.clear()
     clocks = Clocks()
     barrier(world)
@@ -300,11 +317,20 @@ def ours_arm(args, rank, world):
         pass
     peak = peaks.get("bf16_tflops_sustained") or 1700.0
     fps = flops_per_sample_forward(SHAPE, DEPTH, CHANNELS)
-    achieved = rows * fps / (fwd_ms / 1e3) / 1e12 if fwd_ms > 0 else None
+    achieved = rows * row_frac * fps / (fwd_ms / 1e3) / 1e12 if fwd_ms > 0 else None
+    # DRAM bytes of one full forward per configuration, from an ncu capture of
+    # the forward case (profiles/); the local-energy forward moves this
+    # fraction (evaluated rows) per connected configuration
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    tpath = os.path.join(ROOT, "profiles", "ar2d_forward_dram_traffic_10x10_d10_f32_c32768.json")
     if os.path.exists(tpath):
         traffic = json.load(open(tpath)).get("ar2d_forward_bytes_per_config")
+    hbm = None
+    if traffic and fwd_ms > 0:
+        gbs = rows * row_frac * traffic / (fwd_ms / 1e3) / 1e9
+        hbm_peak = peaks.get("hbm_gbs") or 6800.0
+        hbm = {"achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
+               "bytes_per_config": traffic}
 
     if rank == 0:
         line = {"metric": METRIC, "value": samples_per_s, "unit": "samples/s", "n_gpus": world,
@@ -319,9 +345,12 @@ def ours_arm(args, rank, world):
                 "stage_ms": vmc.times,
                 "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                              "frac": achieved / peak if achieved else None,
-                             "traffic": traffic,
+                             "traffic": traffic * row_frac if traffic else None,
+                             "traffic_unit": "DRAM bytes per evaluated connected configuration",
+                             "hbm": hbm,
                              "kernel": "AR2D conv ops (V/H/C) of the local-energy forward",
-                             "flops_per_config": fps, "configs_timed": rows},
+                             "flops_per_config": fps, "configs_timed": rows,
+                             "evaluated_row_fraction": row_frac},
                 "clocks": clk, "gpu_launches": launches, "e2e": e2e}
         if not args.no_cpu_baseline:
             threads = os.cpu_count() or 1
