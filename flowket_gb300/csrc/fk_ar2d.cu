@@ -719,6 +719,204 @@ __global__ void row_reduce_kernel(const float2* __restrict__ part, int64_t batch
   out[b] = make_float2(re.s - re.c, im.s - im.c);
 }
 
+// ============================================================== first causal conv, one row at a time
+// The V and H ops of the first causal conv (input: the spin lattice, K = taps
+// <= 16) for all W pixels of one (tile, row) together: the W main MMAs are
+// issued at once, then the W chained MMAs, so a row costs three round trips
+// instead of three per pixel. Per pixel the MMA operands, the MMA sequence
+// and the epilogue arithmetic are those of run_op on the per-pixel engine:
+// the results are bitwise the same.
+template <int F>
+struct FirstCfg {
+  static constexpr int kNC = (F / 2) < 16 ? 16 : (F / 2);  // chained N (padded)
+  static int smem(int W) {
+    const int a = W * 2 * kTile * 16;        // A rows [W][2][128][8]
+    const int ca = W * kTile * F * 2;        // chained inputs [W][F/8][128][8] (reuse A)
+    return (a > ca ? a : ca) + 2 * F * 16 + F * kNC * 2 + 64;
+  }
+};
+
+template <int F>
+__global__ void __launch_bounds__(128) first_row_kernel(const __grid_constant__ OpArgs a, int H, int W, int* err) {
+  using C = FirstCfg<F>;
+  using T = __nv_bfloat16;
+  constexpr int F2 = F / 2;
+  constexpr int NC = C::kNC;
+  extern __shared__ __align__(1024) uint8_t smem[];
+  const int P = H * W;
+  int64_t item = blockIdx.x;
+  if (a.items) {
+    if ((int)blockIdx.x >= *a.n_items) return;
+    item = a.items[blockIdx.x];
+  }
+  const int64_t tile = item / H;
+  const int r = (int)(item % H);
+  const int m = threadIdx.x;
+  const int ab = W * 2 * kTile * 16, cab = W * kTile * F * 2;
+  uint8_t* abuf = smem;                                  // A rows, then chained inputs
+  uint8_t* wsm = smem + (ab > cab ? ab : cab);           // main weights [2][F][8]
+  uint8_t* cwsm = wsm + 2 * F * 16;                      // chained weights [F/8][NC][8]
+  uint64_t* bar = reinterpret_cast<uint64_t*>(cwsm + F * NC * 2);
+  uint32_t* slot = reinterpret_cast<uint32_t*>(bar + 2);
+  const uint32_t wbytes = 2 * F * 16, cbytes = F * NC * 2;
+  if (m == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  // TMEM: W accumulators of F columns (the chained ones reuse them), a power
+  // of two >= 32 columns
+  uint32_t ncols = 32;
+  while (ncols < (uint32_t)(W * F)) ncols *= 2;
+  if (m < 32) {
+    tmem_alloc(slot, ncols);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *slot;
+  int* e = err;
+  bool ok = true;
+  if (m == 0) {
+    mbar_arrive_expect_tx(&bar[0], wbytes + cbytes);
+    bulk_g2s(wsm, a.main.w, wbytes, &bar[0]);
+    bulk_g2s(cwsm, a.chain.w, cbytes, &bar[0]);
+  }
+  // thread m's K = 16 row per pixel (taps in kernel order, zero padded)
+  for (int c = 0; c < W; ++c) {
+    float v[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) v[k] = 0.f;
+    const int nt = num_taps(a.kind);
+    for (int t = 0; t < nt; ++t) {
+      int dr, dc;
+      tap_offset(a.kind, t, dr, dc);
+      const int rr = r + dr, cc = c + dc;
+      if (rr >= 0 && rr < H && cc >= 0 && cc < W) v[t] = spin_at(a.spins, a.batch, P, tile * kTile + m, rr * W + cc);
+    }
+    st8(reinterpret_cast<T*>(abuf + c * 4096 + m * 16), v);
+    st8(reinterpret_cast<T*>(abuf + c * 4096 + 2048 + m * 16), v + 8);
+  }
+  fence_proxy_async_smem();
+  __syncthreads();
+  ok = mbar_wait(&bar[0], 0, e);
+  if (m == 0 && ok) {
+    tc_fence_after();
+    const uint32_t idesc = umma_idesc_bf16(128, F);
+    const uint64_t bd = umma_sdesc(smem_u32(wsm), F * 16, 128);
+    for (int c = 0; c < W; ++c)
+      umma_bf16(tmem + c * F, umma_sdesc(smem_u32(abuf + c * 4096), 2048, 128), bd, idesc, 0u);
+    umma_commit(&bar[1]);
+  }
+  ok = ok && mbar_wait(&bar[1], 0, e);
+  tc_fence_after();
+  const float* bm = a.main.b;
+  const float* bc = a.chain.b;
+  // first halves; the A rows are dead, their memory holds the chained inputs
+  if (ok) {
+    for (int c = 0; c < W; ++c) {
+      const int pix = r * W + c;
+      float acc[F];
+#pragma unroll
+      for (int q = 0; q < F / 16; ++q) tmem_ld16(tmem + ((uint32_t)((m / 32) * 32) << 16) + c * F + q * 16, acc + q * 16);
+      tmem_ld_wait();
+      if (a.kind == kConvV) {
+#pragma unroll
+        for (int n = 0; n < F; ++n) acc[n] += __ldg(bm + n);
+        if (a.stream_out) {
+          float o[F];
+          if (a.res) {
+            load_row(blk<T>(a.res, tile, P, pix, F), m, 0, F, o);
+#pragma unroll
+            for (int n = 0; n < F; ++n) o[n] = fmaxf(o[n] + acc[n], 0.f);
+          } else {
+#pragma unroll
+            for (int n = 0; n < F; ++n) o[n] = fmaxf(acc[n], 0.f);
+          }
+          store_row(blk<T>(a.stream_out, tile, P, pix, F), m, 0, F, o);
+        }
+#pragma unroll
+        for (int n = 0; n < F; ++n) acc[n] = fmaxf(acc[n], 0.f);
+      } else {
+#pragma unroll
+        for (int n = 0; n < F; ++n) acc[n] = fmaxf(acc[n] + __ldg(bm + n), 0.f);
+      }
+      if (a.aux_out) store_row(blk<T>(a.aux_out, tile, P, pix, F), m, 0, F, acc);
+      T* ca = reinterpret_cast<T*>(abuf + c * (kTile * F * 2));
+#pragma unroll
+      for (int g = 0; g < F / 8; ++g) st8(ca + ((int64_t)g * kTile + m) * 8, acc + 8 * g);
+    }
+  }
+  fence_proxy_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (m == 0 && ok) {
+    const uint32_t idesc = umma_idesc_bf16(128, NC);
+    for (int c = 0; c < W; ++c) {
+#pragma unroll
+      for (int ks = 0; ks < F / 16; ++ks)
+        umma_bf16(tmem + c * NC, umma_sdesc(smem_u32(abuf + c * (kTile * F * 2) + ks * 2 * 2048), 2048, 128),
+                  umma_sdesc(smem_u32(cwsm + ks * 2 * NC * 16), NC * 16, 128), idesc, ks > 0 ? 1u : 0u);
+    }
+    umma_commit(&bar[1]);
+  }
+  ok = ok && mbar_wait(&bar[1], 1, e);
+  tc_fence_after();
+  if (ok) {
+    for (int c = 0; c < W; ++c) {
+      const int pix = r * W + c;
+      float u[NC];
+      tmem_ld16(tmem + ((uint32_t)((m / 32) * 32) << 16) + c * NC, u);
+      tmem_ld_wait();
+      if (a.kind == kConvV) {
+#pragma unroll
+        for (int n = 0; n < F2; ++n) u[n] = fmaxf(u[n] + __ldg(bc + n), 0.f);
+        if (r + 1 < H) store_row(blk<T>(a.cat, tile, P, pix + W, F), m, F2, F2, u);
+        if (r == 0) {
+#pragma unroll
+          for (int n = 0; n < F2; ++n) u[n] = fmaxf(__ldg(bc + n), 0.f);
+          store_row(blk<T>(a.cat, tile, P, c, F), m, F2, F2, u);
+        }
+      } else {
+#pragma unroll
+        for (int n = 0; n < F2; ++n) u[n] = fmaxf(u[n] + __ldg(bc + n), 0.f);
+        const int sh = a.last ? 1 : 0;
+        if (c + sh < W) store_row(blk<T>(a.cat, tile, P, pix + sh, F), m, 0, F2, u);
+        if (sh && c == 0) {
+#pragma unroll
+          for (int n = 0; n < F2; ++n) u[n] = fmaxf(__ldg(bc + n), 0.f);
+          store_row(blk<T>(a.cat, tile, P, pix, F), m, 0, F2, u);
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (m < 32) {
+    tc_fence_after();
+    tmem_dealloc(tmem, ncols);
+  }
+}
+
+// FK_ERR_ARG when the row kernel does not apply (the per-pixel engine runs).
+template <int F>
+static int launch_first_row(const OpArgs& a, int64_t tiles, int H, int W, int* err, cudaStream_t s) {
+  if (!a.first || (a.kind != kConvV && a.kind != kConvH) || F > 32 || W * F > 512 ||
+      W * FirstCfg<F>::kNC > 512)
+    return FK_ERR_ARG;
+  const int smem = FirstCfg<F>::smem(W);
+  if (smem > 200 * 1024) return FK_ERR_ARG;
+  static bool attr = false;
+  if (!attr) {
+    FK_CUDA(cudaFuncSetAttribute(first_row_kernel<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr = true;
+  }
+  first_row_kernel<F><<<(unsigned)(tiles * H), 128, smem, s>>>(a, H, W, err);
+  return check_cuda(launched(), "first_row_kernel");
+}
+
 // ============================================================== op list
 static ConvW convw(const NetLayout& L, const void* packed, int idx) {
   const ConvDesc& c = L.conv[idx];
@@ -836,6 +1034,20 @@ static bool use_pipe_engine() {
   return v == 1;
 }
 
+// One op on the fastest engine that applies: the pipelined engine (ops after
+// the first conv), the row kernel (first conv), else the per-pixel engine.
+template <int F, bool TC>
+static int run_engine_op(const OpArgs& op, int64_t tiles, const NetLayout& L, int* err, cudaStream_t s) {
+  if (TC && use_pipe_engine()) {
+    if (!op.first && pipe_supported(F, L.W)) return launch_pipe_op(F, op, tiles, L.H, L.W, err, s);
+    if (op.first) {
+      const int st = launch_first_row<F>(op, tiles, L.H, L.W, err, s);
+      if (st != FK_ERR_ARG) return st;
+    }
+  }
+  return launch_op<F, TC>(op, tiles, L.H, L.W, err, s);
+}
+
 template <int F, bool TC>
 static int forward_impl(const NetLayout& L, const void* packed, const int8_t* spins, int64_t batch,
                         float* log_psi, float* cond, const Tensors& T, int mode, cudaStream_t s) {
@@ -851,10 +1063,7 @@ static int forward_impl(const NetLayout& L, const void* packed, const int8_t* sp
     }
     for (int k = 0; k < 3; ++k) {
       int st;
-      if (TC && pipe_supported(F, L.W) && !ops[k].first && use_pipe_engine())
-        st = launch_pipe_op(F, ops[k], tiles, L.H, L.W, err, s);
-      else
-        st = launch_op<F, TC>(ops[k], tiles, L.H, L.W, err, s);
+      st = run_engine_op<F, TC>(ops[k], tiles, L, err, s);
       if (st != FK_OK) return st;
     }
   }
@@ -1200,11 +1409,7 @@ static int connections_impl(const NetLayout& L, const void* packed, const int8_t
         ops[k].items = S.items;
         ops[k].n_items = S.n_items;
         if (last && k == 2) ops[k].row_partial = T.row_partial;
-        int st;
-        if (TC && pipe_supported(F, L.W) && !ops[k].first && use_pipe_engine())
-          st = launch_pipe_op(F, ops[k], tiles, L.H, L.W, err, s);
-        else
-          st = launch_op<F, TC>(ops[k], tiles, L.H, L.W, err, s);
+        int st = run_engine_op<F, TC>(ops[k], tiles, L, err, s);
         if (st != FK_OK) return st;
       }
     }
