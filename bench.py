@@ -54,9 +54,14 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--fp32-steps", type=int, default=2)
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--case", default="vmc", choices=["vmc", "forward"],
+    p.add_argument("--case", default="vmc", choices=["vmc", "forward", "energy4x4"],
                    help="forward: only the batched AR2D forward of the local-energy stage on --configs "
-                        "connected configurations (the small case used for ncu captures)")
+                        "connected configurations (the small case used for ncu captures); energy4x4: train "
+                        "the 4x4 Heisenberg model (depth 5, 16 channels) and compare its exact energy "
+                        "(enumeration of all 2^16 states) with Lanczos, in --precision")
+    p.add_argument("--precision", default="bf16", choices=["bf16", "fp32"])
+    p.add_argument("--train-steps", type=int, default=24000)
+    p.add_argument("--train-batch", type=int, default=2048)
     p.add_argument("--configs", type=int, default=32768)
     return p.parse_args()
 
@@ -81,6 +86,48 @@ def forward_case(args):
     fl = flops_per_sample_forward(SHAPE, DEPTH, CHANNELS) * args.configs
     print(json.dumps({"case": "forward", "configs": args.configs, "ms_per_forward": ms,
                       "tflops": fl / (ms / 1e3) / 1e12}), flush=True)
+
+
+def energy4x4_case(args):
+    """Heisenberg 4x4 PBC (Marshall sign), ConvNetAutoregressive2D depth 5,
+    16 channels, no weight norm: Adam with a cosine learning-rate decay from
+    1e-3 to 1e-5, exact sampling; the trained model's energy is evaluated
+    exactly over all 2^16 configurations and compared with the FP64 Lanczos
+    ground-state energy of the same operator (oracle, CPU)."""
+    import math
+    from flowket_gb300.machines import ConvNetAutoregressive2D
+    from flowket_gb300.observables import Observable
+    from flowket_gb300.operators import Heisenberg
+    from flowket_gb300.optimization import VariationalMonteCarlo
+    from flowket_gb300.optimizers import Adam
+    from flowket_gb300.samplers import FastAutoregressiveSampler
+    from oracle import exact, operators as ref_ops
+    shape = (4, 4)
+    op = Heisenberg(hilbert_state_shape=shape, pbc=True)
+    e0 = exact.lanczos_ground_energy(lambda s: ref_ops.heisenberg_find_conn(s, pbc=True), shape)
+    idx = torch.arange(2 ** 16, device="cuda")
+    states = (2 * ((idx[:, None] >> torch.arange(16, device="cuda")[None, :]) & 1) - 1).to(torch.int8).view(-1, 4, 4)
+    obs = Observable(op)
+
+    def exact_energy(m):
+        lp, _, _ = m.forward(states)
+        p = torch.exp(2 * lp[:, 0].double())
+        p = p / p.sum()
+        return float((p * obs.local_values(m, states, log_psi=lp)[:, 0]).sum())
+
+    m = ConvNetAutoregressive2D(shape, 5, 16, weights_normalization=False, precision=args.precision, seed=0)
+    vmc = VariationalMonteCarlo(m, op, FastAutoregressiveSampler(m, args.train_batch, seed=1234))
+    opt = Adam(m, lr=1e-3)
+    t0 = time.perf_counter()
+    for k in range(1, args.train_steps + 1):
+        opt.lr = 1e-5 + 0.5 * (1e-3 - 1e-5) * (1 + math.cos(math.pi * k / args.train_steps))
+        vmc.step(opt)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    e = exact_energy(m)
+    print(json.dumps({"case": "energy4x4", "precision": args.precision, "steps": args.train_steps,
+                      "batch": args.train_batch, "exact_energy": e, "lanczos": e0,
+                      "relative_error": abs(e - e0) / abs(e0), "train_s": train_s}), flush=True)
 
 
 def dist_init(n):
@@ -368,6 +415,8 @@ def main():
     rank, world = dist_init(args.gpus)
     if args.case == "forward":
         forward_case(args)
+    elif args.case == "energy4x4":
+        energy4x4_case(args)
     elif args.impl == "reference":
         reference_arm(args, rank, world)
     else:
