@@ -300,6 +300,7 @@ struct TcSmem {
   uint8_t* cw_ptr;
   uint64_t* bar_load;
   uint64_t* bar_mma;
+  uint64_t* vbar;  // 7 barriers of the one-pass V row op
   uint32_t* tmem_slot;
   int taps_per_group;
 };
@@ -316,7 +317,7 @@ struct TcCfg {
   static constexpr int kBytesW = kTaps * kTapBytesW;
   static constexpr int kBytesCA = kTile * F * 2;
   static constexpr int kBytesCW = F * 32 * 2;
-  static constexpr int kSmem = kBytesA + kBytesW + kBytesCA + kBytesCW + 64;
+  static constexpr int kSmem = kBytesA + kBytesW + kBytesCA + kBytesCW + 128;
 };
 
 template <int F>
@@ -330,6 +331,7 @@ __device__ __forceinline__ void tc_carve(uint8_t* base, TcSmem& s) {
   s.bar_load = reinterpret_cast<uint64_t*>(bars);
   s.bar_mma = reinterpret_cast<uint64_t*>(bars + 8);
   s.tmem_slot = reinterpret_cast<uint32_t*>(bars + 16);
+  s.vbar = reinterpret_cast<uint64_t*>(bars + 24);
   s.a = smem_u32(s.a_ptr);
   s.w = smem_u32(s.w_ptr);
   s.ca = smem_u32(s.ca_ptr);
@@ -338,7 +340,7 @@ __device__ __forceinline__ void tc_carve(uint8_t* base, TcSmem& s) {
 }
 
 struct TcState {
-  uint32_t tmem;
+  uint32_t tmem, ncols;
   uint32_t ph_load, ph_mma;
   int* err;
   bool abort;
@@ -347,21 +349,22 @@ struct TcState {
 constexpr uint32_t kTmemCols = 128;
 constexpr uint32_t kChainCol = 64;
 
-// Setup: barriers + 128 TMEM columns (warp 0 allocates).
-__device__ __forceinline__ void tc_setup(TcSmem& s, TcState& st, int* err) {
+// Setup: barriers + `ncols` TMEM columns (warp 0 allocates).
+__device__ __forceinline__ void tc_setup(TcSmem& s, TcState& st, int* err, uint32_t ncols = kTmemCols) {
   if (threadIdx.x == 0) {
     mbar_init(s.bar_load, 1);
     mbar_init(s.bar_mma, 1);
     fence_mbar_init();
   }
   if (threadIdx.x < 32) {
-    tmem_alloc(s.tmem_slot, kTmemCols);
+    tmem_alloc(s.tmem_slot, ncols);
     tmem_relinquish();
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   st.tmem = *s.tmem_slot;
+  st.ncols = ncols;
   st.ph_load = 0;
   st.ph_mma = 0;
   st.err = err;
@@ -373,7 +376,7 @@ __device__ __forceinline__ void tc_teardown(TcState& st) {
   __syncthreads();
   if (threadIdx.x < 32) {
     tc_fence_after();
-    tmem_dealloc(st.tmem, kTmemCols);
+    tmem_dealloc(st.tmem, st.ncols);
   }
 }
 
@@ -1079,6 +1082,423 @@ static int forward_impl(const NetLayout& L, const void* packed, const int8_t* sp
 //                 for i < last: H op_i (r, c), C op_i (r, c);  H op_last (r, c)
 //   end of row r: for every i: V op_i over (r, 0..W-1)
 // Every (layer, pixel) is evaluated once, after all the sites it depends on.
+// ---- exact sampler on tensor cores (F <= 32)
+// Shared memory of the sampler kernel: a ring of 18 activation blocks (C taps
+// in slots 0..8 during sites; the column ring, residual and chained inputs of
+// the row-end V ops), main / chained weights, the chained-input block, the H
+// buffer set, the residual block and the barriers.
+template <int F>
+struct SiteCfg {
+  static constexpr int kBlk = kTile * F * 2;
+  static constexpr int kSlice = F * F * 2;
+  static constexpr int kNC = (F / 2) < 16 ? 16 : (F / 2);
+  static constexpr int kRingBlocks = 18;
+  static constexpr int kVSlots = kRingBlocks / 3;  // input columns of a V row op in flight
+  static constexpr int kW = kRingBlocks * kBlk;     // 9 tap slices = the column-scatter operand
+  static constexpr int kCW = kW + 9 * kSlice;
+  static constexpr int kCA = kCW + F * 32 * 2;
+  static constexpr int kAH = kCA + kBlk;
+  static constexpr int kWH = kAH + 3 * kBlk;
+  static constexpr int kCWH = kWH + 3 * kSlice;
+  static constexpr int kRes = kCWH + F * kNC * 2;
+  static constexpr int kBar = kRes + kBlk;
+  static constexpr int kSmem = kBar + 256;
+};
+static_assert(SiteCfg<32>::kSmem <= 227 * 1024, "sampler shared memory");
+
+// The V op of one causal conv (after the first) over a whole lattice row of
+// one tile, inside the sampler: the column-scatter MMAs of the pipelined
+// engine (input column x times the three stacked kernel columns into the
+// TMEM accumulators of outputs x-1..x+1, same order: columns ascending,
+// kernel rows ascending, K steps ascending), then the run_op epilogue per
+// output and the chained 1x1 MMAs in groups of 9 outputs. Bitwise equal to the
+// per-pixel and pipelined engines; one pass instead of W sequential ops.
+// Input columns stream through a ring of kVSlots slots; TMEM columns
+// [0, W*F). Barriers are initialised per call and invalidated at its end,
+// after every arrival on them has been waited for.
+template <int F>
+__device__ bool v_row_op(const OpArgs& a, TcSmem& s, TcState& st, int64_t tile, int r, int H, int W) {
+  using T = __nv_bfloat16;
+  using SC = SiteCfg<F>;
+  constexpr int F2 = F / 2;
+  constexpr int NC = SC::kNC;
+  constexpr int NSL = SC::kVSlots;
+  constexpr int kBlk = SC::kBlk;
+  constexpr uint32_t kBlk16 = kBlk >> 4, kWRow16 = (F * 3 * F * 2) >> 4;
+  constexpr uint32_t kKs16 = (2 * 2048) >> 4, kKsW16 = (2 * 3 * F * 16) >> 4;
+  const int P = H * W;
+  const int m = threadIdx.x;
+  uint64_t* full = s.vbar;          // [NSL] column loaded
+  uint64_t* mdone = s.vbar + NSL;   // [NSL] MMAs of the column in the slot done
+  uint64_t* done = s.vbar + 2 * NSL;  // all MMAs done
+  if (m == 0) {
+    for (int i = 0; i < 2 * NSL + 1; ++i) mbar_init(&s.vbar[i], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  const int k_lo = 2 - r > 0 ? 2 - r : 0;
+  auto load_col = [&](int x) {
+    const int sl = x % NSL;
+    mbar_arrive_expect_tx(&full[sl], (uint32_t)(3 - k_lo) * kBlk);
+    for (int k = k_lo; k < 3; ++k)
+      bulk_g2s(s.a_ptr + (sl * 3 + k) * kBlk, blk<T>(a.in, tile, P, (r - 2 + k) * W + x, F), kBlk, &full[sl]);
+  };
+  const uint32_t wbytes = 3 * F * 3 * F * 2, cbytes = F * NC * 2;
+  if (m == 0) {
+    mbar_arrive_expect_tx(s.bar_load, wbytes + cbytes);
+    bulk_g2s(s.w_ptr, a.main.ws, wbytes, s.bar_load);
+    bulk_g2s(s.cw_ptr, a.chain.w, cbytes, s.bar_load);
+    for (int x = 0; x < W && x < NSL - 1; ++x) load_col(x);
+  }
+  if (!tc_wait(s.bar_load, st.ph_load, st)) return false;
+  const uint64_t a0 = umma_sdesc(s.a, 2048, 128);
+  const uint64_t w0 = umma_sdesc(s.w, 3 * F * 16, 128);
+  const uint32_t idesc1 = umma_idesc_bf16(128, F), idesc2 = umma_idesc_bf16(128, 2 * F),
+                 idesc3 = umma_idesc_bf16(128, 3 * F);
+  bool ok = true;
+  for (int x = 0; x < W && ok && m == 0; ++x) {
+    const int sl = x % NSL;
+    ok = mbar_wait(&full[sl], (uint32_t)(x / NSL) & 1, st.err);
+    if (ok) {
+      tc_fence_after();
+      const int c_lo = x - 1 < 0 ? 0 : x - 1;
+      const int c_hi = x + 1 < W - 1 ? x + 1 : W - 1;
+      const int c_f = x == 0 ? c_lo : (x + 1 < c_hi + 1 ? x + 1 : c_hi + 1);
+      bool first = true;
+      for (int k = k_lo; k < 3; ++k) {
+#pragma unroll
+        for (int ks = 0; ks < F / 16; ++ks) {
+          const uint64_t ad = a0 + (uint32_t)(sl * 3 + k) * kBlk16 + ks * kKs16;
+          const uint64_t bd = w0 + (uint32_t)k * kWRow16 + ks * kKsW16;
+          auto mma = [&](int ca, int cb, uint32_t acc) {
+            if (ca > cb) return;
+            const int n = cb - ca + 1;
+            umma_bf16(st.tmem + ca * F, ad, bd + (uint32_t)((ca - x + 1) * F),
+                      n == 3 ? idesc3 : (n == 2 ? idesc2 : idesc1), acc);
+          };
+          if (first) {
+            mma(c_lo, c_f - 1, 1u);
+            mma(c_f, c_hi, 0u);
+            first = false;
+          } else {
+            mma(c_lo, c_hi, 1u);
+          }
+        }
+      }
+      umma_commit(&mdone[sl]);
+    }
+    // the slot of column x+NSL-1 is free once the MMAs of column x-1 completed
+    if (ok && x + NSL - 1 < W) {
+      if (x >= 1) ok = mbar_wait(&mdone[(x - 1) % NSL], (uint32_t)((x - 1) / NSL) & 1, st.err);
+      if (ok) load_col(x + NSL - 1);
+    }
+  }
+  if (m == 0 && ok) umma_commit(done);
+  if (__syncthreads_or(m == 0 && !ok)) {
+    st.abort = true;
+    return false;
+  }
+  uint32_t ph_done = 0;
+  if (!tc_wait(done, ph_done, st)) return false;
+  if (m == 0) {
+    // the last arrival on each slot's barrier, then the barriers are retired
+    for (int x = W - NSL < 0 ? 0 : W - NSL; x < W; ++x)
+      if (!mbar_wait(&mdone[x % NSL], (uint32_t)(x / NSL) & 1, st.err)) st.abort = true;
+    for (int i = 0; i < 2 * NSL + 1; ++i) mbar_inval(&s.vbar[i]);
+  }
+  tc_fence_after();
+  const float* bm = a.main.b;
+  const float* bc = a.chain.b;
+  const bool need_res = a.stream_out && a.res;
+  // ring blocks [0, 9): residual rows of a group; [9, 18): its chained inputs
+  constexpr int kChunk = 9;
+  for (int c0 = 0; c0 < W; c0 += kChunk) {
+    const int c1 = c0 + kChunk < W ? c0 + kChunk : W;
+    if (need_res) {
+      if (m == 0) {
+        mbar_arrive_expect_tx(s.bar_load, (uint32_t)(c1 - c0) * kBlk);
+        bulk_g2s(s.a_ptr, blk<T>(a.res, tile, P, r * W + c0, F), (uint32_t)(c1 - c0) * kBlk, s.bar_load);
+      }
+      if (!tc_wait(s.bar_load, st.ph_load, st)) return false;
+    }
+    for (int c = c0; c < c1; ++c) {
+      const int pix = r * W + c;
+      float acc[F];
+#pragma unroll
+      for (int q = 0; q < F / 16; ++q)
+        tmem_ld16(st.tmem + ((uint32_t)((m / 32) * 32) << 16) + c * F + q * 16, acc + q * 16);
+      tmem_ld_wait();
+#pragma unroll
+      for (int n = 0; n < F; ++n) acc[n] += __ldg(bm + n);
+      if (a.stream_out) {
+        float o[F];
+        if (a.res) {
+          load_row(reinterpret_cast<const T*>(s.a_ptr + (c - c0) * kBlk), m, 0, F, o);
+#pragma unroll
+          for (int n = 0; n < F; ++n) o[n] = fmaxf(o[n] + acc[n], 0.f);
+        } else {
+#pragma unroll
+          for (int n = 0; n < F; ++n) o[n] = fmaxf(acc[n], 0.f);
+        }
+        store_row(blk<T>(a.stream_out, tile, P, pix, F), m, 0, F, o);
+      }
+#pragma unroll
+      for (int n = 0; n < F; ++n) acc[n] = fmaxf(acc[n], 0.f);
+      if (a.aux_out) store_row(blk<T>(a.aux_out, tile, P, pix, F), m, 0, F, acc);
+      T* ca = reinterpret_cast<T*>(s.a_ptr + (kChunk + c - c0) * kBlk);
+#pragma unroll
+      for (int g = 0; g < F / 8; ++g) st8(ca + ((int64_t)g * kTile + m) * 8, acc + 8 * g);
+    }
+    fence_proxy_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (m == 0) {
+      const uint32_t idesc = umma_idesc_bf16(128, NC);
+      for (int c = c0; c < c1; ++c) {
+#pragma unroll
+        for (int ks = 0; ks < F / 16; ++ks)
+          umma_bf16(st.tmem + c * F, umma_sdesc(s.a + (kChunk + c - c0) * kBlk + ks * 2 * 2048, 2048, 128),
+                    umma_sdesc(s.cw + ks * 2 * NC * 16, NC * 16, 128), idesc, ks > 0 ? 1u : 0u);
+      }
+      umma_commit(s.bar_mma);
+    }
+    if (!tc_wait(s.bar_mma, st.ph_mma, st)) return false;
+    tc_fence_after();
+    for (int c = c0; c < c1; ++c) {
+      float u[NC];
+      tmem_ld16(st.tmem + ((uint32_t)((m / 32) * 32) << 16) + c * F, u);
+      tmem_ld_wait();
+#pragma unroll
+      for (int n = 0; n < F2; ++n) u[n] = fmaxf(u[n] + __ldg(bc + n), 0.f);
+      if (r + 1 < H) store_row(blk<T>(a.cat, tile, P, (r + 1) * W + c, F), m, F2, F2, u);
+      if (r == 0) {
+#pragma unroll
+        for (int n = 0; n < F2; ++n) u[n] = fmaxf(__ldg(bc + n), 0.f);
+        store_row(blk<T>(a.cat, tile, P, c, F), m, F2, F2, u);
+      }
+    }
+    // the ring blocks of this group are reused by the next group's copies
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+  }
+  tc_op_end();
+  return true;
+}
+
+// The ops of one site: the head C of the last causal conv at (r, c), then H
+// and C of causal convs 0..L-1, then H of conv L (H ops use the H buffer set,
+// C ops ring slots 0..8). While op k's MMAs run, another thread copies op
+// k+1's weights and its taps written at earlier sites into the other set; the
+// tap op k itself produces (H: the x-half of Cat at the next C op's pixel; C:
+// the stream output the next H reads at (r, c)) is written by op k's
+// epilogue straight into op k+1's buffer, besides global memory, and the
+// residual of a C op comes from the shared-memory block where the C op two
+// convs earlier left its output. Taps sit in slot t = 3 (dr + 2) + (dc + 2)
+// (H: dc + 2), so an op's own pixel is slot 8 (H: 2). MMA order and roundings
+// are those of the per-pixel engine (column-major taps, K steps of 16): sampled
+// configurations and log psi are bitwise equal to the forward's. Global
+// stores are made visible to the copy engine once per site: no op copies a
+// tap written at its own site.
+struct SiteBufs {
+  uint8_t* ah;   // H taps (3 blocks)
+  uint8_t* wh;   // H weight slices (3)
+  uint8_t* cwh;  // H chained 1x1 weights
+  uint8_t* res;  // residual block
+  uint64_t* bar_h;
+  uint32_t ph_h;
+};
+
+// One thread: copies of op `a` at (r, c) into its buffer set, all but the
+// op's own pixel (C: its y-half is copied, the x-half comes from the H op).
+template <int F>
+__device__ void site_prefetch(const OpArgs& a, TcSmem& s, SiteBufs& b, int64_t tile, int r, int c, int H, int W,
+                              bool own_full = false) {
+  using SC = SiteCfg<F>;
+  using T = __nv_bfloat16;
+  const int P = H * W;
+  const bool isC = a.kind == kConvC;
+  uint64_t* bar = isC ? s.bar_load : b.bar_h;
+  const uint32_t chain_bytes = F * (isC ? 16 : SC::kNC) * 2;
+  const bool has_chain = !isC || a.last;
+  if (a.first) {
+    mbar_arrive_expect_tx(bar, 2 * F * 16 + chain_bytes);
+    bulk_g2s(b.wh, a.main.w, 2 * F * 16, bar);
+    bulk_g2s(b.cwh, a.chain.w, chain_bytes, bar);
+    return;
+  }
+  const int j_lo = c >= 2 ? 0 : 2 - c;  // first tap column in the lattice
+  const int k_lo = isC ? (r >= 2 ? 0 : 2 - r) : 2;
+  const int nk = isC ? 3 : 1;
+  uint8_t* A = isC ? s.a_ptr : b.ah;
+  const uint32_t full_row = (uint32_t)(3 - j_lo) * SC::kBlk;
+  const uint32_t own_row = own_full ? full_row : full_row - SC::kBlk;
+  uint32_t bytes = (uint32_t)nk * SC::kSlice * 3 + (has_chain ? chain_bytes : 0);
+  bytes += (uint32_t)(3 - k_lo - 1) * full_row + own_row + ((isC && !own_full) ? SC::kBlk / 2 : 0);
+  mbar_arrive_expect_tx(bar, bytes);
+  for (int k = k_lo; k < 3; ++k) {
+    const int slot = isC ? k * 3 + j_lo : j_lo;
+    const T* src = blk<T>(a.in, tile, P, (r - 2 + k) * W + c - 2 + j_lo, F);
+    const uint32_t n = k < 2 ? full_row : own_row;
+    if (n) bulk_g2s(A + slot * SC::kBlk, src, n, bar);
+  }
+  if (isC && !own_full) {
+    const char* own = reinterpret_cast<const char*>(blk<T>(a.in, tile, P, r * W + c, F));
+    bulk_g2s(A + 8 * SC::kBlk + SC::kBlk / 2, own + SC::kBlk / 2, SC::kBlk / 2, bar);
+  }
+  bulk_g2s(isC ? s.w_ptr : b.wh, a.main.w, (uint32_t)nk * 3 * SC::kSlice, bar);
+  if (has_chain) bulk_g2s(isC ? s.cw_ptr : b.cwh, a.chain.w, chain_bytes, bar);
+}
+
+// Chained 1x1 conv on tensor cores with its weights at shared address cw.
+template <int KC, int NCPAD>
+__device__ bool site_chain(TcSmem& s, TcState& st, uint32_t cw, const float* in, float* out) {
+  const int m = threadIdx.x;
+  __nv_bfloat16* ca = reinterpret_cast<__nv_bfloat16*>(s.ca_ptr);
+#pragma unroll
+  for (int g = 0; g < KC / 8; ++g) st8(ca + ((int64_t)g * kTile + m) * 8, in + 8 * g);
+  fence_proxy_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  if (m == 0) {
+    tc_fence_after();
+    const uint32_t idesc = umma_idesc_bf16(128, NCPAD);
+#pragma unroll
+    for (int ks = 0; ks < KC / 16; ++ks)
+      umma_bf16(st.tmem + kChainCol, umma_sdesc(s.ca + ks * 2 * 2048, 2048, 128),
+                umma_sdesc(cw + ks * 2 * NCPAD * 16, NCPAD * 16, 128), idesc, ks > 0 ? 1u : 0u);
+    umma_commit(s.bar_mma);
+  }
+  if (!tc_wait(s.bar_mma, st.ph_mma, st)) return false;
+  tc_fence_after();
+  tc_read<NCPAD>(st, kChainCol, out);
+  return true;
+}
+
+// Op `a` at (r, c) from its buffer set, the run_op epilogue, and (thread 32)
+// the copies of the next op `nx` at (r, nc). keep_res: the C output is the
+// residual of the C op two convs later. site_end: last op of the site.
+template <int F>
+__device__ bool site_op(const OpArgs& a, TcSmem& s, TcState& st, SiteBufs& b, int64_t tile, int r, int c, int H,
+                        int W, const OpArgs* nx, int nc, bool keep_res, bool site_end, HeadOut* head) {
+  using SC = SiteCfg<F>;
+  using T = __nv_bfloat16;
+  constexpr int F2 = F / 2;
+  constexpr int NC2 = SC::kNC;
+  const int P = H * W;
+  const int m = threadIdx.x;
+  const bool isC = a.kind == kConvC;
+  uint8_t* A = isC ? s.a_ptr : b.ah;
+  uint8_t* Wt = isC ? s.w_ptr : b.wh;
+  if (a.first) {
+    // cin = 1: the K = 16 row of spins at the H taps (zero padded)
+    float v[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) v[k] = 0.f;
+    for (int t = 0; t < 3; ++t) {
+      int dr, dc;
+      tap_offset(a.kind, t, dr, dc);
+      const int rr = r + dr, cc = c + dc;
+      if (rr >= 0 && rr < H && cc >= 0 && cc < W) v[t] = spin_at(a.spins, a.batch, P, tile * kTile + m, rr * W + cc);
+    }
+    st8(reinterpret_cast<T*>(A + m * 16), v);
+    st8(reinterpret_cast<T*>(A + 2048 + m * 16), v + 8);
+    fence_proxy_async_smem();
+    __syncthreads();
+  }
+  if (!tc_wait(isC ? s.bar_load : b.bar_h, isC ? st.ph_load : b.ph_h, st)) return false;
+  if (m == 0) {
+    tc_fence_after();
+    const uint64_t a0 = umma_sdesc(smem_u32(A), 2048, 128);
+    const uint64_t w0 = umma_sdesc(smem_u32(Wt), F * 16, 128);
+    const uint32_t idesc = umma_idesc_bf16(128, F);
+    if (a.first) {
+      umma_bf16(st.tmem, a0, w0, idesc, 0u);
+    } else {
+      // column-major taps: tap column j outer, tap row k inner
+      const int j_lo = c >= 2 ? 0 : 2 - c;
+      const int k_lo = isC ? (r >= 2 ? 0 : 2 - r) : 2;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          if (j < j_lo || k < k_lo || (!isC && k < 2)) continue;
+          const uint32_t t = isC ? (uint32_t)(k * 3 + j) : (uint32_t)j;
+#pragma unroll
+          for (int ks = 0; ks < F / 16; ++ks)
+            umma_bf16(st.tmem, a0 + ((t * SC::kBlk + ks * 4096) >> 4), w0 + ((t * SC::kSlice + ks * 2 * F * 16) >> 4),
+                      idesc, (j > j_lo || k > k_lo || ks > 0) ? 1u : 0u);
+        }
+      }
+    }
+    umma_commit(s.bar_mma);
+  }
+  if (m == 32 && nx) site_prefetch<F>(*nx, s, b, tile, r, nc, H, W);
+  if (!tc_wait(s.bar_mma, st.ph_mma, st)) return false;
+  tc_fence_after();
+  float acc[F];
+  tc_read<F>(st, 0, acc);
+  const float* bm = a.main.b;
+  const float* bc = a.chain.b;
+  const int pix = r * W + c;
+  if (!isC) {
+#pragma unroll
+    for (int n = 0; n < F; ++n) acc[n] = fmaxf(acc[n] + __ldg(bm + n), 0.f);
+    if (a.aux_out) store_row(blk<T>(a.aux_out, tile, P, pix, F), m, 0, F, acc);
+    float z[NC2];
+    if (!site_chain<F, NC2>(s, st, smem_u32(b.cwh), acc, z)) return false;
+#pragma unroll
+    for (int n = 0; n < F2; ++n) z[n] = fmaxf(z[n] + __ldg(bc + n), 0.f);
+    const int sh = a.last ? 1 : 0;
+    if (c + sh < W) {
+      store_row(blk<T>(a.cat, tile, P, pix + sh, F), m, 0, F2, z);
+      // x-half of the next C op's own pixel (r, c + sh)
+      store_row(reinterpret_cast<T*>(s.a_ptr + 8 * SC::kBlk), m, 0, F2, z);
+    }
+    if (sh && c == 0) {
+#pragma unroll
+      for (int n = 0; n < F2; ++n) z[n] = fmaxf(__ldg(bc + n), 0.f);
+      store_row(blk<T>(a.cat, tile, P, pix, F), m, 0, F2, z);
+    }
+  } else {
+#pragma unroll
+    for (int n = 0; n < F; ++n) acc[n] += __ldg(bm + n);
+    if (!a.last) {
+      float o[F];
+      if (a.res) {
+        load_row(reinterpret_cast<const T*>(b.res), m, 0, F, o);
+#pragma unroll
+        for (int n = 0; n < F; ++n) o[n] = fmaxf(o[n] + acc[n], 0.f);
+      } else {
+#pragma unroll
+        for (int n = 0; n < F; ++n) o[n] = fmaxf(acc[n], 0.f);
+      }
+      store_row(blk<T>(a.stream_out, tile, P, pix, F), m, 0, F, o);
+      // the next H op's own pixel, and the residual of a later C op
+      store_row(reinterpret_cast<T*>(b.ah + 2 * SC::kBlk), m, 0, F, o);
+      if (keep_res) store_row(reinterpret_cast<T*>(b.res), m, 0, F, o);
+    } else {
+#pragma unroll
+      for (int n = 0; n < F; ++n) acc[n] = fmaxf(acc[n], 0.f);
+      if (a.stream_out) store_row(blk<T>(a.stream_out, tile, P, pix, F), m, 0, F, acc);
+      float l[16];
+      if (!site_chain<F, 16>(s, st, s.cw, acc, l)) return false;
+#pragma unroll
+      for (int n = 0; n < 4; ++n) l[n] += __ldg(bc + n);
+      *head = normalise_head(l);
+    }
+  }
+  if (site_end)
+    asm volatile("fence.proxy.async;" ::: "memory");
+  else
+    fence_proxy_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  return true;
+}
+
 struct SampleArgs {
   OpArgs op[40][3];
   int n_cc;
@@ -1086,6 +1506,7 @@ struct SampleArgs {
   uint32_t seed_lo, seed_hi, off_lo, off_hi;
   int8_t* spins;
   float2* row_partial;
+  uint64_t keep_res;  // bit i: the C output of causal conv i is the residual of conv i + 2
 };
 
 template <int F, bool TC>
@@ -1117,14 +1538,79 @@ __global__ void __launch_bounds__(128) sample_kernel(const __grid_constant__ Sam
   __syncthreads();
   TcSmem s;
   TcState st;
-  if (TC) {
+  // the V ops of a row run as one pass when the TMEM holds W accumulators
+  uint32_t ncols = kTmemCols;
+  const bool vrow = TC && F <= 32 && W * F <= 512;
+  if (vrow)
+    while (ncols < (uint32_t)(W * F)) ncols *= 2;
+  constexpr bool kSite = TC && F <= 32;
+  SiteBufs b;
+  if constexpr (kSite) {
+    using SC = SiteCfg<F>;
+    s.a_ptr = smem;
+    s.w_ptr = smem + SC::kW;
+    s.cw_ptr = smem + SC::kCW;
+    s.ca_ptr = smem + SC::kCA;
+    s.bar_load = reinterpret_cast<uint64_t*>(smem + SC::kBar);
+    s.bar_mma = s.bar_load + 1;
+    s.tmem_slot = reinterpret_cast<uint32_t*>(s.bar_load + 2);
+    s.vbar = s.bar_load + 3;  // 2 * kVSlots + 1 barriers
+    s.a = smem_u32(s.a_ptr);
+    s.w = smem_u32(s.w_ptr);
+    s.ca = smem_u32(s.ca_ptr);
+    s.cw = smem_u32(s.cw_ptr);
+    s.taps_per_group = TcCfg<F>::kTaps;
+    b.ah = smem + SC::kAH;
+    b.wh = smem + SC::kWH;
+    b.cwh = smem + SC::kCWH;
+    b.res = smem + SC::kRes;
+    b.bar_h = s.vbar + 2 * SC::kVSlots + 1;
+    b.ph_h = 0;
+    if (m == 0) {
+      mbar_init(b.bar_h, 1);
+      fence_mbar_init();
+    }
+    tc_setup(s, st, err, ncols);
+  } else if (TC) {
     tc_carve<F>(smem, s);
-    tc_setup(s, st, err);
+    tc_setup(s, st, err, ncols);
   }
   Engine<F, TC> eng{&s, &st};
+  // op k of a site: 0 = head C of conv L, then H_0, C_0, ..., H_{L-1}, C_{L-1}, H_L
+  const int nseq = 2 * a.n_cc;
+  auto seq_op = [&](int k) -> const OpArgs& {
+    return k == 0 ? a.op[last][2] : (k == nseq - 1 ? a.op[last][1] : a.op[(k - 1) / 2][(k & 1) ? 1 : 2]);
+  };
   for (int r = 0; r < H && !eng.aborted(); ++r) {
     Kahan kre, kim;
-    for (int c = 0; c < W; ++c) {
+    for (int c = 0; c < W && kSite; ++c) {
+      if constexpr (kSite) {
+        const int pix = r * W + c;
+        if (c == 0 && m == 32) site_prefetch<F>(seq_op(0), s, b, tile, r, 0, H, W, true);
+        for (int k = 0; k < nseq; ++k) {
+          const OpArgs* nx = k + 1 < nseq ? &seq_op(k + 1) : (c + 1 < W ? &seq_op(0) : nullptr);
+          const bool keep = k >= 2 && (k & 1) == 0 && ((a.keep_res >> ((k - 2) / 2)) & 1);
+          HeadOut h;
+          if (!site_op<F>(seq_op(k), s, st, b, tile, r, c, H, W, nx, k + 1 < nseq ? c : c + 1, keep, k == nseq - 1,
+                          &h)) {
+            st.abort = true;
+            break;
+          }
+          if (k == 0) {
+            // deepar/samplers/autoregressive.py:41-43 (+1 iff p(+1) > U), drawn
+            // with Philox counter (sample, site, offset).
+            U4 x = philox4x32(U4{(uint32_t)sample, (uint32_t)pix, a.off_lo, a.off_hi}, a.seed_lo, a.seed_hi);
+            float u = philox_uniform(x.x);
+            bool up = expf(2.f * h.re0) > u;
+            kre.add(up ? h.re0 : h.re1);
+            kim.add(up ? h.im0 : h.im1);
+            if (sample < a.batch) a.spins[sample * P + pix] = up ? (int8_t)1 : (int8_t)-1;
+          }
+        }
+        if (eng.aborted()) break;
+      }
+    }
+    for (int c = 0; c < W && !kSite; ++c) {
       const int pix = r * W + c;
       HeadOut h;
       run_op<F, TC, T>(a.op[last][2], eng, tile, r, c, H, W, P, &h);
@@ -1151,6 +1637,12 @@ __global__ void __launch_bounds__(128) sample_kernel(const __grid_constant__ Sam
     if (eng.aborted()) break;
     a.row_partial[((int64_t)tile * H + r) * kTile + m] = make_float2(kre.s - kre.c, kim.s - kim.c);
     for (int i = 0; i < a.n_cc && !eng.aborted(); ++i) {
+      if (TC && vrow && a.op[i][0].main.ws) {
+        if constexpr (TC) {
+          if (!v_row_op<F>(a.op[i][0], s, st, tile, r, H, W)) st.abort = true;
+        }
+        continue;
+      }
       for (int c = 0; c < W; ++c) {
         HeadOut h;
         run_op<F, TC, T>(a.op[i][0], eng, tile, r, c, H, W, P, &h);
@@ -1179,11 +1671,27 @@ static int sample_impl(const NetLayout& L, const void* packed, int64_t batch, ui
     CCTensors x = cc_tensors(L, T, FK_AR2D_SAVE, i);
     make_ops(L, packed, i, spins, batch, x.vin, x.hin, x.vres, x.hres, x.vout, x.hout, x.cat, x.t, x.rv, a->op[i]);
   }
-  size_t smem = TC ? (size_t)TcCfg<F>::kSmem : 0;
+  // the tensor-core sampler keeps a C output in shared memory for the C op
+  // whose residual it is, which must be the one two causal convs later
+  for (int i = 0; i < L.n_cc; ++i) {
+    if (!a->op[i][2].res) continue;
+    if (i < 2 || a->op[i][2].res != a->op[i - 2][2].stream_out) {
+      delete a;
+      return FK_ERR_ARG;
+    }
+    a->keep_res |= 1ull << (i - 2);
+  }
+  if (a->keep_res & (a->keep_res >> 1)) {  // one residual block: sources two convs apart
+    delete a;
+    return FK_ERR_ARG;
+  }
+  size_t smem = TC ? (size_t)(F <= 32 ? SiteCfg<F>::kSmem : TcCfg<F>::kSmem) : 0;
+  // a CTA that holds all 512 TMEM columns keeps its SM to itself
+  if (TC && F <= 32 && L.W * F > 256 && smem < 120 * 1024) smem = 120 * 1024;
   int st = FK_OK;
   if (TC) {
     st = check_cuda(cudaFuncSetAttribute(sample_kernel<F, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)TcCfg<F>::kSmem),
+                                         (int)smem),
                     "cudaFuncSetAttribute");
   }
   if (st == FK_OK) {
