@@ -1083,6 +1083,40 @@ static int forward_impl(const NetLayout& L, const void* packed, const int8_t* sp
 //   end of row r: for every i: V op_i over (r, 0..W-1)
 // Every (layer, pixel) is evaluated once, after all the sites it depends on.
 // ---- exact sampler on tensor cores (F <= 32)
+// Op record of the sampler, copied from the kernel parameters into shared
+// memory at kernel start (the ops of a site cycle through more parameter data
+// than the constant cache holds).
+struct SampOp {
+  const void* in;
+  const void* w;    // main weights (V: the column-scatter operand)
+  const void* cw;   // chained 1x1 weights
+  const float* b;   // main bias
+  const float* cb;  // chained bias
+  void* out;        // stream output
+  void* aux;        // saved activation
+  void* cat;
+  const void* res;
+  int kind;
+  int flags;  // 1: first causal conv, 2: last causal conv
+  __device__ bool first() const { return flags & 1; }
+  __device__ bool last() const { return (flags >> 1) & 1; }
+};
+static_assert(sizeof(SampOp) == 80, "sampler op record");
+
+__device__ __forceinline__ void samp_op_from(const OpArgs& a, SampOp& o) {
+  o.in = a.in;
+  o.w = a.kind == kConvV ? a.main.ws : a.main.w;
+  o.cw = a.chain.w;
+  o.b = a.main.b;
+  o.cb = a.chain.b;
+  o.out = a.stream_out;
+  o.aux = a.aux_out;
+  o.cat = a.cat;
+  o.res = a.res;
+  o.kind = a.kind;
+  o.flags = (a.first ? 1 : 0) | (a.last ? 2 : 0);
+}
+
 // Shared memory of the sampler kernel: a ring of 18 activation blocks (C taps
 // in slots 0..8 during sites; the column ring, residual and chained inputs of
 // the row-end V ops), main / chained weights, the chained-input block, the H
@@ -1102,7 +1136,8 @@ struct SiteCfg {
   static constexpr int kCWH = kWH + 3 * kSlice;
   static constexpr int kRes = kCWH + F * kNC * 2;
   static constexpr int kBar = kRes + kBlk;
-  static constexpr int kSmem = kBar + 256;
+  static constexpr int kOps = kBar + 256;  // SampOp[3 * 40]
+  static constexpr int kSmem = kOps + 3 * 40 * (int)sizeof(SampOp);
 };
 static_assert(SiteCfg<32>::kSmem <= 227 * 1024, "sampler shared memory");
 
@@ -1114,10 +1149,11 @@ static_assert(SiteCfg<32>::kSmem <= 227 * 1024, "sampler shared memory");
 // output and the chained 1x1 MMAs in groups of 9 outputs. Bitwise equal to the
 // per-pixel and pipelined engines; one pass instead of W sequential ops.
 // Input columns stream through a ring of kVSlots slots; TMEM columns
-// [0, W*F). Barriers are initialised per call and invalidated at its end,
-// after every arrival on them has been waited for.
+// [0, W*F). Barriers are initialised per call and invalidated at its end;
+// every arrival on them is waited for (an MMA commit arrives on its barrier
+// some time after the commit that follows it may have been observed).
 template <int F>
-__device__ bool v_row_op(const OpArgs& a, TcSmem& s, TcState& st, int64_t tile, int r, int H, int W) {
+__device__ bool v_row_op(const SampOp& a, TcSmem& s, TcState& st, int64_t tile, int r, int H, int W) {
   using T = __nv_bfloat16;
   using SC = SiteCfg<F>;
   constexpr int F2 = F / 2;
@@ -1146,8 +1182,8 @@ __device__ bool v_row_op(const OpArgs& a, TcSmem& s, TcState& st, int64_t tile, 
   const uint32_t wbytes = 3 * F * 3 * F * 2, cbytes = F * NC * 2;
   if (m == 0) {
     mbar_arrive_expect_tx(s.bar_load, wbytes + cbytes);
-    bulk_g2s(s.w_ptr, a.main.ws, wbytes, s.bar_load);
-    bulk_g2s(s.cw_ptr, a.chain.w, cbytes, s.bar_load);
+    bulk_g2s(s.w_ptr, a.w, wbytes, s.bar_load);
+    bulk_g2s(s.cw_ptr, a.cw, cbytes, s.bar_load);
     for (int x = 0; x < W && x < NSL - 1; ++x) load_col(x);
   }
   if (!tc_wait(s.bar_load, st.ph_load, st)) return false;
@@ -1185,7 +1221,8 @@ __device__ bool v_row_op(const OpArgs& a, TcSmem& s, TcState& st, int64_t tile, 
           }
         }
       }
-      umma_commit(&mdone[sl]);
+      // only columns whose slot is refilled signal it: every arrival is waited for
+      if (x + NSL < W) umma_commit(&mdone[sl]);
     }
     // the slot of column x+NSL-1 is free once the MMAs of column x-1 completed
     if (ok && x + NSL - 1 < W) {
@@ -1200,16 +1237,12 @@ __device__ bool v_row_op(const OpArgs& a, TcSmem& s, TcState& st, int64_t tile, 
   }
   uint32_t ph_done = 0;
   if (!tc_wait(done, ph_done, st)) return false;
-  if (m == 0) {
-    // the last arrival on each slot's barrier, then the barriers are retired
-    for (int x = W - NSL < 0 ? 0 : W - NSL; x < W; ++x)
-      if (!mbar_wait(&mdone[x % NSL], (uint32_t)(x / NSL) & 1, st.err)) st.abort = true;
+  if (m == 0)
     for (int i = 0; i < 2 * NSL + 1; ++i) mbar_inval(&s.vbar[i]);
-  }
   tc_fence_after();
-  const float* bm = a.main.b;
-  const float* bc = a.chain.b;
-  const bool need_res = a.stream_out && a.res;
+  const float* bm = a.b;
+  const float* bc = a.cb;
+  const bool need_res = a.out && a.res;
   // ring blocks [0, 9): residual rows of a group; [9, 18): its chained inputs
   constexpr int kChunk = 9;
   for (int c0 = 0; c0 < W; c0 += kChunk) {
@@ -1230,7 +1263,7 @@ __device__ bool v_row_op(const OpArgs& a, TcSmem& s, TcState& st, int64_t tile, 
       tmem_ld_wait();
 #pragma unroll
       for (int n = 0; n < F; ++n) acc[n] += __ldg(bm + n);
-      if (a.stream_out) {
+      if (a.out) {
         float o[F];
         if (a.res) {
           load_row(reinterpret_cast<const T*>(s.a_ptr + (c - c0) * kBlk), m, 0, F, o);
@@ -1240,11 +1273,11 @@ __device__ bool v_row_op(const OpArgs& a, TcSmem& s, TcState& st, int64_t tile, 
 #pragma unroll
           for (int n = 0; n < F; ++n) o[n] = fmaxf(acc[n], 0.f);
         }
-        store_row(blk<T>(a.stream_out, tile, P, pix, F), m, 0, F, o);
+        store_row(blk<T>(a.out, tile, P, pix, F), m, 0, F, o);
       }
 #pragma unroll
       for (int n = 0; n < F; ++n) acc[n] = fmaxf(acc[n], 0.f);
-      if (a.aux_out) store_row(blk<T>(a.aux_out, tile, P, pix, F), m, 0, F, acc);
+      if (a.aux) store_row(blk<T>(a.aux, tile, P, pix, F), m, 0, F, acc);
       T* ca = reinterpret_cast<T*>(s.a_ptr + (kChunk + c - c0) * kBlk);
 #pragma unroll
       for (int g = 0; g < F / 8; ++g) st8(ca + ((int64_t)g * kTile + m) * 8, acc + 8 * g);
@@ -1308,12 +1341,14 @@ struct SiteBufs {
   uint8_t* res;  // residual block
   uint64_t* bar_h;
   uint32_t ph_h;
+  const int8_t* spins;
+  int64_t batch;
 };
 
 // One thread: copies of op `a` at (r, c) into its buffer set, all but the
 // op's own pixel (C: its y-half is copied, the x-half comes from the H op).
 template <int F>
-__device__ void site_prefetch(const OpArgs& a, TcSmem& s, SiteBufs& b, int64_t tile, int r, int c, int H, int W,
+__device__ void site_prefetch(const SampOp& a, TcSmem& s, SiteBufs& b, int64_t tile, int r, int c, int H, int W,
                               bool own_full = false) {
   using SC = SiteCfg<F>;
   using T = __nv_bfloat16;
@@ -1321,11 +1356,11 @@ __device__ void site_prefetch(const OpArgs& a, TcSmem& s, SiteBufs& b, int64_t t
   const bool isC = a.kind == kConvC;
   uint64_t* bar = isC ? s.bar_load : b.bar_h;
   const uint32_t chain_bytes = F * (isC ? 16 : SC::kNC) * 2;
-  const bool has_chain = !isC || a.last;
-  if (a.first) {
+  const bool has_chain = !isC || a.last();
+  if (a.first()) {
     mbar_arrive_expect_tx(bar, 2 * F * 16 + chain_bytes);
-    bulk_g2s(b.wh, a.main.w, 2 * F * 16, bar);
-    bulk_g2s(b.cwh, a.chain.w, chain_bytes, bar);
+    bulk_g2s(b.wh, a.w, 2 * F * 16, bar);
+    bulk_g2s(b.cwh, a.cw, chain_bytes, bar);
     return;
   }
   const int j_lo = c >= 2 ? 0 : 2 - c;  // first tap column in the lattice
@@ -1347,8 +1382,8 @@ __device__ void site_prefetch(const OpArgs& a, TcSmem& s, SiteBufs& b, int64_t t
     const char* own = reinterpret_cast<const char*>(blk<T>(a.in, tile, P, r * W + c, F));
     bulk_g2s(A + 8 * SC::kBlk + SC::kBlk / 2, own + SC::kBlk / 2, SC::kBlk / 2, bar);
   }
-  bulk_g2s(isC ? s.w_ptr : b.wh, a.main.w, (uint32_t)nk * 3 * SC::kSlice, bar);
-  if (has_chain) bulk_g2s(isC ? s.cw_ptr : b.cwh, a.chain.w, chain_bytes, bar);
+  bulk_g2s(isC ? s.w_ptr : b.wh, a.w, (uint32_t)nk * 3 * SC::kSlice, bar);
+  if (has_chain) bulk_g2s(isC ? s.cw_ptr : b.cwh, a.cw, chain_bytes, bar);
 }
 
 // Chained 1x1 conv on tensor cores with its weights at shared address cw.
@@ -1380,8 +1415,8 @@ __device__ bool site_chain(TcSmem& s, TcState& st, uint32_t cw, const float* in,
 // the copies of the next op `nx` at (r, nc). keep_res: the C output is the
 // residual of the C op two convs later. site_end: last op of the site.
 template <int F>
-__device__ bool site_op(const OpArgs& a, TcSmem& s, TcState& st, SiteBufs& b, int64_t tile, int r, int c, int H,
-                        int W, const OpArgs* nx, int nc, bool keep_res, bool site_end, HeadOut* head) {
+__device__ bool site_op(const SampOp& a, TcSmem& s, TcState& st, SiteBufs& b, int64_t tile, int r, int c, int H,
+                        int W, const SampOp* nx, int nc, bool keep_res, bool site_end, HeadOut* head) {
   using SC = SiteCfg<F>;
   using T = __nv_bfloat16;
   constexpr int F2 = F / 2;
@@ -1391,7 +1426,7 @@ __device__ bool site_op(const OpArgs& a, TcSmem& s, TcState& st, SiteBufs& b, in
   const bool isC = a.kind == kConvC;
   uint8_t* A = isC ? s.a_ptr : b.ah;
   uint8_t* Wt = isC ? s.w_ptr : b.wh;
-  if (a.first) {
+  if (a.first()) {
     // cin = 1: the K = 16 row of spins at the H taps (zero padded)
     float v[16];
 #pragma unroll
@@ -1400,7 +1435,7 @@ __device__ bool site_op(const OpArgs& a, TcSmem& s, TcState& st, SiteBufs& b, in
       int dr, dc;
       tap_offset(a.kind, t, dr, dc);
       const int rr = r + dr, cc = c + dc;
-      if (rr >= 0 && rr < H && cc >= 0 && cc < W) v[t] = spin_at(a.spins, a.batch, P, tile * kTile + m, rr * W + cc);
+      if (rr >= 0 && rr < H && cc >= 0 && cc < W) v[t] = spin_at(b.spins, b.batch, P, tile * kTile + m, rr * W + cc);
     }
     st8(reinterpret_cast<T*>(A + m * 16), v);
     st8(reinterpret_cast<T*>(A + 2048 + m * 16), v + 8);
@@ -1413,7 +1448,7 @@ __device__ bool site_op(const OpArgs& a, TcSmem& s, TcState& st, SiteBufs& b, in
     const uint64_t a0 = umma_sdesc(smem_u32(A), 2048, 128);
     const uint64_t w0 = umma_sdesc(smem_u32(Wt), F * 16, 128);
     const uint32_t idesc = umma_idesc_bf16(128, F);
-    if (a.first) {
+    if (a.first()) {
       umma_bf16(st.tmem, a0, w0, idesc, 0u);
     } else {
       // column-major taps: tap column j outer, tap row k inner
@@ -1439,18 +1474,18 @@ __device__ bool site_op(const OpArgs& a, TcSmem& s, TcState& st, SiteBufs& b, in
   tc_fence_after();
   float acc[F];
   tc_read<F>(st, 0, acc);
-  const float* bm = a.main.b;
-  const float* bc = a.chain.b;
+  const float* bm = a.b;
+  const float* bc = a.cb;
   const int pix = r * W + c;
   if (!isC) {
 #pragma unroll
     for (int n = 0; n < F; ++n) acc[n] = fmaxf(acc[n] + __ldg(bm + n), 0.f);
-    if (a.aux_out) store_row(blk<T>(a.aux_out, tile, P, pix, F), m, 0, F, acc);
+    if (a.aux) store_row(blk<T>(a.aux, tile, P, pix, F), m, 0, F, acc);
     float z[NC2];
     if (!site_chain<F, NC2>(s, st, smem_u32(b.cwh), acc, z)) return false;
 #pragma unroll
     for (int n = 0; n < F2; ++n) z[n] = fmaxf(z[n] + __ldg(bc + n), 0.f);
-    const int sh = a.last ? 1 : 0;
+    const int sh = a.last() ? 1 : 0;
     if (c + sh < W) {
       store_row(blk<T>(a.cat, tile, P, pix + sh, F), m, 0, F2, z);
       // x-half of the next C op's own pixel (r, c + sh)
@@ -1464,7 +1499,7 @@ __device__ bool site_op(const OpArgs& a, TcSmem& s, TcState& st, SiteBufs& b, in
   } else {
 #pragma unroll
     for (int n = 0; n < F; ++n) acc[n] += __ldg(bm + n);
-    if (!a.last) {
+    if (!a.last()) {
       float o[F];
       if (a.res) {
         load_row(reinterpret_cast<const T*>(b.res), m, 0, F, o);
@@ -1474,14 +1509,14 @@ __device__ bool site_op(const OpArgs& a, TcSmem& s, TcState& st, SiteBufs& b, in
 #pragma unroll
         for (int n = 0; n < F; ++n) o[n] = fmaxf(acc[n], 0.f);
       }
-      store_row(blk<T>(a.stream_out, tile, P, pix, F), m, 0, F, o);
+      store_row(blk<T>(a.out, tile, P, pix, F), m, 0, F, o);
       // the next H op's own pixel, and the residual of a later C op
       store_row(reinterpret_cast<T*>(b.ah + 2 * SC::kBlk), m, 0, F, o);
       if (keep_res) store_row(reinterpret_cast<T*>(b.res), m, 0, F, o);
     } else {
 #pragma unroll
       for (int n = 0; n < F; ++n) acc[n] = fmaxf(acc[n], 0.f);
-      if (a.stream_out) store_row(blk<T>(a.stream_out, tile, P, pix, F), m, 0, F, acc);
+      if (a.out) store_row(blk<T>(a.out, tile, P, pix, F), m, 0, F, acc);
       float l[16];
       if (!site_chain<F, 16>(s, st, s.cw, acc, l)) return false;
 #pragma unroll
@@ -1566,6 +1601,10 @@ __global__ void __launch_bounds__(128) sample_kernel(const __grid_constant__ Sam
     b.res = smem + SC::kRes;
     b.bar_h = s.vbar + 2 * SC::kVSlots + 1;
     b.ph_h = 0;
+    b.spins = a.spins;
+    b.batch = a.batch;
+    SampOp* ops = reinterpret_cast<SampOp*>(smem + SC::kOps);
+    for (int i = m; i < 3 * a.n_cc; i += kTile) samp_op_from(a.op[i / 3][i % 3], ops[i]);
     if (m == 0) {
       mbar_init(b.bar_h, 1);
       fence_mbar_init();
@@ -1578,8 +1617,9 @@ __global__ void __launch_bounds__(128) sample_kernel(const __grid_constant__ Sam
   Engine<F, TC> eng{&s, &st};
   // op k of a site: 0 = head C of conv L, then H_0, C_0, ..., H_{L-1}, C_{L-1}, H_L
   const int nseq = 2 * a.n_cc;
-  auto seq_op = [&](int k) -> const OpArgs& {
-    return k == 0 ? a.op[last][2] : (k == nseq - 1 ? a.op[last][1] : a.op[(k - 1) / 2][(k & 1) ? 1 : 2]);
+  const SampOp* ops = reinterpret_cast<const SampOp*>(smem + SiteCfg<F <= 32 ? F : 32>::kOps);
+  auto seq_op = [&](int k) -> const SampOp& {
+    return k == 0 ? ops[3 * last + 2] : (k == nseq - 1 ? ops[3 * last + 1] : ops[3 * ((k - 1) / 2) + ((k & 1) ? 1 : 2)]);
   };
   for (int r = 0; r < H && !eng.aborted(); ++r) {
     Kahan kre, kim;
@@ -1588,7 +1628,7 @@ __global__ void __launch_bounds__(128) sample_kernel(const __grid_constant__ Sam
         const int pix = r * W + c;
         if (c == 0 && m == 32) site_prefetch<F>(seq_op(0), s, b, tile, r, 0, H, W, true);
         for (int k = 0; k < nseq; ++k) {
-          const OpArgs* nx = k + 1 < nseq ? &seq_op(k + 1) : (c + 1 < W ? &seq_op(0) : nullptr);
+          const SampOp* nx = k + 1 < nseq ? &seq_op(k + 1) : (c + 1 < W ? &seq_op(0) : nullptr);
           const bool keep = k >= 2 && (k & 1) == 0 && ((a.keep_res >> ((k - 2) / 2)) & 1);
           HeadOut h;
           if (!site_op<F>(seq_op(k), s, st, b, tile, r, c, H, W, nx, k + 1 < nseq ? c : c + 1, keep, k == nseq - 1,
@@ -1637,9 +1677,9 @@ __global__ void __launch_bounds__(128) sample_kernel(const __grid_constant__ Sam
     if (eng.aborted()) break;
     a.row_partial[((int64_t)tile * H + r) * kTile + m] = make_float2(kre.s - kre.c, kim.s - kim.c);
     for (int i = 0; i < a.n_cc && !eng.aborted(); ++i) {
-      if (TC && vrow && a.op[i][0].main.ws) {
-        if constexpr (TC) {
-          if (!v_row_op<F>(a.op[i][0], s, st, tile, r, H, W)) st.abort = true;
+      if (kSite && vrow && a.op[i][0].main.ws) {
+        if constexpr (kSite) {
+          if (!v_row_op<F>(ops[3 * i], s, st, tile, r, H, W)) st.abort = true;
         }
         continue;
       }
