@@ -215,6 +215,10 @@ __global__ void __launch_bounds__(kPipeThreads, 1) op_pipe_kernel(const __grid_c
           reinterpret_cast<float4*>(a.cond)[sample * P + pix] = make_float4(re0, re1, out[2], out[3]);
       }
     };
+    // residual rows (raw bf16) of the group's next output in the same row,
+    // loaded while the current output is processed
+    uint4 rraw[F / 8];
+    bool have_raw = false;
     uint32_t p = 0, it_count = 0;
     for (int64_t it = blockIdx.x; it < n_items && !abort; it += gridDim.x, ++it_count) {
       const int64_t item = item_at(it);
@@ -227,13 +231,18 @@ __global__ void __launch_bounds__(kPipeThreads, 1) op_pipe_kernel(const __grid_c
         const uint32_t sl = p % NS;
         const int pix = r * W + c;
         float o[F];
-        if (need_res) load_row(blk<T>(a.res, tile, P, pix, F), m, 0, F, o);
+        if (need_res && !have_raw) load_raw<F>(blk<T>(a.res, tile, P, pix, F), m, rraw);
         if (!uwait(&accf[sl], (p / NS) & 1, err, abort)) break;
         tc_fence_after();
         float acc[F];
         tread<F>(tl, sl * F, acc);
         tc_fence_before();
         warp_arrive(&acce[sl]);
+        if (need_res) {
+          unpack_raw<F>(rraw, o);
+          have_raw = c + C::kGroups < W;
+          if (have_raw) load_raw<F>(blk<T>(a.res, tile, P, pix + C::kGroups, F), m, rraw);
+        }
         float cin[F];
         if (kind == kConvV) {
 #pragma unroll
