@@ -69,6 +69,14 @@ def test_lanczos_heisenberg_chain_20_pbc():
     assert e == pytest.approx(-35.6175461195, abs=1e-8)
 
 
+def test_lanczos_heisenberg_4x4_pbc():
+    # the exact energy the 4x4 training case of bench.py is compared with
+    import bench
+    e = exact.lanczos_ground_energy(lambda s: operators.heisenberg_find_conn(s, pbc=True), (4, 4))
+    assert e == pytest.approx(bench.HEISENBERG_4X4_PBC_E0, abs=1e-8)
+    assert e == pytest.approx(-44.91393283371548, abs=1e-8)
+
+
 def test_lanczos_j1j2_4x4_obc():
     # examples/j1j2_2d_monte_carlo_4.py:43,48
     basis = exact.sz_sector((4, 4), 0)
