@@ -69,6 +69,8 @@ _SIGNATURES = {
     "fk_rbm_mh_sweeps": (c_i32, [c_p, c_i32, c_i32, c_i32, c_i32, c_i32, c_p, c_p, c_i64, c_i64, c_i32, c_i32, c_u64,
                                  c_u64, c_p, c_p, c_p]),
     "fk_mh_independent_step": (c_i32, [c_p, c_p, c_p, c_p, c_p, c_p, c_i64, c_i32, c_u64, c_u64, c_p, c_p]),
+    "fk_mh_hamiltonian_propose": (c_i32, [c_p, c_p, c_p, c_i32, c_i64, c_i32, c_u64, c_u64, c_p, c_p, c_p]),
+    "fk_mh_hamiltonian_accept": (c_i32, [c_p, c_p, c_p, c_p, c_p, c_p, c_i32, c_i64, c_i32, c_u64, c_u64, c_p, c_p]),
 }
 
 _lib = None

@@ -295,6 +295,62 @@ __global__ void mh_independent_kernel(int8_t* __restrict__ chains, float2* __res
   }
 }
 
+// Metropolis-Hastings with Hamiltonian proposals (metropolis_hastings.py:170-195):
+// the candidate is one of the chain's used connections of the operator (in
+// find_conn slot order), drawn uniformly with Philox word 0 of counter
+// (chain, sweep_lo, sweep_hi, 0x484D); it is accepted with
+// min(1, |psi(s')|^2 n(s) / (|psi(s)|^2 n(s'))), n = number of used
+// connections, against word 2 of the same counter.
+__global__ void mh_ham_propose_kernel(const int8_t* __restrict__ chains, const short2* __restrict__ flips,
+                                      const uint8_t* __restrict__ use, int n_slots, int64_t n_chains, int n,
+                                      uint32_t k0, uint32_t k1, uint64_t sweep, int8_t* __restrict__ cand,
+                                      int32_t* __restrict__ n_conn) {
+  int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n_chains) return;
+  int cnt = 0;
+  for (int q = 0; q < n_slots; ++q) cnt += use[(int64_t)q * n_chains + c] != 0;
+  U4 x = philox4x32(U4{(uint32_t)c, (uint32_t)sweep, (uint32_t)(sweep >> 32), 0x484Du}, k0, k1);
+  int f0 = -1, f1 = -1;
+  if (cnt > 0) {
+    int k = (int)(philox_uniform(x.x) * (float)cnt);
+    if (k >= cnt) k = cnt - 1;
+    for (int q = 0; q < n_slots; ++q) {
+      if (!use[(int64_t)q * n_chains + c]) continue;
+      if (k-- == 0) {
+        short2 f = flips[(int64_t)q * n_chains + c];
+        f0 = f.x;
+        f1 = f.y;
+        break;
+      }
+    }
+  }
+  for (int i = 0; i < n; ++i) {
+    int8_t v = chains[c * n + i];
+    cand[c * n + i] = (i == f0 || i == f1) ? (int8_t)-v : v;
+  }
+  n_conn[c] = cnt > 0 ? cnt : 1;
+}
+
+__global__ void mh_ham_accept_kernel(int8_t* __restrict__ chains, float2* __restrict__ lp_chain,
+                                     const int8_t* __restrict__ cand, const float2* __restrict__ lp_cand,
+                                     const int32_t* __restrict__ n_conn, const uint8_t* __restrict__ use_cand,
+                                     int n_slots, int64_t n_chains, int n, uint32_t k0, uint32_t k1, uint64_t sweep,
+                                     unsigned long long* accepted) {
+  int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n_chains) return;
+  int nc = 0;
+  for (int q = 0; q < n_slots; ++q) nc += use_cand[(int64_t)q * n_chains + c] != 0;
+  if (nc == 0) nc = 1;
+  U4 x = philox4x32(U4{(uint32_t)c, (uint32_t)sweep, (uint32_t)(sweep >> 32), 0x484Du}, k0, k1);
+  const float u = philox_uniform(x.z);
+  const float d = 2.f * (lp_cand[c].x - lp_chain[c].x) + logf((float)n_conn[c] / (float)nc);
+  if (d >= 0.f || expf(d) > u) {
+    for (int i = 0; i < n; ++i) chains[c * n + i] = cand[c * n + i];
+    lp_chain[c] = lp_cand[c];
+    if (accepted) atomicAdd(accepted, 1ull);
+  }
+}
+
 }  // namespace fk
 
 using namespace fk;
@@ -397,6 +453,32 @@ int fk_mh_independent_step(int8_t* chains, float* lp_chain, float* lq_chain, con
       chains, reinterpret_cast<float2*>(lp_chain), reinterpret_cast<float2*>(lq_chain), candidates,
       reinterpret_cast<const float2*>(lp_cand), reinterpret_cast<const float2*>(lq_cand), n_chains, n_visible,
       (uint32_t)seed, (uint32_t)(seed >> 32), step, accepted);
+  FK_CUDA(launched());
+  return FK_OK;
+}
+
+int fk_mh_hamiltonian_propose(const int8_t* chains, const int16_t* flips, const uint8_t* use, int32_t n_slots,
+                              int64_t n_chains, int32_t n_sites, uint64_t seed, uint64_t sweep, int8_t* candidates,
+                              int32_t* n_conn, void* stream) {
+  FK_CHECK_ARG(chains && flips && use && candidates && n_conn && n_slots > 0 && n_chains > 0 && n_sites > 0,
+               "fk_mh_hamiltonian_propose: bad arguments");
+  mh_ham_propose_kernel<<<(unsigned)((n_chains + 127) / 128), 128, 0, static_cast<cudaStream_t>(stream)>>>(
+      chains, reinterpret_cast<const short2*>(flips), use, n_slots, n_chains, n_sites, (uint32_t)seed,
+      (uint32_t)(seed >> 32), sweep, candidates, n_conn);
+  FK_CUDA(launched());
+  return FK_OK;
+}
+
+int fk_mh_hamiltonian_accept(int8_t* chains, float* lp_chain, const int8_t* candidates, const float* lp_cand,
+                             const int32_t* n_conn, const uint8_t* use_cand, int32_t n_slots, int64_t n_chains,
+                             int32_t n_sites, uint64_t seed, uint64_t sweep, unsigned long long* accepted,
+                             void* stream) {
+  FK_CHECK_ARG(chains && lp_chain && candidates && lp_cand && n_conn && use_cand && n_slots > 0 && n_chains > 0 &&
+                   n_sites > 0,
+               "fk_mh_hamiltonian_accept: bad arguments");
+  mh_ham_accept_kernel<<<(unsigned)((n_chains + 127) / 128), 128, 0, static_cast<cudaStream_t>(stream)>>>(
+      chains, reinterpret_cast<float2*>(lp_chain), candidates, reinterpret_cast<const float2*>(lp_cand), n_conn,
+      use_cand, n_slots, n_chains, n_sites, (uint32_t)seed, (uint32_t)(seed >> 32), sweep, accepted);
   FK_CUDA(launched());
   return FK_OK;
 }

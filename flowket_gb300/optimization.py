@@ -71,9 +71,14 @@ class VariationalMonteCarlo(MiniBatchGenerator):
 
     def _sample(self):
         out = self.sampler.sample()
-        if isinstance(out, tuple):
-            return out
-        return out, None, None
+        if not isinstance(out, tuple):
+            return out, None, None
+        if getattr(self.sampler, "machine", self.model) is not self.model:
+            # drawn from another machine (the base of a symmetrised ensemble,
+            # experiments/run_evaluation.py:12-24): log psi and the local
+            # energy's connected configurations come from the model itself
+            return out[0], None, None
+        return out
 
     def _local_energy(self, spins, log_psi, saved=None):
         if saved is not None:
@@ -126,3 +131,82 @@ class VariationalMonteCarlo(MiniBatchGenerator):
         self.current_local_energy_variance = st[2]
         self.current_local_energy = torch.complex(self._local[:, 0], self._local[:, 1])
         return self.times
+
+
+class ExactVariational:
+    """Exact-enumeration driver (optimization/exact_variational.py:96-155).
+
+    All 2^N configurations (site i = bit i of the index, bit 1 -> +1, as
+    exact/utils.py:48-57) are evaluated on the GPU, |psi|^2 is normalised
+    over them (exact_variational.py:124-130, FP64 log-sum-exp), E_loc is
+    computed for every configuration (the connected configurations reuse
+    the base activations), E = sum_s p_s E_loc(s) and
+    var = sum_s p_s (Re E_loc(s) - Re E)^2 in FP64
+    (exact_variational.py:91-95), and the loss coefficients are
+    y_s = p_s conj(E_loc(s) - E) (exact_variational.py:132-135).
+
+    ``step(optimizer)`` takes one optimizer step per enumeration with the
+    exact energy gradient 2 Re sum_s y_s dlogpsi_s, i.e. the reference's
+    generator with ``batch_size`` = 2^N without Keras' division by the
+    mini-batch size (a constant factor). ``to_generator()`` yields
+    (configurations, y) batches of ``batch_size`` as the reference's does.
+    Sampling-free: for lattices up to ~24 sites."""
+
+    def __init__(self, model, operator, batch_size=None):
+        h, w = model.hilbert_state_shape
+        n = h * w
+        if n > 24:
+            raise ValueError("ExactVariational enumerates 2^N configurations; N <= 24")
+        self.model = model
+        self.operator = operator
+        self.num_of_states = 1 << n
+        bs = self.num_of_states if batch_size is None else min(int(batch_size), self.num_of_states)
+        if self.num_of_states % bs != 0:
+            raise ValueError("In exact the batch size must divide the total number of states in the system")
+        self.batch_size = bs
+        idx = torch.arange(self.num_of_states, device=model.device, dtype=torch.int64)
+        bits = (idx[:, None] >> torch.arange(n, device=model.device, dtype=torch.int64)[None, :]) & 1
+        self.states = (2 * bits - 1).to(torch.int8).view(-1, h, w)
+        self.energy_observable = Observable(operator)
+        self.probs = None
+        self.current_energy = None
+        self.current_local_energy = None
+        self.current_local_energy_variance = None
+        self._w = None
+        self._saved = None
+
+    def machine_updated(self):
+        """wave function, probabilities, local energies, energy and coefficients."""
+        lp, _, saved = self.model.forward(self.states, mode=_lib.FK_AR2D_SAVE)
+        local = self.energy_observable.local_values(self.model, self.states, log_psi=lp, base_saved=saved)
+        lr2 = 2.0 * lp[:, 0].double()
+        p = torch.exp(lr2 - torch.logsumexp(lr2, 0))
+        e = (p[:, None] * local).sum(0)
+        d_re = local[:, 0] - e[0]
+        d_im = local[:, 1] - e[1]
+        self.probs = p
+        self.current_local_energy = torch.complex(local[:, 0], local[:, 1])
+        self.current_energy = complex(e[0].item(), e[1].item())
+        self.current_local_energy_variance = float((p * d_re * d_re).sum().item())
+        self.y = torch.complex(p * d_re, -p * d_im)
+        # adjoint seeds of 2 Re(logpsi y): (d/dRe logpsi, d/dIm logpsi)
+        self._w = torch.stack((2.0 * p * d_re, 2.0 * p * d_im), dim=1).float().contiguous()
+        self._saved = saved
+        return self.current_energy
+
+    def step(self, optimizer):
+        self.machine_updated()
+        if hasattr(optimizer, "update"):
+            raise ValueError("ExactVariational takes gradient optimizers (the SR Gram is sample-space)")
+        grad = self.model.backward(self.states, self._w, self._saved)
+        optimizer.apply_gradient(grad)
+        return self.current_energy
+
+    def to_generator(self):
+        while True:
+            self.machine_updated()
+            for i in range(0, self.num_of_states, self.batch_size):
+                yield self.states[i:i + self.batch_size], self.y[i:i + self.batch_size]
+
+    def __iter__(self):
+        return self.to_generator()

@@ -107,3 +107,74 @@ class ComplexValuesStochasticReconfiguration:
                   _lib.ptr(x), st)
         self.lr = lr
         return x
+
+
+class AccumulateGradientOptimizer:
+    """optimizers/accumulate_gradient_optimizer.py:13-88: gradients of
+    ``update_params_frequency`` consecutive steps are summed (or averaged:
+    each divided by the frequency) in a device buffer and applied by the
+    wrapped optimiser on every ``update_params_frequency``-th call, which
+    then clears the buffer. With ``ema_decay`` > 0 an exponential moving
+    average of the parameters after each applied update is kept;
+    ``set_weights_ema`` loads its bias-corrected value
+    (ema / (1 - decay^updates)). One GPU per process: there is no Horovod
+    allreduce (replicas only)."""
+
+    def __init__(self, optimizer, update_params_frequency, accumulate_sum_or_mean=True, ema_decay=0,
+                 use_horovod=False):
+        if update_params_frequency < 1:
+            raise ValueError("update_params_frequency must be >= 1")
+        if use_horovod:
+            raise ValueError("no Horovod allreduce: one process per GPU runs independent replicas")
+        self.optimizer = optimizer
+        self.machine = optimizer.machine
+        self.update_params_frequency = int(update_params_frequency)
+        self.accumulate_sum = bool(accumulate_sum_or_mean)
+        self.ema_decay = float(ema_decay)
+        self.accumulated_iterations = 0
+        self.total_iterations = 0
+        self.accumulated_gradient = torch.zeros_like(self.machine.params)
+        self.params_ema = torch.zeros_like(self.machine.params) if self.ema_decay > 0 else None
+
+    def set_update_params_frequency(self, update_params_frequency):
+        self.update_params_frequency = int(update_params_frequency)
+
+    def apply_gradient(self, grad):
+        if self.accumulate_sum:
+            self.accumulated_gradient.add_(grad)
+        else:
+            self.accumulated_gradient.add_(grad, alpha=1.0 / self.update_params_frequency)
+        self.accumulated_iterations += 1
+        if self.accumulated_iterations % self.update_params_frequency != 0:
+            return
+        self.optimizer.apply_gradient(self.accumulated_gradient)
+        self.accumulated_gradient.zero_()
+        if self.params_ema is not None:
+            self.total_iterations += 1
+            self.params_ema.mul_(self.ema_decay).add_(self.machine.params, alpha=1.0 - self.ema_decay)
+
+    def set_weights_ema(self):
+        if self.params_ema is None or self.total_iterations == 0:
+            return
+        self.machine.params.copy_(self.params_ema / (1.0 - self.ema_decay ** self.total_iterations))
+        self.machine.params_updated()
+
+    def state_dict(self):
+        return {"optimizer": self.optimizer.state_dict(), "accumulated_gradient": self.accumulated_gradient,
+                "accumulated_iterations": self.accumulated_iterations, "total_iterations": self.total_iterations,
+                "params_ema": self.params_ema}
+
+    def load_state_dict(self, state):
+        self.optimizer.load_state_dict(state["optimizer"])
+        self.accumulated_gradient.copy_(state["accumulated_gradient"])
+        self.accumulated_iterations = int(state["accumulated_iterations"])
+        self.total_iterations = int(state["total_iterations"])
+        if self.params_ema is not None and state["params_ema"] is not None:
+            self.params_ema.copy_(state["params_ema"])
+
+
+def convert_to_accumulate_gradient_optimizer(orig_optimizer, update_params_frequency, accumulate_sum_or_mean=True,
+                                             ema_decay=0, use_horovod=False):
+    """accumulate_gradient_optimizer.py:13: the wrapped optimiser."""
+    return AccumulateGradientOptimizer(orig_optimizer, update_params_frequency, accumulate_sum_or_mean, ema_decay,
+                                       use_horovod)

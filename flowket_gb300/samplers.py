@@ -183,6 +183,89 @@ class MetropolisHastingsExchange(MetropolisHastingsSampler):
     kind = 1
 
 
+class MetropolisHastingsHamiltonian(Sampler):
+    """metropolis_hastings.py:170-195: each sweep proposes, per chain, one of
+    the operator's used connections of the current configuration (uniformly,
+    slot 0 included when used) and accepts it with
+    min(1, |psi(s')|^2 n(s) / (|psi(s)|^2 n(s'))), n = number of used
+    connections. Chains start from ``hamiltonian.random_states`` (the
+    total_sz sector when the operator has one). The warm-up and thinning
+    schedule is the one of the other Metropolis-Hastings samplers. One sweep =
+    enumeration of the chains' connections, the propose kernel, enumeration of
+    the candidates' connections, the machine's log psi of the candidates and
+    the accept kernel. Works with RBM and ConvNetAutoregressive2D machines."""
+
+    def __init__(self, machine, batch_size, hamiltonian, num_of_chains=1, unused_sampels=0, discard_ratio=10,
+                 seed=4321, mini_batch_size=None):
+        super().__init__(machine.hilbert_state_shape, batch_size, mini_batch_size)
+        if batch_size % num_of_chains != 0:
+            raise ValueError("Num of samplers must divide the batch size")
+        self.machine = machine
+        self.hamiltonian = hamiltonian
+        self.num_of_chains = int(num_of_chains)
+        self.unused_sampels = int(unused_sampels)
+        self.discard_ratio = int(discard_ratio)
+        self.seed = int(seed)
+        self.sweep = 0
+        self.n_sites = int(np.prod(machine.hilbert_state_shape))
+        gen = torch.Generator().manual_seed(self.seed)
+        init = hamiltonian.random_states(self.num_of_chains, generator=gen)
+        self.sample = torch.as_tensor(init).to(device=machine.device, dtype=torch.int8).reshape(
+            self.num_of_chains, self.n_sites).contiguous()
+        self.lp = self._log_psi(self.sample)
+        self.cand = torch.empty_like(self.sample)
+        self.n_conn = torch.empty(self.num_of_chains, dtype=torch.int32, device=machine.device)
+        self.accepted = torch.zeros(1, dtype=torch.int64, device=machine.device)
+        self.acceptance_ratio = 1.0
+
+    def _log_psi(self, x):
+        m = self.machine
+        if hasattr(m, "log_psi_pairs"):
+            return m.log_psi_pairs(x).contiguous()
+        lp, _, _ = m.forward(x.view((-1,) + tuple(m.hilbert_state_shape)))
+        return lp.contiguous()
+
+    def _sweep(self, accepted):
+        op = self.hamiltonian
+        flips, _, use, _ = op.enumerate(self.sample)
+        n_slots = use.shape[0]
+        _lib.call("fk_mh_hamiltonian_propose", _lib.ptr(self.sample), _lib.ptr(flips), _lib.ptr(use), n_slots,
+                  self.num_of_chains, self.n_sites, self.seed, self.sweep, _lib.ptr(self.cand),
+                  _lib.ptr(self.n_conn), _lib.stream_ptr())
+        _, _, use_c, _ = op.enumerate(self.cand)
+        lp_c = self._log_psi(self.cand)
+        _lib.call("fk_mh_hamiltonian_accept", _lib.ptr(self.sample), _lib.ptr(self.lp), _lib.ptr(self.cand),
+                  _lib.ptr(lp_c), _lib.ptr(self.n_conn), _lib.ptr(use_c), n_slots, self.num_of_chains, self.n_sites,
+                  self.seed, self.sweep, _lib.ptr(accepted) if accepted is not None else None,
+                  _lib.stream_ptr())
+        self.sweep += 1
+
+    def __next__(self):
+        spc = self.batch_size // self.num_of_chains
+        warm = (spc // self.discard_ratio) * self.unused_sampels if self.discard_ratio > 0 else 0
+        out = torch.empty((self.num_of_chains, spc, self.n_sites), dtype=torch.int8, device=self.machine.device)
+        self.accepted.zero_()
+        for _ in range(warm):
+            self._sweep(None)
+        for i in range(spc):
+            for _ in range(self.unused_sampels + 1):
+                self._sweep(self.accepted)
+            out[:, i].copy_(self.sample)
+        self._accepted_pending = (self.accepted, self.batch_size * (self.unused_sampels + 1))
+        return out.view((self.batch_size,) + tuple(self.input_size))
+
+    def sample_with_log_psi(self):
+        return self.__next__(), None, None
+
+    def update_acceptance_ratio(self):
+        acc, total = self._accepted_pending
+        self.acceptance_ratio = int(acc.item()) / total
+        return self.acceptance_ratio
+
+    def calc_r_hat_value(self, estimated_values):
+        return r_hat_and_correlations(estimated_values, self.num_of_chains)
+
+
 class MetropolisHastingsIndependent(Sampler):
     """Independent Metropolis-Hastings with a learned autoregressive proposal.
 

@@ -194,6 +194,25 @@ int fk_mh_independent_step(int8_t* chains, float* lp_chain, float* lq_chain, con
                            const float* lp_cand, const float* lq_cand, int64_t n_chains, int32_t n_visible,
                            uint64_t seed, uint64_t step, unsigned long long* accepted, void* stream);
 
+/* Hamiltonian-proposal Metropolis-Hastings (MetropolisHastingsHamiltonian,
+ * samplers/metropolis_hastings.py:170-195), one sweep as propose -> the
+ * caller enumerates the candidates' connections and evaluates their log psi
+ * -> accept. Propose: the candidate of chain c is its used connection number
+ * floor(U * n(c)) (find_conn slot order; flips/use as fk_find_conn_* give them,
+ * [n_slots][n_chains]); n_conn[c] = n(c), the chain's number of used
+ * connections. Accept: min(1, |psi(s')|^2 n(s) / (|psi(s)|^2 n(s'))), with
+ * use_cand the candidates' use flags; accepted chains take the candidate and
+ * its log psi; `accepted` (may be NULL) counts acceptances. Both draw from
+ * the Philox counter (chain, sweep_lo, sweep_hi, 0x484D): word 0 proposes,
+ * word 2 accepts. */
+int fk_mh_hamiltonian_propose(const int8_t* chains, const int16_t* flips, const uint8_t* use, int32_t n_slots,
+                              int64_t n_chains, int32_t n_sites, uint64_t seed, uint64_t sweep, int8_t* candidates,
+                              int32_t* n_conn, void* stream);
+int fk_mh_hamiltonian_accept(int8_t* chains, float* lp_chain, const int8_t* candidates, const float* lp_cand,
+                             const int32_t* n_conn, const uint8_t* use_cand, int32_t n_slots, int64_t n_chains,
+                             int32_t n_sites, uint64_t seed, uint64_t sweep, unsigned long long* accepted,
+                             void* stream);
+
 /* ------------------------------------------------------------------ SR (kernel d)
  * Sample-space stochastic reconfiguration
  * (optimizers/stochastic_reconfiguration/optimizer.py:33-124): per-sample

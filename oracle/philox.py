@@ -68,3 +68,12 @@ def mh_words(seed, chain, sweep):
     sweep = int(sweep)
     return philox4x32(np.asarray(chain, dtype=np.uint32), np.uint32(sweep & 0xFFFFFFFF),
                       np.uint32(sweep >> 32), np.uint32(0x4D48), k0, k1)
+
+
+def ham_words(seed, chain, sweep):
+    """Four words for (chain, sweep) of a Hamiltonian-proposal
+    Metropolis-Hastings run: counter (chain, sweep_lo, sweep_hi, 0x484D)."""
+    k0, k1 = seed_key(seed)
+    sweep = int(sweep)
+    return philox4x32(np.asarray(chain, dtype=np.uint32), np.uint32(sweep & 0xFFFFFFFF),
+                      np.uint32(sweep >> 32), np.uint32(0x484D), k0, k1)

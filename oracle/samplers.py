@@ -7,6 +7,8 @@
 * ``metropolis_hastings`` restates samplers/metropolis_hastings.py:15-145
   (Local and Exchange proposals, exp(min(2 dRe log psi, 0)) > U acceptance,
   warm-up and thinning schedule of :46-65).
+* ``metropolis_hastings_hamiltonian`` restates metropolis_hastings.py:170-195
+  (connections of the operator as proposals, with the n(s)/n(s') factor).
 * ``r_hat_and_correlations`` restates metropolis_hastings.py:8-12,67-89.
 Test infrastructure only.
 """
@@ -92,6 +94,58 @@ def metropolis_hastings(log_psi_fn, init_chains, kind, samples_per_chain, unused
         out[:, i] = chains
     ratio = accepted / (n_chains * samples_per_chain * (unused_samples + 1))
     return out.reshape((-1,) + shape), ratio, sweep - sweep_offset
+
+
+def metropolis_hastings_hamiltonian(log_psi_fn, find_conn, init_chains, samples_per_chain, unused_samples,
+                                    discard_ratio, seed, sweep_offset=0):
+    """samplers/metropolis_hastings.py:170-195: the candidate is a uniformly
+    chosen used connection of find_conn (index floor(U * n) in slot order, U
+    from word 0 of the Philox counter (chain, sweep, 0x484D), the product
+    rounded to float32 as the GPU forms it); acceptance
+    exp(2 dRe log psi + log(n(s) / n(s'))) > U with word 2. Schedule as
+    ``metropolis_hastings``. Returns (batch chain-major, acceptance ratio)."""
+    chains = np.array(init_chains, dtype=np.float64)
+    shape = chains.shape[1:]
+    n_chains = chains.shape[0]
+    lp = np.real(log_psi_fn(chains))
+    sweep = sweep_offset
+    accepted = 0
+    idx = np.arange(n_chains)
+
+    def one_sweep():
+        nonlocal chains, lp, sweep
+        words = philox.ham_words(seed, idx, sweep)
+        conn, _, use = find_conn(chains)
+        use = np.asarray(use, dtype=bool)
+        n_s = np.maximum(use.sum(axis=0), 1)
+        u0 = philox.to_uniform(words[0]).astype(np.float32)
+        k = np.floor(u0 * n_s.astype(np.float32)).astype(np.int64)
+        k = np.minimum(k, n_s - 1)
+        cand = chains.copy()
+        for c in range(n_chains):
+            slots = np.nonzero(use[:, c])[0]
+            if slots.size:
+                cand[c] = conn[slots[k[c]], c]
+        _, _, use_c = find_conn(cand)
+        n_c = np.maximum(np.asarray(use_c, dtype=bool).sum(axis=0), 1)
+        lpc = np.real(log_psi_fn(cand))
+        d = 2.0 * (lpc - lp) + np.log(n_s / n_c)
+        a = (d >= 0) | (np.exp(np.minimum(d, 0.0)) > philox.to_uniform(words[2]))
+        chains[a] = cand[a]
+        lp[a] = lpc[a]
+        sweep += 1
+        return int(a.sum())
+
+    if discard_ratio > 0:
+        for _ in range((samples_per_chain // discard_ratio) * unused_samples):
+            one_sweep()
+    out = np.empty((n_chains, samples_per_chain) + shape)
+    for i in range(samples_per_chain):
+        for _ in range(unused_samples + 1):
+            accepted += one_sweep()
+        out[:, i] = chains
+    ratio = accepted / (n_chains * samples_per_chain * (unused_samples + 1))
+    return out.reshape((-1,) + shape), ratio
 
 
 def sum_correlations(corr):

@@ -117,3 +117,45 @@ def test_independent_proposal_keeps_target_and_gains_over_local_moves(cuda):
     y = np.bincount(exact.states_to_index(ref), minlength=4096)
     z = ((np.square(x - y) - x - y) / (x + y + 1e-20)).sum()
     assert z <= 3 * np.sqrt(got.shape[0]) * max(1.0, tau_ind), z
+
+
+def test_mh_hamiltonian_reproduces_oracle_chains(cuda):
+    """MetropolisHastingsHamiltonian (metropolis_hastings.py:170-195) against the
+    oracle's chains from the same Philox words."""
+    from flowket_gb300.operators import Heisenberg
+    from flowket_gb300.samplers import MetropolisHastingsHamiltonian
+    m, p = _rbm((10,), 2, 0.3, seed=3)
+    op = Heisenberg(hilbert_state_shape=(10,), pbc=True)
+    sampler = MetropolisHastingsHamiltonian(m, 64 * 8, op, num_of_chains=64, unused_sampels=3, discard_ratio=2,
+                                            seed=23)
+    init = sampler.sample.cpu().numpy().astype(np.float64)
+    assert np.all(init.sum(axis=1) == 0)  # random_states of the total_sz = 0 sector
+    got = next(sampler).cpu().numpy()
+    want, ratio = ref_samplers.metropolis_hastings_hamiltonian(
+        lambda x: ref_rbm.rbm_log_psi(p, x), lambda s: ref_ops.heisenberg_find_conn(s, pbc=True), init, 8, 3, 2,
+        seed=23)
+    agree = np.mean(np.all(got == want.astype(np.int8), axis=1))
+    assert agree > 0.97, agree
+    assert sampler.update_acceptance_ratio() == pytest.approx(ratio, abs=0.02)
+    assert np.all(got.sum(axis=1) == 0)  # exchange moves keep the sector
+
+
+def test_mh_hamiltonian_matches_exact_distribution(cuda):
+    """The chains sample |psi|^2 restricted to the Sz = 0 sector they move in."""
+    from flowket_gb300.operators import Heisenberg
+    from flowket_gb300.samplers import MetropolisHastingsHamiltonian
+    m, p = _rbm((8,), 2, 0.15, seed=4)
+    op = Heisenberg(hilbert_state_shape=(8,), pbc=True)
+    n = 128 * 128
+    sampler = MetropolisHastingsHamiltonian(m, n, op, num_of_chains=128, unused_sampels=8, discard_ratio=4, seed=6)
+    got = next(sampler).cpu().numpy()
+    states = exact.all_states((8,))
+    sector = states.sum(axis=1) == 0
+    probs, _ = exact.exact_distribution(ref_rbm.rbm_log_psi(p, states))
+    probs = np.where(sector, probs, 0.0)
+    probs = probs / probs.sum()
+    ref = exact.exact_sample(probs, (8,), n, np.random.default_rng(0))
+    x = np.bincount(exact.states_to_index(got), minlength=256)
+    y = np.bincount(exact.states_to_index(ref), minlength=256)
+    z = ((np.square(x - y) - x - y) / (x + y + 1e-20)).sum()
+    assert z <= 2 * np.sqrt(n), z
