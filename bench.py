@@ -54,7 +54,7 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--fp32-steps", type=int, default=2)
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--case", default="vmc", choices=["vmc", "forward", "energy4x4"],
+    p.add_argument("--case", default="vmc", choices=["vmc", "forward", "energy4x4", "vmc16"],
                    help="forward: only the batched AR2D forward of the local-energy stage on --configs "
                         "connected configurations (the small case used for ncu captures); energy4x4: train "
                         "the 4x4 Heisenberg model (depth 5, 16 channels) and compare its exact energy "
@@ -63,6 +63,7 @@ def parse():
     p.add_argument("--train-steps", type=int, default=24000)
     p.add_argument("--train-batch", type=int, default=2048)
     p.add_argument("--configs", type=int, default=32768)
+    p.add_argument("--batch", type=int, default=8192)
     return p.parse_args()
 
 
@@ -86,6 +87,42 @@ def forward_case(args):
     fl = flops_per_sample_forward(SHAPE, DEPTH, CHANNELS) * args.configs
     print(json.dumps({"case": "forward", "configs": args.configs, "ms_per_forward": ms,
                       "tflops": fl / (ms / 1e3) / 1e12}), flush=True)
+
+
+def vmc16_case(args):
+    """Heisenberg 16x16 PBC (Marshall sign), ConvNetAutoregressive2D depth 20,
+    64 channels (weight norm), `--batch` samples per step: full VMC steps
+    (exact sampling, local energy over the connected configurations with
+    causal reuse, adjoint gradient, Adam) of the BF16 path and of the plain
+    FP32 path of the same code, each after one warm-up step, CUDA-event
+    timed. Both start from the same seeded parameters."""
+    from flowket_gb300.machines import ConvNetAutoregressive2D
+    from flowket_gb300.operators import Heisenberg
+    from flowket_gb300.optimization import VariationalMonteCarlo
+    from flowket_gb300.optimizers import Adam
+    from flowket_gb300.samplers import FastAutoregressiveSampler
+    shape = (16, 16)
+    out = {"case": "vmc16", "workload": "Heisenberg 16x16 PBC, Marshall sign; ConvNetAutoregressive2D depth 20 F64 "
+                                        "(weight norm); full VMC step with Adam", "batch": args.batch}
+    for prec in ("bf16", "fp32"):
+        m = ConvNetAutoregressive2D(shape, 20, 64, weights_normalization=True, precision=prec, seed=0)
+        vmc = VariationalMonteCarlo(m, Heisenberg(hilbert_state_shape=shape, pbc=True),
+                                    FastAutoregressiveSampler(m, args.batch, seed=1234))
+        opt = Adam(m, lr=1e-3)
+        vmc.step(opt)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        steps = max(1, args.steps if prec == "bf16" else args.fp32_steps)
+        torch.cuda.synchronize()
+        a.record()
+        for _ in range(steps):
+            vmc.step(opt)
+        b.record()
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / steps
+        out[prec] = {"ms_per_step": ms, "samples_per_s": args.batch / (ms / 1e3), "steps": steps,
+                     "stage_ms": vmc.times, "energy": vmc.current_energy.real}
+    out["bf16_over_fp32"] = out["fp32"]["ms_per_step"] / out["bf16"]["ms_per_step"]
+    print(json.dumps(out), flush=True)
 
 
 # FP64 Lanczos ground-state energy of the 4x4 periodic Heisenberg operator
@@ -422,6 +459,8 @@ def main():
         forward_case(args)
     elif args.case == "energy4x4":
         energy4x4_case(args)
+    elif args.case == "vmc16":
+        vmc16_case(args)
     elif args.impl == "reference":
         reference_arm(args, rank, world)
     else:
