@@ -23,7 +23,7 @@ c_i32, c_i64, c_u64, c_f32, c_f64, c_p = (ctypes.c_int32, ctypes.c_int64, ctypes
 
 class Ar2dDesc(ctypes.Structure):
     _fields_ = [("height", c_i32), ("width", c_i32), ("depth", c_i32), ("channels", c_i32),
-                ("weights_normalization", c_i32), ("precision", c_i32)]
+                ("weights_normalization", c_i32), ("precision", c_i32), ("equal_up_down_spins", c_i32)]
 
 
 class RbmDesc(ctypes.Structure):

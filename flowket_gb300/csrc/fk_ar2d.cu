@@ -52,6 +52,7 @@ int build_layout(const fk_ar2d_desc* d, NetLayout* L) {
   L->F = d->channels;
   L->wn = d->weights_normalization ? 1 : 0;
   L->precision = d->precision;
+  L->updown = d->equal_up_down_spins ? 1 : 0;
   L->n_cc = 2 * d->depth - 2;
   const int F = L->F;
   int64_t p = 0, w = 0;
@@ -142,6 +143,7 @@ int64_t workspace_layout(const NetLayout& L, int64_t batch, int mode, char* base
     }
   }
   t->row_partial = static_cast<float2*>(take(tiles * L.H * kTile * sizeof(float2)));
+  if (L.updown) t->updown = static_cast<uint8_t*>(take(tiles * kTile * (int64_t)L.P));
   t->bytes = off;
   return off;
 }
@@ -532,12 +534,31 @@ struct HeadOut {
   float re0, re1, im0, im1;
 };
 
-__device__ __forceinline__ HeadOut normalise_head(const float* l) {
+// `mask` bit k: outcome k is masked by EqualUpDownSpins (layers/spins_invariants.py:13-22):
+// its real part becomes -inf (LOG_ZERO in float32) before the normalisation, so
+// the other outcome normalises to exactly 0.
+__device__ __forceinline__ HeadOut normalise_head(const float* l, int mask = 0) {
   // abstract_machine.py:56-57, autoregressive.py:7-15 (norm_type 2)
-  float a = 2.f * l[0], b = 2.f * l[1];
+  const float l0 = (mask & 1) ? -INFINITY : l[0], l1 = (mask & 2) ? -INFINITY : l[1];
+  float a = 2.f * l0, b = 2.f * l1;
   float mx = fmaxf(a, b);
   float lse = 0.5f * (mx + logf(expf(a - mx) + expf(b - mx)));
-  return HeadOut{l[0] - lse, l[1] - lse, l[2], l[3]};
+  return HeadOut{l0 - lse, l1 - lse, l[2], l[3]};
+}
+
+// EqualUpDownSpins mask bits of every (sample, site): bit 0 when at least N/2
+// earlier sites (raster order) hold +1, bit 1 when at least N/2 hold -1.
+__global__ void updown_mask_kernel(const int8_t* __restrict__ spins, int64_t batch, int P, uint8_t* __restrict__ out) {
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= batch) return;
+  int up = 0, down = 0;
+  for (int k = 0; k < P; ++k) {
+    out[b * P + k] = (uint8_t)((2 * up >= P ? 1 : 0) | (2 * down >= P ? 2 : 0));
+    if (spins[b * P + k] > 0)
+      ++up;
+    else
+      ++down;
+  }
 }
 
 template <int F, bool TC>
@@ -577,7 +598,7 @@ struct Engine<F, true> {
 // output in *head (valid for every thread).
 template <int F, bool TC, typename T>
 __device__ void run_op(const OpArgs& a, Engine<F, TC>& eng, int64_t tile, int r, int c, int H, int W, int P,
-                       HeadOut* head) {
+                       HeadOut* head, int head_mask = -1) {
   const int m = threadIdx.x;
   float acc[F];
   eng.main(a, tile, m, r, c, H, W, P, acc);
@@ -655,7 +676,11 @@ __device__ void run_op(const OpArgs& a, Engine<F, TC>& eng, int64_t tile, int r,
       if (eng.aborted()) return;
 #pragma unroll
       for (int n = 0; n < 4; ++n) l[n] += __ldg(bc + n);
-      *head = normalise_head(l);
+      if (head_mask < 0) {
+        const int64_t sample = tile * kTile + m;
+        head_mask = (a.updown && sample < a.batch) ? a.updown[sample * P + pix] : 0;
+      }
+      *head = normalise_head(l, head_mask);
     }
   }
   eng.end();
@@ -1056,6 +1081,10 @@ static int forward_impl(const NetLayout& L, const void* packed, const int8_t* sp
                         float* log_psi, float* cond, const Tensors& T, int mode, cudaStream_t s) {
   int64_t tiles = (batch + kTile - 1) / kTile;
   int* err = device_error_word();
+  if (L.updown) {
+    updown_mask_kernel<<<(unsigned)((batch + 127) / 128), 128, 0, s>>>(spins, batch, L.P, T.updown);
+    FK_CUDA(launched());
+  }
   for (int i = 0; i < L.n_cc; ++i) {
     CCTensors x = cc_tensors(L, T, mode, i);
     OpArgs ops[3];
@@ -1063,6 +1092,7 @@ static int forward_impl(const NetLayout& L, const void* packed, const int8_t* sp
     if (i == L.n_cc - 1) {
       ops[2].row_partial = T.row_partial;
       ops[2].cond = cond;
+      ops[2].updown = T.updown;
     }
     for (int k = 0; k < 3; ++k) {
       int st;
@@ -1416,7 +1446,8 @@ __device__ bool site_chain(TcSmem& s, TcState& st, uint32_t cw, const float* in,
 // residual of the C op two convs later. site_end: last op of the site.
 template <int F>
 __device__ bool site_op(const SampOp& a, TcSmem& s, TcState& st, SiteBufs& b, int64_t tile, int r, int c, int H,
-                        int W, const SampOp* nx, int nc, bool keep_res, bool site_end, HeadOut* head) {
+                        int W, const SampOp* nx, int nc, bool keep_res, bool site_end, HeadOut* head,
+                        int head_mask) {
   using SC = SiteCfg<F>;
   using T = __nv_bfloat16;
   constexpr int F2 = F / 2;
@@ -1521,7 +1552,7 @@ __device__ bool site_op(const SampOp& a, TcSmem& s, TcState& st, SiteBufs& b, in
       if (!site_chain<F, 16>(s, st, s.cw, acc, l)) return false;
 #pragma unroll
       for (int n = 0; n < 4; ++n) l[n] += __ldg(bc + n);
-      *head = normalise_head(l);
+      *head = normalise_head(l, head_mask);
     }
   }
   if (site_end)
@@ -1542,6 +1573,7 @@ struct SampleArgs {
   int8_t* spins;
   float2* row_partial;
   uint64_t keep_res;  // bit i: the C output of causal conv i is the residual of conv i + 2
+  int updown;         // EqualUpDownSpins mask from the running counts of drawn spins
 };
 
 template <int F, bool TC>
@@ -1621,6 +1653,8 @@ __global__ void __launch_bounds__(128) sample_kernel(const __grid_constant__ Sam
   auto seq_op = [&](int k) -> const SampOp& {
     return k == 0 ? ops[3 * last + 2] : (k == nseq - 1 ? ops[3 * last + 1] : ops[3 * ((k - 1) / 2) + ((k & 1) ? 1 : 2)]);
   };
+  // EqualUpDownSpins: +1 spins drawn so far and the mask of the next site
+  int n_up = 0, hmask = 0;
   for (int r = 0; r < H && !eng.aborted(); ++r) {
     Kahan kre, kim;
     for (int c = 0; c < W && kSite; ++c) {
@@ -1632,7 +1666,7 @@ __global__ void __launch_bounds__(128) sample_kernel(const __grid_constant__ Sam
           const bool keep = k >= 2 && (k & 1) == 0 && ((a.keep_res >> ((k - 2) / 2)) & 1);
           HeadOut h;
           if (!site_op<F>(seq_op(k), s, st, b, tile, r, c, H, W, nx, k + 1 < nseq ? c : c + 1, keep, k == nseq - 1,
-                          &h)) {
+                          &h, hmask)) {
             st.abort = true;
             break;
           }
@@ -1645,6 +1679,8 @@ __global__ void __launch_bounds__(128) sample_kernel(const __grid_constant__ Sam
             kre.add(up ? h.re0 : h.re1);
             kim.add(up ? h.im0 : h.im1);
             if (sample < a.batch) a.spins[sample * P + pix] = up ? (int8_t)1 : (int8_t)-1;
+            n_up += up ? 1 : 0;
+            hmask = a.updown ? ((2 * n_up >= P ? 1 : 0) | (2 * (pix + 1 - n_up) >= P ? 2 : 0)) : 0;
           }
         }
         if (eng.aborted()) break;
@@ -1653,7 +1689,7 @@ __global__ void __launch_bounds__(128) sample_kernel(const __grid_constant__ Sam
     for (int c = 0; c < W && !kSite; ++c) {
       const int pix = r * W + c;
       HeadOut h;
-      run_op<F, TC, T>(a.op[last][2], eng, tile, r, c, H, W, P, &h);
+      run_op<F, TC, T>(a.op[last][2], eng, tile, r, c, H, W, P, &h, hmask);
       if (eng.aborted()) break;
       // deepar/samplers/autoregressive.py:41-43 (+1 iff p(+1) > U), drawn with
       // Philox counter (sample, site, offset).
@@ -1663,6 +1699,8 @@ __global__ void __launch_bounds__(128) sample_kernel(const __grid_constant__ Sam
       kre.add(up ? h.re0 : h.re1);
       kim.add(up ? h.im0 : h.im1);
       if (sample < a.batch) a.spins[sample * P + pix] = up ? (int8_t)1 : (int8_t)-1;
+      n_up += up ? 1 : 0;
+      hmask = a.updown ? ((2 * n_up >= P ? 1 : 0) | (2 * (pix + 1 - n_up) >= P ? 2 : 0)) : 0;
       __syncthreads();
       for (int i = 0; i < last && !eng.aborted(); ++i) {
         run_op<F, TC, T>(a.op[i][1], eng, tile, r, c, H, W, P, &h);
@@ -1700,6 +1738,7 @@ static int sample_impl(const NetLayout& L, const void* packed, int64_t batch, ui
   SampleArgs* a = new SampleArgs;
   memset(a, 0, sizeof(SampleArgs));
   a->n_cc = L.n_cc;
+  a->updown = L.updown;
   a->batch = batch;
   a->seed_lo = (uint32_t)seed;
   a->seed_hi = (uint32_t)(seed >> 32);
@@ -1943,6 +1982,10 @@ static int connections_impl(const NetLayout& L, const void* packed, const int8_t
                                                                                  L.P, S.cfg, S.cown);
     conn_items_kernel<<<1, 1024, 0, s>>>(S.srk, j0, n, L.H, S.rk_start, S.items, S.n_items);
     FK_CUDA(launched(2));
+    if (L.updown) {
+      updown_mask_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(S.cfg, n, L.P, T.updown);
+      FK_CUDA(launched());
+    }
     for (int i = 0; i < L.n_cc; ++i) {
       CCTensors x = cc_tensors(L, T, FK_AR2D_INFER, i);
       const bool last = i == L.n_cc - 1;
@@ -1956,7 +1999,10 @@ static int connections_impl(const NetLayout& L, const void* packed, const int8_t
       for (int k = 0; k < 3; ++k) {
         ops[k].items = S.items;
         ops[k].n_items = S.n_items;
-        if (last && k == 2) ops[k].row_partial = T.row_partial;
+        if (last && k == 2) {
+          ops[k].row_partial = T.row_partial;
+          ops[k].updown = T.updown;
+        }
         int st = run_engine_op<F, TC>(ops[k], tiles, L, err, s);
         if (st != FK_OK) return st;
       }

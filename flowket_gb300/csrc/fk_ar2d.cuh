@@ -35,6 +35,7 @@ constexpr int kMaxConvs = 5 * 38 + 1;
 
 struct NetLayout {
   int H, W, P, depth, F, wn, precision, n_cc;
+  int updown;  // EqualUpDownSpins mask
   int n_convs;
   int64_t num_params;
   int64_t packed_bytes;
@@ -81,6 +82,7 @@ struct OpArgs {
   void* cat;            // concat tensor (F channels): H writes [0,F/2), V writes [F/2,F)
   float2* row_partial;  // last C: [tiles][H][128] log psi partial per row
   float* cond;          // last C: [batch][P][4] normalised conditionals (optional)
+  const uint8_t* updown;  // last C: [batch][P] EqualUpDownSpins mask bits (1: outcome +1, 2: -1) or NULL
   int64_t batch;
   // Optional work list: item k = tile * H + row for k < *n_items (row-suffix
   // evaluation of connected configurations); NULL = every (tile, row).
@@ -97,6 +99,7 @@ struct Tensors {
   void* t[40];
   void* rv[40];
   float2* row_partial;
+  uint8_t* updown;  // [batch][P] mask bits (EqualUpDownSpins) or NULL
   int64_t bytes;
 };
 

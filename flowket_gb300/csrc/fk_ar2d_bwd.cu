@@ -62,6 +62,7 @@ struct HeadBwdArgs {
   int64_t batch;
   float* gL;             // [tiles][P][8ch] fp32 (4 used)
   void* ghp;             // [tiles][P][F] (gradient type)
+  int updown;            // EqualUpDownSpins mask (from the spins)
 };
 
 template <int F, typename T, typename TG>
@@ -72,8 +73,13 @@ __global__ void __launch_bounds__(128) head_bwd_kernel(const __grid_constant__ H
   const int m = threadIdx.x;
   const int64_t b = tile * kTile + m;
   float2 w = b < a.batch ? a.seeds[b] : make_float2(0.f, 0.f);
+  // EqualUpDownSpins: +1 spins before the row's first site
+  int n_up = 0;
+  if (a.updown)
+    for (int k = 0; k < r * W; ++k) n_up += spin_at(a.spins, a.batch, P, b, k) > 0.f ? 1 : 0;
   for (int c = 0; c < W; ++c) {
     const int pix = r * W + c;
+    const int mk = a.updown ? ((2 * n_up >= P ? 1 : 0) | (2 * (pix - n_up) >= P ? 2 : 0)) : 0;
     float g[F];
     load_row(blk<T>(a.hlast, tile, P, pix, F), m, 0, F, g);
     float l[4];
@@ -84,9 +90,11 @@ __global__ void __launch_bounds__(128) head_bwd_kernel(const __grid_constant__ H
 #pragma unroll
       for (int j = 0; j < 4; ++j) l[j] += g[k] * __ldg(a.wo + k * 4 + j);
     }
-    float pi0 = 1.f / (1.f + expf(2.f * (l[1] - l[0])));
+    // a masked outcome has probability 0 (layers/spins_invariants.py:13-22)
+    float pi0 = (mk & 1) ? 0.f : ((mk & 2) ? 1.f : 1.f / (1.f + expf(2.f * (l[1] - l[0]))));
     float pi1 = 1.f - pi0;
     bool up = spin_at(a.spins, a.batch, P, b, pix) > 0.f;
+    n_up += up ? 1 : 0;
     float gl[8] = {w.x * ((up ? 1.f : 0.f) - pi0), w.x * ((up ? 0.f : 1.f) - pi1), up ? w.y : 0.f,
                    up ? 0.f : w.y, 0.f, 0.f, 0.f, 0.f};
     store_g(a.gL, tile, P, pix, 8, m, 0, 8, gl);
@@ -568,6 +576,7 @@ static int backward_impl(const NetLayout& L, const void* packed, const float* pa
     h.batch = batch;
     h.gL = G.gl;
     h.ghp = G.ghp[last];
+    h.updown = L.updown;
     head_bwd_kernel<F, T, float><<<rows, 128, 0, s>>>(h, L.H, L.W);
     FK_CUDA(launched());
     WgArgs w;
@@ -746,6 +755,7 @@ static int backward_tc(const NetLayout& L, const void* packed, const float* para
     h.batch = batch;
     h.gL = G.gl;
     h.ghp = G.ghp[last];
+    h.updown = L.updown;
     head_bwd_kernel<F, T, T><<<rows, 128, 0, s>>>(h, L.H, L.W);
     FK_CUDA(launched());
     WgArgs w;

@@ -203,12 +203,18 @@ __global__ void __launch_bounds__(kPipeThreads, 1) op_pipe_kernel(const __grid_c
       } else {
 #pragma unroll
         for (int n = 0; n < 4; ++n) out[n] += bc[n];
+        const int64_t sample = ptile * kTile + m;
+        if (a.updown && sample < a.batch) {
+          // EqualUpDownSpins (layers/spins_invariants.py:13-22)
+          const int mk = a.updown[sample * P + pix];
+          if (mk & 1) out[0] = -INFINITY;
+          if (mk & 2) out[1] = -INFINITY;
+        }
         // abstract_machine.py:56-57 normalisation (same arithmetic as the per-pixel engine)
         float a2 = 2.f * out[0], b2 = 2.f * out[1];
         float mx = fmaxf(a2, b2);
         float lse = 0.5f * (mx + logf(expf(a2 - mx) + expf(b2 - mx)));
         float re0 = out[0] - lse, re1 = out[1] - lse;
-        const int64_t sample = ptile * kTile + m;
         bool up = spin_at(a.spins, a.batch, P, sample, pix) > 0.f;
         head_sm[pc * kTile + m] = make_float2(up ? re0 : re1, up ? out[2] : out[3]);
         if (a.cond && sample < a.batch)

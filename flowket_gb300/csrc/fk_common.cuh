@@ -233,6 +233,11 @@ __host__ __device__ inline float philox_uniform(uint32_t x) {
 struct Kahan {
   float s = 0.f, c = 0.f;
   __host__ __device__ void add(float x) {
+    if (isinf(x) || isinf(s)) {  // log psi = -inf (a masked configuration): the sum stays -inf
+      s += x;
+      c = 0.f;
+      return;
+    }
     float y = x - c;
     float t = s + y;
     c = (t - s) - y;

@@ -77,7 +77,8 @@ class ConvNetAutoregressive2D:
     CUDA-core path ('fp32')."""
 
     def __init__(self, hilbert_state_shape, depth, num_of_channels, kernel_size=3, weights_normalization=True,
-                 exponential_norm=True, precision="bf16", seed=0, device=None, params=None):
+                 exponential_norm=True, precision="bf16", seed=0, device=None, params=None,
+                 equal_up_down_spins=False):
         if kernel_size != 3 or not exponential_norm:
             raise ValueError("only kernel_size=3 with exponential_norm=True (the reference defaults) is supported")
         shape = tuple(int(x) for x in hilbert_state_shape)
@@ -89,9 +90,11 @@ class ConvNetAutoregressive2D:
         self.weights_normalization = bool(weights_normalization)
         self.precision = precision
         self.device = _device(device)
+        self.equal_up_down_spins = bool(equal_up_down_spins)
         self.desc = _lib.Ar2dDesc(shape[0], shape[1], self.depth, self.num_of_channels,
                                   1 if self.weights_normalization else 0,
-                                  _lib.FK_PRECISION_BF16 if precision == "bf16" else _lib.FK_PRECISION_FP32)
+                                  _lib.FK_PRECISION_BF16 if precision == "bf16" else _lib.FK_PRECISION_FP32,
+                                  1 if self.equal_up_down_spins else 0)
         lib = _lib.load()
         self.layout, n = ar2d_param_layout(self.depth, self.num_of_channels, self.weights_normalization)
         n_lib = lib.fk_ar2d_num_params(ctypes_ref(self.desc))

@@ -99,6 +99,11 @@ typedef struct fk_ar2d_desc {
   int32_t channels;              /* num_of_channels: 16, 32 or 64 */
   int32_t weights_normalization; /* 1 = WeightNormalization(exponential_norm=True) */
   int32_t precision;             /* FK_PRECISION_FP32 or FK_PRECISION_BF16 */
+  int32_t equal_up_down_spins;   /* 1 = EqualUpDownSpins mask before the normalisation
+                                    (abstract_machine.py:52-53, layers/spins_invariants.py:13-22):
+                                    outcome k of a site gets log-amplitude -inf once N/2 earlier
+                                    sites (raster order) hold it, so the distribution lives on the
+                                    Sz = 0 sector */
 } fk_ar2d_desc;
 
 /* Flat FP32 parameter vector in Keras layer order: per causal conv i and conv

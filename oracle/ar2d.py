@@ -116,19 +116,36 @@ def logits(params, spins, depth, weights_normalization):
     return _conv_valid(relu(h), params["out.kernel"], params["out.bias"])
 
 
-def conditional_log_wave_function(params, spins, depth, weights_normalization):
+def equal_up_down_mask(spins):
+    """layers/spins_invariants.py:13-22: outcome k (0: spin +1, 1: spin -1) of
+    a site is masked when the number of earlier sites in raster order
+    holding outcome k (exclusive cumulative sum) is >= N/2. (B,H,W,2) bool."""
+    b = spins.shape[0]
+    n = int(np.prod(spins.shape[1:]))
+    idx = ((1 - spins.to(torch.int64)) // 2).reshape(b, n)
+    onehot = torch.nn.functional.one_hot(idx, 2).to(torch.float64)
+    cum = torch.cumsum(onehot, dim=1) - onehot
+    return (cum >= n / 2.0).reshape(tuple(spins.shape) + (2,))
+
+
+def conditional_log_wave_function(params, spins, depth, weights_normalization, equal_up_down=False):
     """(B,H,W,2) real and imaginary parts of the normalised conditionals
-    (abstract_machine.py:56-57 with norm_type=2; autoregressive.py:7-15)."""
+    (abstract_machine.py:56-57 with norm_type=2; autoregressive.py:7-15).
+    With ``equal_up_down`` the EqualUpDownSpins mask (abstract_machine.py:52-53)
+    adds LOG_ZERO (-1e300, -inf in float32) to the masked outcomes' real part
+    before the normalisation; -inf is used here."""
     out = logits(params, spins, depth, weights_normalization)
     re, im = out[..., 0:2], out[..., 2:4]
+    if equal_up_down:
+        re = torch.where(equal_up_down_mask(spins), torch.full_like(re, -math.inf), re)
     re = re - 0.5 * torch.logsumexp(2.0 * re, dim=-1, keepdim=True)
     return re, im
 
 
-def log_psi(params, spins, depth, weights_normalization):
+def log_psi(params, spins, depth, weights_normalization, equal_up_down=False):
     """log psi(s) = sum over sites of the conditional picked by the one-hot spin
     (abstract_machine.py:31-46, autoregressive.py:18-22). Returns (re, im)."""
-    re, im = conditional_log_wave_function(params, spins, depth, weights_normalization)
+    re, im = conditional_log_wave_function(params, spins, depth, weights_normalization, equal_up_down)
     idx = ((1 - spins.to(torch.int64)) // 2).unsqueeze(-1)
     re_s = torch.gather(re, -1, idx).squeeze(-1)
     im_s = torch.gather(im, -1, idx).squeeze(-1)
@@ -159,20 +176,20 @@ def params_to(params, dtype):
     return {k: v.detach().to(dtype).clone() for k, v in params.items()}
 
 
-def log_psi_numpy(params, spins, depth, weights_normalization, dtype=torch.float64):
+def log_psi_numpy(params, spins, depth, weights_normalization, dtype=torch.float64, equal_up_down=False):
     p = params_to(params, dtype)
     with torch.no_grad():
-        re, im = log_psi(p, torch.as_tensor(np.asarray(spins)), depth, weights_normalization)
+        re, im = log_psi(p, torch.as_tensor(np.asarray(spins)), depth, weights_normalization, equal_up_down)
     return re.numpy() + 1j * im.numpy()
 
 
 def weighted_gradient(params, spins, depth, weights_normalization, w_re, w_im,
-                      dtype=torch.float64):
+                      dtype=torch.float64, equal_up_down=False):
     """d/dtheta sum_s (w_re[s] Re log psi(s) + w_im[s] Im log psi(s)) by autograd.
     This is the loss gradient of optimization/loss.py:4-5 when
     w = 2 Re(y)/B, -2 Im(y)/B, and the per-sample O_k rows when w is one-hot."""
     p = {k: v.detach().to(dtype).clone().requires_grad_(True) for k, v in params.items()}
-    re, im = log_psi(p, torch.as_tensor(np.asarray(spins)), depth, weights_normalization)
+    re, im = log_psi(p, torch.as_tensor(np.asarray(spins)), depth, weights_normalization, equal_up_down)
     loss = (torch.as_tensor(w_re, dtype=dtype) * re).sum() + (torch.as_tensor(w_im, dtype=dtype) * im).sum()
     loss.backward()
     return {k: v.grad.detach() for k, v in p.items()}

@@ -262,3 +262,27 @@ def test_fast_sampler_restatement_equals_slow_sampler():
 
     slow = samplers.autoregressive_sample(cond_lp, shape, 64, seed=3, offset=1)
     assert np.array_equal(fast, slow.astype(np.int8))
+
+
+def test_equal_up_down_mask_restricts_the_distribution_to_sz0():
+    """EqualUpDownSpins (layers/spins_invariants.py:13-22): the masked AR
+    network is normalised over the Sz = 0 sector and zero outside it; the
+    mask marks outcome k once N/2 earlier sites hold it."""
+    import torch
+    x = torch.tensor([[[1, 1], [-1, 1]]], dtype=torch.int8)
+    m = ar2d.equal_up_down_mask(x)[0].reshape(4, 2)
+    # earlier +1 counts 0, 1, 2, 2 -> outcome 0 masked from the third site on
+    assert m[:, 0].tolist() == [False, False, True, True]
+    assert m[:, 1].tolist() == [False, False, False, False]
+    shape = (3, 4)
+    params = ar2d.init_params(shape, 3, 16, True, seed=5, dtype=torch.float64)
+    g = torch.Generator().manual_seed(1)
+    params = {k: v + 0.05 * torch.randn(v.shape, generator=g, dtype=torch.float64) for k, v in params.items()}
+    states = exact.all_states(shape)
+    lp = ar2d.log_psi_numpy(params, states, 3, True, equal_up_down=True)
+    p = np.exp(2 * lp.real)
+    sz0 = states.reshape(states.shape[0], -1).sum(axis=1) == 0
+    assert np.all(p[~sz0] == 0.0)
+    assert p[sz0].sum() == pytest.approx(1.0, abs=1e-12)
+    lp0 = ar2d.log_psi_numpy(params, states, 3, True)
+    assert np.exp(2 * lp0.real).sum() == pytest.approx(1.0, abs=1e-12)
