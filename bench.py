@@ -15,6 +15,7 @@ bounded sample of the same workload.
 """
 import argparse
 import json
+import math
 import os
 import subprocess
 import sys
@@ -54,7 +55,7 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--fp32-steps", type=int, default=2)
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--case", default="vmc", choices=["vmc", "forward", "energy4x4", "vmc16"],
+    p.add_argument("--case", default="vmc", choices=["vmc", "forward", "energy4x4", "vmc16", "ising12"],
                    help="forward: only the batched AR2D forward of the local-energy stage on --configs "
                         "connected configurations (the small case used for ncu captures); energy4x4: train "
                         "the 4x4 Heisenberg model (depth 5, 16 channels) and compare its exact energy "
@@ -64,6 +65,9 @@ def parse():
     p.add_argument("--train-batch", type=int, default=2048)
     p.add_argument("--configs", type=int, default=32768)
     p.add_argument("--batch", type=int, default=8192)
+    p.add_argument("--weights", default=None, help="ising12: a Keras weight file of the reference's 12x12 models")
+    p.add_argument("--gamma", type=float, default=3.0)
+    p.add_argument("--samples", type=int, default=1 << 15)
     return p.parse_args()
 
 
@@ -122,6 +126,56 @@ def vmc16_case(args):
         out[prec] = {"ms_per_step": ms, "samples_per_s": args.batch / (ms / 1e3), "steps": steps,
                      "stage_ms": vmc.times, "energy": vmc.current_energy.real}
     out["bf16_over_fp32"] = out["fp32"]["ms_per_step"] / out["bf16"]["ms_per_step"]
+    print(json.dumps(out), flush=True)
+
+
+# experiments/README.md, "Ising (2^15 sampels)": 12x12 open-boundary transverse
+# Ising at field gamma, the published depth-10 32-channel models evaluated
+# with the D4 x spin-flip ensemble: energy, local-energy variance, |Mz|.
+PUBLISHED_ISING_12X12 = {2.0: (-346.9817926, 0.00125, 0.783929189), 2.5: (-395.6618438, 0.00421, 0.57235633),
+                         3.0: (-457.0420317, 0.000821, 0.1622390747), 3.5: (-524.5172088, 0.000647, 0.1106881036),
+                         4.0: (-593.5389339, 0.000777, 0.09679073758)}
+
+
+def ising12_case(args):
+    """The reference's published evaluation (experiments/run_evaluation.py:12-24)
+    on this stack: the Keras weight file loaded into ConvNetAutoregressive2D
+    (12x12, depth 10, 32 channels, weight norm), wrapped in
+    make_up_down_invariant(make_2d_obc_invariants(model)), samples of the base
+    model's exact sampler, local energies of the ensemble for the open-boundary
+    Ising operator at field gamma; mean energy, variance and |Mz| over
+    `--samples` samples, next to the published numbers."""
+    from flowket_gb300.ensemble import make_2d_obc_invariants, make_up_down_invariant
+    from flowket_gb300.machines import ConvNetAutoregressive2D
+    from flowket_gb300.operators import Ising
+    from flowket_gb300.optimization import VariationalMonteCarlo
+    from flowket_gb300.samplers import FastAutoregressiveSampler
+    if not args.weights:
+        raise SystemExit("--weights is required for --case ising12")
+    shape = (12, 12)
+    m = ConvNetAutoregressive2D(shape, 10, 32, weights_normalization=True, precision=args.precision, seed=0)
+    m.load_weights(args.weights)
+    ens = make_up_down_invariant(make_2d_obc_invariants(m))
+    batch = min(args.batch, args.samples)
+    vmc = VariationalMonteCarlo(ens, Ising(h=args.gamma, hilbert_state_shape=shape, pbc=False),
+                                FastAutoregressiveSampler(m, batch, seed=2024))
+    loc, mz = [], []
+    t0 = time.perf_counter()
+    for _ in range(max(1, args.samples // batch)):
+        spins, _ = vmc.next_batch()
+        loc.append(vmc.current_local_energy.real.double())
+        mz.append(spins.reshape(batch, -1).double().mean(dim=1).abs())
+    torch.cuda.synchronize()
+    e = torch.cat(loc)
+    n = e.numel()
+    energy, var = float(e.mean()), float(e.var(unbiased=False))
+    out = {"case": "ising12", "gamma": args.gamma, "precision": args.precision, "samples": n,
+           "energy": energy, "energy_per_spin": energy / 144, "local_energy_variance": var,
+           "abs_mz": float(torch.cat(mz).mean()), "stderr": math.sqrt(var / n), "seconds": time.perf_counter() - t0}
+    if args.gamma in PUBLISHED_ISING_12X12:
+        pe, pv, pm = PUBLISHED_ISING_12X12[args.gamma]
+        out["published"] = {"energy": pe, "local_energy_variance": pv, "abs_mz": pm}
+        out["energy_minus_published"] = energy - pe
     print(json.dumps(out), flush=True)
 
 
@@ -461,6 +515,8 @@ def main():
         energy4x4_case(args)
     elif args.case == "vmc16":
         vmc16_case(args)
+    elif args.case == "ising12":
+        ising12_case(args)
     elif args.impl == "reference":
         reference_arm(args, rank, world)
     else:

@@ -125,6 +125,12 @@ class ConvNetAutoregressive2D:
     def count_params(self):
         return self.num_params
 
+    def load_weights(self, filepath):
+        """Keras ``model.load_weights`` of a weight file saved by the reference's
+        ConvNetAutoregressive2D (HDF5, see flowket_gb300.h5weights)."""
+        from .h5weights import load_conv_net_autoregressive_2d
+        return load_conv_net_autoregressive_2d(self, filepath)
+
     def params_updated(self):
         """Call after writing `params` through a raw pointer (the optimisers do)."""
         self._manual_version += 1
