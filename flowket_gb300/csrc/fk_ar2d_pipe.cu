@@ -34,7 +34,9 @@ struct FwdCfg {
   static int head_bytes(int w) { return w * kTile * 8; }
 };
 
-template <int F>
+// RES: the op adds a residual to its stream output (its own instantiation, so
+// that ops without one compile without the residual prefetch).
+template <int F, bool RES>
 __global__ void __launch_bounds__(kPipeThreads, 1) op_pipe_kernel(const __grid_constant__ OpArgs a, int H, int W,
                                                                   int64_t n_items, int* err) {
   // With a work list, n_items is an upper bound and the list's count is read
@@ -163,7 +165,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) op_pipe_kernel(const __grid_c
     const uint32_t tl = tmem + ((uint32_t)(q4 * 32) << 16);
     const float* bm = bias_sm;
     const float* bc = bias_sm + 32;
-    const bool need_res = (kind == kConvV && a.stream_out && a.res) || (kind == kConvC && !a.last && a.res);
+    constexpr bool need_res = RES;
     // deferred second half: output index, tile, row, column
     bool pend = false;
     uint32_t pq = 0;
@@ -254,7 +256,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) op_pipe_kernel(const __grid_c
 #pragma unroll
           for (int n = 0; n < F; ++n) acc[n] += bm[n];
           if (a.stream_out) {
-            if (a.res) {
+            if (need_res) {
 #pragma unroll
               for (int n = 0; n < F; ++n) o[n] = fmaxf(o[n] + acc[n], 0.f);
             } else {
@@ -274,7 +276,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) op_pipe_kernel(const __grid_c
 #pragma unroll
           for (int n = 0; n < F; ++n) acc[n] += bm[n];
           if (!a.last) {
-            if (a.res) {
+            if (need_res) {
 #pragma unroll
               for (int n = 0; n < F; ++n) o[n] = fmaxf(o[n] + acc[n], 0.f);
             } else {
@@ -349,14 +351,20 @@ static int launch_pipe(const OpArgs& a, int64_t tiles, int H, int W, int* err, c
   if (smem < kMinSmem) smem = kMinSmem;
   if (!attr) {
     const int most = FwdCfg<F>::kSmemBase + FwdCfg<F>::head_bytes(FwdCfg<F>::kMaxW);
-    FK_CUDA(cudaFuncSetAttribute(op_pipe_kernel<F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    FK_CUDA(cudaFuncSetAttribute(op_pipe_kernel<F, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 most > kMinSmem ? most : kMinSmem));
+    FK_CUDA(cudaFuncSetAttribute(op_pipe_kernel<F, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  most > kMinSmem ? most : kMinSmem));
     attr = true;
   }
   const int64_t items = tiles * H;
   int64_t grid = (int64_t)sms;  // one CTA per SM (512 TMEM columns)
   if (grid > items) grid = items;
-  op_pipe_kernel<F><<<(unsigned)grid, kPipeThreads, smem, s>>>(a, H, W, items, err);
+  const bool res = (a.kind == kConvV && a.stream_out && a.res) || (a.kind == kConvC && !a.last && a.res);
+  if (res)
+    op_pipe_kernel<F, true><<<(unsigned)grid, kPipeThreads, smem, s>>>(a, H, W, items, err);
+  else
+    op_pipe_kernel<F, false><<<(unsigned)grid, kPipeThreads, smem, s>>>(a, H, W, items, err);
   return check_cuda(launched(), "op_pipe_kernel");
 }
 
