@@ -55,7 +55,7 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--fp32-steps", type=int, default=2)
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--case", default="vmc", choices=["vmc", "forward", "energy4x4", "vmc16", "ising12"],
+    p.add_argument("--case", default="vmc", choices=["vmc", "forward", "energy4x4", "vmc16", "ising12", "matched"],
                    help="forward: only the batched AR2D forward of the local-energy stage on --configs "
                         "connected configurations (the small case used for ncu captures); energy4x4: train "
                         "the 4x4 Heisenberg model (depth 5, 16 channels) and compare its exact energy "
@@ -126,6 +126,52 @@ def vmc16_case(args):
         out[prec] = {"ms_per_step": ms, "samples_per_s": args.batch / (ms / 1e3), "steps": steps,
                      "stage_ms": vmc.times, "energy": vmc.current_energy.real}
     out["bf16_over_fp32"] = out["fp32"]["ms_per_step"] / out["bf16"]["ms_per_step"]
+    print(json.dumps(out), flush=True)
+
+
+def matched_case(args):
+    """The metric's "at matched energy": the bench workload (TFIM 10x10 PBC
+    h=3, depth 10, 32 channels, weight norm) trained from the same seeded
+    parameters for `--train-steps` VMC steps of `--batch` samples with Adam
+    (lr 1e-3) on the BF16 path and on the plain FP32 path; each trained model's
+    energy is then estimated from `--samples` fresh samples of its own
+    sampler. Reports both energies, their relative difference and the
+    training throughput of each path."""
+    from flowket_gb300.machines import ConvNetAutoregressive2D
+    from flowket_gb300.observables import Observable, energy_stats
+    from flowket_gb300.operators import Ising
+    from flowket_gb300.optimization import VariationalMonteCarlo
+    from flowket_gb300.optimizers import Adam
+    from flowket_gb300.samplers import FastAutoregressiveSampler
+    op = Ising(h=H_FIELD, hilbert_state_shape=SHAPE, pbc=True)
+    out = {"case": "matched", "workload": WORKLOAD, "train_steps": args.train_steps, "batch": args.batch,
+           "eval_samples": args.samples}
+    for prec in ("bf16", "fp32"):
+        m = ConvNetAutoregressive2D(SHAPE, DEPTH, CHANNELS, weights_normalization=True, precision=prec, seed=0)
+        vmc = VariationalMonteCarlo(m, op, FastAutoregressiveSampler(m, args.batch, seed=1234))
+        opt = Adam(m, lr=1e-3)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(args.train_steps):
+            vmc.step(opt, sync=False)
+        b.record()
+        torch.cuda.synchronize()
+        train_ms = a.elapsed_time(b)
+        sampler = FastAutoregressiveSampler(m, min(args.samples, 8192), seed=777)
+        obs = Observable(op)
+        loc = []
+        for _ in range(max(1, args.samples // sampler.batch_size)):
+            spins, lp, saved = sampler.sample()
+            loc.append(obs.local_values(m, spins, log_psi=lp, base_saved=saved).clone())
+        stats, _ = energy_stats(torch.cat(loc))
+        st = stats.tolist()
+        n = sum(x.shape[0] for x in loc)
+        out[prec] = {"energy": st[0], "stderr": math.sqrt(st[2] / n), "train_ms": train_ms,
+                     "train_samples_per_s": args.train_steps * args.batch / (train_ms / 1e3)}
+    e16, e32 = out["bf16"]["energy"], out["fp32"]["energy"]
+    out["relative_difference"] = abs(e16 - e32) / abs(e32)
+    out["bf16_over_fp32"] = out["bf16"]["train_samples_per_s"] / out["fp32"]["train_samples_per_s"]
     print(json.dumps(out), flush=True)
 
 
@@ -517,6 +563,8 @@ def main():
         vmc16_case(args)
     elif args.case == "ising12":
         ising12_case(args)
+    elif args.case == "matched":
+        matched_case(args)
     elif args.impl == "reference":
         reference_arm(args, rank, world)
     else:
