@@ -3,7 +3,7 @@
 TEST INFRASTRUCTURE ONLY. Nothing in the product (``flowket_gb300``) imports,
 calls or links anything in this package; only ``tests/``, the smoke check in
 ``__graft_entry__.py`` and the CPU-baseline leg of ``bench.py`` use it, and
-only as the checker / the timed CPU baseline.
+only to check results or as the timed CPU baseline.
 
 Each function cites the reference file:line it restates (paths relative to the
 FlowKet source tree). The reference itself (TensorFlow 1.x / tf.keras) cannot

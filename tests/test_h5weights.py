@@ -7,7 +7,8 @@ import os
 import numpy as np
 import pytest
 
-REF_WEIGHTS = os.path.join(os.sep, "root", "reference", "experiments", "weights")
+# the reference checkout's experiments/weights directory (read here, never copied)
+REF_WEIGHTS = os.environ.get("FLOWKET_REFERENCE_WEIGHTS", "/root/reference/experiments/weights")
 
 
 def _path(name):

@@ -51,7 +51,7 @@ def test_descriptor_queries_without_gpu(built):
         n = lib.fk_ar2d_num_params(ctypes.byref(desc))
         assert n == ar2d_param_layout(d, f, bool(wn))[1]
         assert lib.fk_ar2d_workspace_bytes(ctypes.byref(desc), 4096, 1) > 0
-    # 42,756 parameters for depth 5, 16 channels without weight norm
+    # 42,756 parameters for depth 5, 16 channels without weight norm (the reference's 4x4 machine)
     assert lib.fk_ar2d_num_params(ctypes.byref(_lib.Ar2dDesc(4, 4, 5, 16, 0, 1))) == 42756
     bad = _lib.Ar2dDesc(4, 4, 5, 24, 0, 1)
     assert lib.fk_ar2d_num_params(ctypes.byref(bad)) < 0
