@@ -102,3 +102,23 @@ def test_compaction_and_local_energy_match_oracle(cuda):
     got = local[:, 0].cpu().numpy() + 1j * local[:, 1].cpu().numpy()
     assert r == int(use_np[1:].sum())
     np.testing.assert_allclose(got, want, rtol=2e-5, atol=2e-5)
+
+
+def test_find_conn_equals_golden_fixture(cuda):
+    """Bit-exact against the committed fixture tests/golden/connections_4x4.json."""
+    import json
+    import os
+    from flowket_gb300 import operators as ops
+    gold = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "connections_4x4.json")))
+    s = torch.as_tensor(np.array(gold["configs"], dtype=np.int8)).cuda()
+    shape = (4, 4)
+    for name, op in (("heisenberg", ops.Heisenberg(hilbert_state_shape=shape, pbc=True)),
+                     ("ising", ops.Ising(h=3.0, hilbert_state_shape=shape, pbc=True)),
+                     ("j1j2", ops.J1J2(hilbert_state_shape=shape, j2=0.5, pbc=True))):
+        conn, mel, use = op.find_conn(s)
+        g = gold[name]
+        assert np.array_equal(conn.cpu().numpy(), np.array(g["conn"], dtype=np.int8)), name
+        m = mel.cpu().numpy()
+        m = m.real if np.iscomplexobj(m) else m
+        assert np.array_equal(m, np.array(g["mel"])), name
+        assert np.array_equal(use.cpu().numpy(), np.array(g["use"], dtype=bool)), name

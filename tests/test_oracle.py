@@ -286,3 +286,21 @@ def test_equal_up_down_mask_restricts_the_distribution_to_sz0():
     assert p[sz0].sum() == pytest.approx(1.0, abs=1e-12)
     lp0 = ar2d.log_psi_numpy(params, states, 3, True)
     assert np.exp(2 * lp0.real).sum() == pytest.approx(1.0, abs=1e-12)
+
+
+def test_oracle_reproduces_golden_connections():
+    """tests/golden/connections_4x4.json (written by tests/golden/make_golden.py)."""
+    import json
+    import os
+    path = os.path.join(os.path.dirname(__file__), "golden", "connections_4x4.json")
+    gold = json.load(open(path))
+    s = np.array(gold["configs"], dtype=np.float64)
+    fcs = {"heisenberg": lambda x: operators.heisenberg_find_conn(x, pbc=True),
+           "ising": lambda x: operators.ising_find_conn(x, h=3.0, pbc=True),
+           "j1j2": lambda x: operators.j1j2_find_conn(x, j2=0.5, pbc=True)}
+    for name, fc in fcs.items():
+        conn, mel, use = fc(s)
+        g = gold[name]
+        assert np.array_equal(np.asarray(conn).astype(np.int8), np.array(g["conn"], dtype=np.int8)), name
+        assert np.array_equal(np.asarray(mel, dtype=np.complex128).real, np.array(g["mel"])), name
+        assert np.array_equal(np.asarray(use, dtype=bool), np.array(g["use"], dtype=bool)), name
