@@ -161,3 +161,18 @@ def test_sampler_wide_rows_equals_forward(cuda, shape, f):
     fwd, _, _ = m.forward(spins)
     assert torch.equal(fwd, lp)
     assert torch.all(torch.isfinite(lp))
+
+
+@pytest.mark.parametrize("updown", [False, True])
+def test_sampler_f64_equals_forward(cuda, updown):
+    """F = 64 runs the sampler's per-pixel ops; log psi bitwise equal to the
+    forward's, with and without the EqualUpDownSpins mask."""
+    from flowket_gb300.machines import ConvNetAutoregressive2D
+    from flowket_gb300.samplers import FastAutoregressiveSampler
+    m = ConvNetAutoregressive2D((4, 4), 2, 64, weights_normalization=True, precision="bf16", seed=3,
+                                equal_up_down_spins=updown)
+    spins, lp, _ = FastAutoregressiveSampler(m, 256, seed=9).sample()
+    fwd, _, _ = m.forward(spins)
+    assert torch.equal(fwd, lp)
+    if updown:
+        assert torch.all(spins.view(256, -1).sum(dim=1) == 0)
