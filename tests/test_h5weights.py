@@ -55,3 +55,15 @@ def test_flat_vector_matches_the_machine_layout_and_oracle():
     np.testing.assert_allclose(torch.exp(2 * re).sum(-1).numpy(), 1.0, rtol=1e-12)
     with pytest.raises(ValueError):
         keras_weights_to_flat(read_keras_weights(_path("ising_2.h5")), ar2d_param_layout(8, 32, True)[0])
+
+
+def test_reader_rejects_what_it_does_not_read(tmp_path):
+    from flowket_gb300.h5weights import read_keras_weights
+    p = tmp_path / "x.h5"
+    p.write_bytes(b"not an hdf5 file at all" * 4)
+    with pytest.raises(ValueError):
+        read_keras_weights(str(p))
+    # an HDF5 signature with a newer superblock version
+    p.write_bytes(b"\x89HDF\r\n\x1a\n" + bytes([2]) + bytes(200))
+    with pytest.raises(ValueError):
+        read_keras_weights(str(p))
