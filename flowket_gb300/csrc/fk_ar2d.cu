@@ -1649,7 +1649,8 @@ __global__ void __launch_bounds__(128) sample_kernel(const __grid_constant__ Sam
   Engine<F, TC> eng{&s, &st};
   // op k of a site: 0 = head C of conv L, then H_0, C_0, ..., H_{L-1}, C_{L-1}, H_L
   const int nseq = 2 * a.n_cc;
-  const SampOp* ops = reinterpret_cast<const SampOp*>(smem + SiteCfg<F <= 32 ? F : 32>::kOps);
+  // op records (the tensor-core site path only; the other paths read the kernel parameters)
+  const SampOp* ops = kSite ? reinterpret_cast<const SampOp*>(smem + SiteCfg<F <= 32 ? F : 32>::kOps) : nullptr;
   auto seq_op = [&](int k) -> const SampOp& {
     return k == 0 ? ops[3 * last + 2] : (k == nseq - 1 ? ops[3 * last + 1] : ops[3 * ((k - 1) / 2) + ((k & 1) ? 1 : 2)]);
   };
