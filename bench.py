@@ -19,6 +19,7 @@ import math
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -304,10 +305,10 @@ class Clocks:
 
     def __init__(self):
         self.proc = None
-        self.path = os.path.join(ROOT, "_work", "bench_clocks.csv")
+        fd, self.path = tempfile.mkstemp(prefix="fk_bench_clocks_", suffix=".csv")
+        os.close(fd)
 
     def start(self):
-        os.makedirs(os.path.dirname(self.path), exist_ok=True)
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -329,9 +330,11 @@ class Clocks:
         except Exception:
             self.proc.kill()
         self.f.close()
+        lines = open(self.path).read().splitlines()
+        os.unlink(self.path)
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in open(self.path):
+        for line in lines:
             parts = [x.strip() for x in line.split(",")]
             if len(parts) < 9:
                 continue

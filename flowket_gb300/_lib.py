@@ -62,6 +62,12 @@ _SIGNATURES = {
     "fk_sr_solve": (c_i32, [c_p, c_i64, c_f64, c_f64, c_p, c_f64, c_i32, c_p, c_p, c_p, c_i64, c_p]),
     "fk_sr_solve_noalloc": (c_i32, [c_p, c_i64, c_f64, c_f64, c_p, c_f64, c_i32, c_p, c_p, c_p]),
     "fk_sr_backmap": (c_i32, [c_p, c_p, c_i64, c_i64, c_p, c_f64, c_f32, c_p, c_p, c_p]),
+    "fk_sr_hermitian_embed": (c_i32, [c_p, c_i64, c_p]),
+    "fk_sr_complex_backmap": (c_i32, [c_p, c_p, c_i64, c_i64, c_p, c_f64, c_f32, c_p, c_p, c_p]),
+    "fk_selftest_wait_timeout": (c_i32, [c_i32, c_p]),
+    "fk_gather_complex": (c_i32, [c_p, c_p, c_i64, c_p, c_p]),
+    "fk_segment_sum_rows": (c_i32, [c_p, c_p, c_p, c_i64, c_i64, c_p, c_p]),
+    "fk_complex_param_gradient": (c_i32, [c_p, c_p, c_i64, c_i64, c_p, c_p, c_p]),
     "fk_center_columns": (c_i32, [c_p, c_i64, c_i64, c_p, c_p]),
     "fk_rbm_log_psi": (c_i32, [c_p, c_i32, c_i32, c_p, c_i64, c_p, c_p]),
     "fk_rbm_local_energy": (c_i32, [c_p, c_i32, c_i32, c_p, c_i64, c_p, c_p, c_p, c_i32, c_p, c_p]),
@@ -132,7 +138,32 @@ def stream_ptr(device=None):
     return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
 
 
+FK_STATUS_TIMEOUT = 1
+FK_STATUS_NONFINITE = 2
+
+
+class DeviceTimeout(FlowketError):
+    """A bounded device-side wait gave up; the kernel's outputs are incomplete."""
+
+
+class NonFiniteError(FlowketError):
+    """A non-finite energy statistic (the reference raises on a non-finite
+    wave function, samplers/metropolis_hastings.py:103-105)."""
+
+
 def device_status(clear=True):
     out = ctypes.c_int32(0)
     check(load().fk_device_status(ctypes.byref(out), 1 if clear else 0, stream_ptr()), "fk_device_status")
     return out.value
+
+
+def check_device(what="flowket_gb300"):
+    """Reads and clears the device error word (synchronises the current
+    stream) and raises if a kernel recorded a failure since the last check."""
+    st = device_status(clear=True)
+    if st & FK_STATUS_TIMEOUT:
+        raise DeviceTimeout(f"{what}: a device-side wait timed out; results of this step are incomplete")
+    if st & FK_STATUS_NONFINITE:
+        raise NonFiniteError(f"{what}: non-finite local energy (the wave function is not finite)")
+    if st:
+        raise FlowketError(f"{what}: device error word {st:#x}")

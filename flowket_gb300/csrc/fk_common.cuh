@@ -85,13 +85,22 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 // slice per poll, so this bounds a wait to well under a minute.
 constexpr uint32_t kMaxPolls = 1u << 24;
 
-// Returns false (and records FK_ERR_TIMEOUT) when the phase never completes.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err) {
-  for (uint32_t i = 0; i < kMaxPolls; ++i) {
+// Bits of the device error word (read by fk_device_status).
+constexpr int kStatusTimeout = 1;    // a bounded wait gave up
+constexpr int kStatusNonfinite = 2;  // a non-finite energy / log psi statistic
+
+// Returns false (and records kStatusTimeout) when the phase never completes
+// within `limit` polls.
+__device__ __forceinline__ bool mbar_wait_limit(uint64_t* bar, uint32_t parity, int* err, uint32_t limit) {
+  for (uint32_t i = 0; i < limit; ++i) {
     if (mbar_try_wait(bar, parity)) return true;
   }
-  if (err) atomicOr(err, 1);
+  if (err) atomicOr(err, kStatusTimeout);
   return false;
+}
+
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err) {
+  return mbar_wait_limit(bar, parity, err, kMaxPolls);
 }
 
 // 1D bulk copy global -> shared, completion counted in bytes on `bar`.

@@ -303,7 +303,7 @@ __global__ void local_energy_kernel(const float2* __restrict__ lp_self, const do
 // FP64 mean / variance and loss weights; single block, compensated by
 // accumulating in double over a fixed pairwise order.
 __global__ void energy_stats_kernel(const double2* __restrict__ local, int64_t batch, double* stats,
-                                    float2* __restrict__ w) {
+                                    float2* __restrict__ w, int* err) {
   __shared__ double sre[1024], sim[1024];
   int t = threadIdx.x;
   double a = 0.0, c = 0.0;
@@ -338,6 +338,9 @@ __global__ void energy_stats_kernel(const double2* __restrict__ local, int64_t b
     stats[0] = mre;
     stats[1] = mim;
     stats[2] = sre[0] / (double)batch;
+    // the reference raises on a non-finite wave function
+    // (samplers/metropolis_hastings.py:103-105); here it is flagged for the host
+    if (err && !(isfinite(mre) && isfinite(mim) && isfinite(sre[0]))) atomicOr(err, kStatusNonfinite);
   }
   // y = conj(E - Ebar)/B ; loss = mean 2 Re(logpsi y) -> weights 2Re(y)/B, -2Im(y)/B
   double inv = 1.0 / (double)batch;
@@ -464,7 +467,7 @@ int fk_local_energy_reduce(const float* log_psi_self, const double* mel_self, in
 int fk_energy_stats(const double* local, int64_t batch, double* stats, float* w, void* stream) {
   FK_CHECK_ARG(local && stats && w && batch > 0, "fk_energy_stats: bad arguments");
   energy_stats_kernel<<<1, 1024, 0, static_cast<cudaStream_t>(stream)>>>(
-      reinterpret_cast<const double2*>(local), batch, stats, reinterpret_cast<float2*>(w));
+      reinterpret_cast<const double2*>(local), batch, stats, reinterpret_cast<float2*>(w), device_error_word());
   FK_CUDA(launched());
   return FK_OK;
 }

@@ -4,6 +4,7 @@
 #include <string.h>
 
 #include <atomic>
+#include <mutex>
 
 #include "fk_common.cuh"
 
@@ -35,16 +36,20 @@ cudaError_t launched(int n) {
   return cudaGetLastError();
 }
 
+// Looked up once per device (std::call_once: safe when several host threads
+// make their first call together). The address belongs to the device's
+// current context; after cudaDeviceReset the library must be reloaded.
 int* device_error_word() {
+  constexpr int kMaxDevices = 64;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
-  static int* cached[64] = {nullptr};
-  if (dev < 0 || dev >= 64) return nullptr;
-  if (!cached[dev]) {
+  if (dev < 0 || dev >= kMaxDevices) return nullptr;
+  static std::once_flag once[kMaxDevices];
+  static int* cached[kMaxDevices] = {nullptr};
+  std::call_once(once[dev], [dev] {
     void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_device_error) != cudaSuccess) return nullptr;
-    cached[dev] = static_cast<int*>(p);
-  }
+    if (cudaGetSymbolAddress(&p, g_device_error) == cudaSuccess) cached[dev] = static_cast<int*>(p);
+  });
   return cached[dev];
 }
 
@@ -60,6 +65,18 @@ __global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ g, 
     v[i] = vi;
     p[i] -= lr_t * mi / (sqrtf(vi) + eps);
   }
+}
+
+// Self-test of the bounded-wait mechanism: waits on an mbarrier that nothing
+// arrives at, `limit` polls at most, so the wait runs out, sets the timeout bit
+// of the error word and the kernel returns normally.
+__global__ void selftest_wait_kernel(int* err, uint32_t limit) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x != 0) return;
+  mbar_init(&bar, 1);
+  fence_mbar_init();
+  mbar_wait_limit(&bar, 0, err, limit);
+  mbar_inval(&bar);
 }
 
 __global__ void axpy_kernel(int64_t n, float a, const float* __restrict__ x, float* __restrict__ y) {
@@ -99,6 +116,18 @@ int fk_device_status(int* status, int clear, void* stream) {
   FK_CUDA(cudaMemcpyAsync(status, word, sizeof(int), cudaMemcpyDeviceToHost, s));
   FK_CUDA(cudaStreamSynchronize(s));
   if (clear) FK_CUDA(cudaMemsetAsync(word, 0, sizeof(int), s));
+  return FK_OK;
+}
+
+int fk_selftest_wait_timeout(int32_t polls, void* stream) {
+  FK_CHECK_ARG(polls >= 1 && polls <= (1 << 20), "fk_selftest_wait_timeout: polls must be in [1, 2^20]");
+  int* word = fk::device_error_word();
+  if (!word) {
+    fk::set_error("fk_selftest_wait_timeout: no device error word");
+    return FK_ERR_CUDA;
+  }
+  fk::selftest_wait_kernel<<<1, 32, 0, static_cast<cudaStream_t>(stream)>>>(word, (uint32_t)polls);
+  FK_CUDA(fk::launched());
   return FK_OK;
 }
 

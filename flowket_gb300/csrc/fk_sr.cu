@@ -16,6 +16,8 @@
 //   4. x = Y alpha / B and theta <- theta - lr x (fk_sr_backmap).
 // For real parameters (the AR network) eps = [Re(E - Ebar); Im(E - Ebar)] and
 // the update solves the real SR system S = Re<O_c^* O_c>, F = Re<O_c^* E_c>.
+#include <mutex>
+
 #include "fk_common.cuh"
 
 namespace fk {
@@ -227,11 +229,88 @@ __global__ void backmap_kernel(const float* __restrict__ a, const float* __restr
   }
 }
 
+// ---------------------------------------------------------------- complex parameters
+// For complex parameters (the RBM family) the SR system is Hermitian:
+// S = O_c^H O_c / B, F = O_c^H E_c / B (optimizer.py:94-114). With
+// O_c = A + iC (A, C real, stored parameter-major [P][B] as o_re, o_im) the
+// push-through identity gives x = O_c^H (T/B + lambda I)^-1 E_c / B with the
+// B x B Hermitian T = O_c O_c^H = (A^T A + C^T C) + i (C^T A - A^T C) (samples
+// as rows here). The 2B x 2B real Gram G of [A | C] holds these blocks:
+// Tr = G11 + G22, Ti = G21 - G12. The Hermitian system T z = e is solved as
+// the real symmetric positive (semi)definite embedding
+//     [[Tr, -Ti], [Ti, Tr]] [zr; zi] = [er; ei],
+// written over G in place: each thread owns the four entries (i, j),
+// (i, n+j), (n+i, j), (n+i, n+j) of one (i, j), reads them and writes them.
+__global__ void hermitian_embed_kernel(double* g, int64_t n) {
+  int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n * n) return;
+  const int64_t i = idx / n, j = idx % n, m = 2 * n;
+  const double g11 = g[i * m + j], g12 = g[i * m + n + j];
+  const double g21 = g[(n + i) * m + j], g22 = g[(n + i) * m + n + j];
+  const double tr = g11 + g22, ti = g21 - g12;
+  g[i * m + j] = tr;
+  g[i * m + n + j] = -ti;
+  g[(n + i) * m + j] = ti;
+  g[(n + i) * m + n + j] = tr;
+}
+
+// x = scale * O_c^H z = scale * [(A zr + C zi) + i (A zi - C zr)] per parameter
+// (A, C parameter-major rows); params (interleaved re, im) -= lr * x when
+// params != NULL, x (interleaved) written to x_out when != NULL. Warp per row.
+__global__ void complex_backmap_kernel(const float* __restrict__ a, const float* __restrict__ c, int64_t P,
+                                       int64_t bsz, const double* __restrict__ z, double scale, float lr,
+                                       float2* __restrict__ params, float2* __restrict__ x_out) {
+  int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (row >= P) return;
+  const float* ar = a + row * bsz;
+  const float* cr = c + row * bsz;
+  double xr = 0.0, xi = 0.0;
+  for (int64_t j = lane; j < bsz; j += 32) {
+    double av = ar[j], cv = cr[j], zr = z[j], zi = z[bsz + j];
+    xr += av * zr + cv * zi;
+    xi += av * zi - cv * zr;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    xr += __shfl_xor_sync(0xffffffffu, xr, o);
+    xi += __shfl_xor_sync(0xffffffffu, xi, o);
+  }
+  if (lane == 0) {
+    float2 xv = make_float2((float)(scale * xr), (float)(scale * xi));
+    if (x_out) x_out[row] = xv;
+    if (params) {
+      float2 p = params[row];
+      params[row] = make_float2(p.x - lr * xv.x, p.y - lr * xv.y);
+    }
+  }
+}
+
 }  // namespace fk
 
 using namespace fk;
 
 extern "C" {
+
+int fk_sr_hermitian_embed(double* gram, int64_t n_samples, void* stream) {
+  FK_CHECK_ARG(gram && n_samples > 0, "fk_sr_hermitian_embed: bad arguments");
+  int64_t nn = n_samples * n_samples;
+  hermitian_embed_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(gram,
+                                                                                                     n_samples);
+  FK_CUDA(launched());
+  return FK_OK;
+}
+
+int fk_sr_complex_backmap(const float* o_re, const float* o_im, int64_t n_params, int64_t n_samples,
+                          const double* z, double scale, float lr, float* params, float* x_out, void* stream) {
+  FK_CHECK_ARG(o_re && o_im && z && n_params > 0 && n_samples > 0 && (params || x_out),
+               "fk_sr_complex_backmap: bad arguments");
+  int64_t threads = n_params * 32;
+  complex_backmap_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      o_re, o_im, n_params, n_samples, z, scale, lr, reinterpret_cast<float2*>(params),
+      reinterpret_cast<float2*>(x_out));
+  FK_CUDA(launched());
+  return FK_OK;
+}
 
 int fk_center_columns(float* y, int64_t rows, int64_t cols, float* mean, void* stream) {
   FK_CHECK_ARG(y && rows >= 0 && cols > 0, "fk_center_columns: bad arguments");
@@ -339,19 +418,28 @@ static __device__ __align__(256) double g_sr_noalloc_scratch[3 * kNoAllocMaxN + 
 // Device address of the scratch array on the current device, looked up once
 // per device with that device current (the host-side name is not a device
 // pointer and must never be handed to a kernel).
+// std::call_once makes the per-device set-up safe when several host threads
+// make their first call on a device at the same time. The address belongs to
+// the device's current context: after cudaDeviceReset the library must be
+// reloaded before this entry point is called again on that device.
+constexpr int kNoAllocMaxDevices = 64;
+
 static double* noalloc_scratch() {
   int dev = 0;
   if (check_cuda(cudaGetDevice(&dev), "cudaGetDevice") != FK_OK) return nullptr;
-  static double* cached[64] = {nullptr};
-  if (dev < 0 || dev >= 64) {
+  if (dev < 0 || dev >= kNoAllocMaxDevices) {
     set_error("fk_sr_solve_noalloc: device index %d out of range", dev);
     return nullptr;
   }
-  if (!cached[dev]) {
+  static std::once_flag once[kNoAllocMaxDevices];
+  static double* cached[kNoAllocMaxDevices] = {nullptr};
+  static cudaError_t lookup[kNoAllocMaxDevices];
+  std::call_once(once[dev], [dev] {
     void* p = nullptr;
-    if (check_cuda(cudaGetSymbolAddress(&p, g_sr_noalloc_scratch), "cudaGetSymbolAddress") != FK_OK) return nullptr;
-    cached[dev] = static_cast<double*>(p);
-  }
+    lookup[dev] = cudaGetSymbolAddress(&p, g_sr_noalloc_scratch);
+    if (lookup[dev] == cudaSuccess) cached[dev] = static_cast<double*>(p);
+  });
+  if (check_cuda(lookup[dev], "cudaGetSymbolAddress") != FK_OK) return nullptr;
   return cached[dev];
 }
 

@@ -260,7 +260,15 @@ class RBM:
     """flowket.machines.RBM (machines/rbm.py:35-48): complex RBM with alpha*N
     hidden units, log psi = a.s + sum_j lncosh(b_j + W_j.s). Parameters are
     one float32 tensor of interleaved complex values [a | b | W]; real and
-    imaginary parts are initialised N(0, stddev) (rbm.py:23)."""
+    imaginary parts are initialised N(0, stddev) (rbm.py:23).
+
+    The machine protocol of the driver: ``forward`` (log psi), ``backward``
+    (the loss gradient with respect to the stored (re, im) pairs),
+    ``log_derivatives_split`` (per-sample complex O for SR) and
+    ``local_energy`` (E_loc from the operator's enumeration, ratios from
+    incremental theta updates)."""
+
+    is_complex = True
 
     def __init__(self, hilbert_state_shape, alpha=1, stddev=1.0, use_float64_ops=False, seed=0, device=None,
                  params=None):
@@ -282,8 +290,15 @@ class RBM:
     def params_updated(self):
         pass
 
+    def count_params(self):
+        return self.num_params
+
+    def kernel_params(self):
+        """The dense [a | b | W] parameters the RBM kernels read."""
+        return self.params
+
     def complex_params(self):
-        c = torch.view_as_complex(self.params.view(-1, 2))
+        c = torch.view_as_complex(self.kernel_params().view(-1, 2))
         n, m = self.n, self.m
         return {"a": c[:n], "b": c[n:n + m], "W": c[n + m:].view(n, m)}
 
@@ -296,9 +311,16 @@ class RBM:
     def log_psi_pairs(self, spins):
         s = self._spins(spins)
         out = torch.empty((s.shape[0], 2), dtype=torch.float32, device=self.device)
-        _lib.call("fk_rbm_log_psi", _lib.ptr(self.params), self.n, self.m, _lib.ptr(s), s.shape[0], _lib.ptr(out),
-                  _lib.stream_ptr())
+        _lib.call("fk_rbm_log_psi", _lib.ptr(self.kernel_params()), self.n, self.m, _lib.ptr(s), s.shape[0],
+                  _lib.ptr(out), _lib.stream_ptr())
         return out
+
+    def forward(self, spins, mode=_lib.FK_AR2D_INFER, with_cond=False, workspace=None):
+        """(log_psi float32 (B, 2) (re, im), None, None): the RBM keeps no
+        activations (the adjoint recomputes theta)."""
+        if with_cond:
+            raise ValueError("an RBM has no autoregressive conditionals")
+        return self.log_psi_pairs(spins), None, None
 
     def log_psi(self, spins):
         lp = self.log_psi_pairs(spins)
@@ -312,51 +334,134 @@ class RBM:
     def local_energy(self, operator, spins):
         flips, mel, use, s = operator.enumerate(spins)
         local = torch.empty((s.shape[0], 2), dtype=torch.float64, device=self.device)
-        _lib.call("fk_rbm_local_energy", _lib.ptr(self.params), self.n, self.m, _lib.ptr(s), s.shape[0],
+        _lib.call("fk_rbm_local_energy", _lib.ptr(self.kernel_params()), self.n, self.m, _lib.ptr(s), s.shape[0],
                   _lib.ptr(flips), _lib.ptr(mel), _lib.ptr(use), mel.shape[0], _lib.ptr(local), _lib.stream_ptr())
         return local
 
-    def log_derivatives_split(self, spins):
-        """(O_re, O_im) parameter-major (num_complex_params, B)."""
-        s = self._spins(spins)
+    def _dense_log_derivatives(self, s):
         b = s.shape[0]
-        o_re = torch.empty((self.num_complex_params, b), dtype=torch.float32, device=self.device)
+        o_re = torch.empty((self.n + self.m + self.n * self.m, b), dtype=torch.float32, device=self.device)
         o_im = torch.empty_like(o_re)
-        _lib.call("fk_rbm_log_derivatives", _lib.ptr(self.params), self.n, self.m, _lib.ptr(s), b, _lib.ptr(o_re),
-                  _lib.ptr(o_im), _lib.stream_ptr())
+        _lib.call("fk_rbm_log_derivatives", _lib.ptr(self.kernel_params()), self.n, self.m, _lib.ptr(s), b,
+                  _lib.ptr(o_re), _lib.ptr(o_im), _lib.stream_ptr())
         return o_re, o_im
+
+    def log_derivatives_split(self, spins):
+        """(O_re, O_im) parameter-major (num_complex_params, B): O_k = d log psi / d theta_k
+        (holomorphic) for the trainable complex parameters."""
+        return self._dense_log_derivatives(self._spins(spins))
 
     def log_derivatives(self, spins):
         o_re, o_im = self.log_derivatives_split(spins)
         return torch.complex(o_re, o_im)
 
+    def backward(self, spins, seeds, saved=None, per_sample=False):
+        """Gradient of sum_b (w_re Re log psi_b + w_im Im log psi_b) with respect
+        to the stored (re, im) parameter pairs (num_params,) float32."""
+        if per_sample:
+            raise ValueError("RBM: per-sample rows are log_derivatives_split (complex O)")
+        s = self._spins(spins)
+        b = s.shape[0]
+        w = torch.as_tensor(seeds, dtype=torch.float32, device=self.device).reshape(b, 2).contiguous()
+        o_re, o_im = self.log_derivatives_split(s)
+        grad = torch.empty(self.num_params, dtype=torch.float32, device=self.device)
+        _lib.call("fk_complex_param_gradient", _lib.ptr(o_re), _lib.ptr(o_im), self.num_params // 2, b, _lib.ptr(w),
+                  _lib.ptr(grad), _lib.stream_ptr())
+        return grad
+
+
+def rbm_sym_tied_index(shape, alpha):
+    """Index map dense -> bare of RBMSym (machines/rbm.py:51-65 with
+    layers/complex/dense.py:53-85): bare = [a (1) | b (alpha) | W (shape + (alpha,))];
+    dense = [a (N) | b (alpha*N) | W (N x alpha*N)], kernel column u*T + t the
+    bare kernel rolled by translation t (itertools order over the lattice),
+    bias u*N + t = bare bias u, every visible bias = the single bare a
+    (Flatten -> sum -> ComplexDense(1) in rbm.py:59-62)."""
+    import itertools
+    n = int(np.prod(shape))
+    dims = tuple(range(len(shape)))
+    w_idx = torch.arange(n * alpha, dtype=torch.int64).reshape(tuple(shape) + (alpha,))
+    trans = [torch.roll(w_idx, t, dims) for t in itertools.product(*[range(d) for d in shape])]
+    w_map = torch.stack(trans, dim=-1).reshape(n, alpha * len(trans)) + 1 + alpha
+    b_map = torch.arange(alpha, dtype=torch.int64).repeat_interleave(n) + 1
+    a_map = torch.zeros(n, dtype=torch.int64)
+    return torch.cat([a_map, b_map, w_map.reshape(-1)])
+
 
 class RBMSym(RBM):
     """flowket.machines.RBMSym (machines/rbm.py:51-65): translation-invariant
-    kernel (shape + (alpha,)), a single visible bias; evaluated through the
-    dense RBM kernels after expanding every translation of the bare kernel
-    (layers/complex/dense.py:53-85: column f*T + t, bias repeated)."""
+    kernel (shape + (alpha,)), one hidden bias per feature and a single
+    visible bias. The trainable ``params`` are the bare complex values
+    [a (1) | b (alpha) | W (shape + (alpha,))] interleaved (re, im); the
+    kernels evaluate the dense RBM, expanded from them on the device
+    (fk_gather_complex) whenever they change, and the per-sample O of a bare
+    parameter is the sum of its dense copies' (fk_segment_sum_rows)."""
 
-    def __init__(self, hilbert_state_shape, alpha=1, stddev=1.0, use_float64_ops=False, seed=0, device=None):
+    def __init__(self, hilbert_state_shape, alpha=1, stddev=1.0, use_float64_ops=False, seed=0, device=None,
+                 params=None):
+        if use_float64_ops:
+            raise ValueError("the GPU RBM computes in complex64 (use_float64_ops=False)")
         shape = tuple(int(x) for x in hilbert_state_shape)
-        n = int(np.prod(shape))
-        gen = torch.Generator().manual_seed(seed)
-        bare_w = torch.complex(torch.randn(shape + (alpha,), generator=gen, dtype=torch.float64) * stddev,
-                               torch.randn(shape + (alpha,), generator=gen, dtype=torch.float64) * stddev)
-        bare_b = torch.complex(torch.randn(alpha, generator=gen, dtype=torch.float64) * stddev,
-                               torch.randn(alpha, generator=gen, dtype=torch.float64) * stddev)
-        bare_a = torch.complex(torch.randn(1, generator=gen, dtype=torch.float64) * stddev,
-                               torch.randn(1, generator=gen, dtype=torch.float64) * stddev)
-        self.bare = {"W": bare_w, "b": bare_b, "a": bare_a}
-        import itertools
-        dims = tuple(range(len(shape)))
-        trans = [torch.roll(bare_w, t, dims) for t in itertools.product(*[range(d) for d in shape])]
-        w = torch.stack(trans, dim=-1).reshape(n, alpha * len(trans))
-        b = bare_b.repeat_interleave(n)
-        a = bare_a.expand(n)
-        full = torch.cat([a, b, w.reshape(-1)])
-        super().__init__(shape, alpha=alpha, device=device,
-                         params=torch.view_as_real(full).reshape(-1).to(torch.float32))
+        self.hilbert_state_shape = shape
+        self.n = int(np.prod(shape))
+        self.alpha = int(alpha)
+        self.m = self.alpha * self.n
+        self.device = _device(device)
+        n_bare = 1 + self.alpha + self.n * self.alpha
+        if params is None:
+            gen = torch.Generator().manual_seed(seed)
+            bare_w = torch.complex(torch.randn(shape + (alpha,), generator=gen, dtype=torch.float64) * stddev,
+                                   torch.randn(shape + (alpha,), generator=gen, dtype=torch.float64) * stddev)
+            bare_b = torch.complex(torch.randn(alpha, generator=gen, dtype=torch.float64) * stddev,
+                                   torch.randn(alpha, generator=gen, dtype=torch.float64) * stddev)
+            bare_a = torch.complex(torch.randn(1, generator=gen, dtype=torch.float64) * stddev,
+                                   torch.randn(1, generator=gen, dtype=torch.float64) * stddev)
+            params = torch.view_as_real(torch.cat([bare_a, bare_b, bare_w.reshape(-1)])).reshape(-1)
+        self.params = torch.as_tensor(params, dtype=torch.float32).reshape(-1).to(self.device).contiguous()
+        assert self.params.numel() == 2 * n_bare
+        self.num_complex_params = n_bare
+        self.num_params = 2 * n_bare
+        self.num_dense_complex_params = self.n + self.m + self.n * self.m
+        tied = rbm_sym_tied_index(shape, self.alpha)
+        self._tied = tied.to(torch.int32).to(self.device)
+        order = torch.argsort(tied, stable=True)
+        counts = torch.bincount(tied, minlength=n_bare)
+        offsets = torch.zeros(n_bare + 1, dtype=torch.int64)
+        offsets[1:] = torch.cumsum(counts, 0)
+        self._seg_rows = order.to(torch.int32).to(self.device)
+        self._seg_offsets = offsets.to(self.device)
+        self._dense = torch.empty(2 * self.num_dense_complex_params, dtype=torch.float32, device=self.device)
+        self._dense_version = None
+        self._manual_version = 0
+
+    @property
+    def bare(self):
+        c = torch.view_as_complex(self.params.view(-1, 2)).detach().cpu().to(torch.complex128)
+        al = self.alpha
+        return {"a": c[:1], "b": c[1:1 + al], "W": c[1 + al:].view(self.hilbert_state_shape + (al,))}
+
+    def params_updated(self):
+        self._manual_version += 1
+
+    def kernel_params(self):
+        ver = (self.params._version, self._manual_version)
+        if self._dense_version != ver:
+            _lib.call("fk_gather_complex", _lib.ptr(self.params), _lib.ptr(self._tied), self.num_dense_complex_params,
+                      _lib.ptr(self._dense), _lib.stream_ptr())
+            self._dense_version = ver
+        return self._dense
+
+    def log_derivatives_split(self, spins):
+        s = self._spins(spins)
+        d_re, d_im = self._dense_log_derivatives(s)
+        b = s.shape[0]
+        o_re = torch.empty((self.num_complex_params, b), dtype=torch.float32, device=self.device)
+        o_im = torch.empty_like(o_re)
+        st = _lib.stream_ptr()
+        for src, dst in ((d_re, o_re), (d_im, o_im)):
+            _lib.call("fk_segment_sum_rows", _lib.ptr(src), _lib.ptr(self._seg_offsets), _lib.ptr(self._seg_rows),
+                      self.num_complex_params, b, _lib.ptr(dst), st)
+        return o_re, o_im
 
 
 def _ar2d_forward_connections(machine, configs, owner, cflips, n_rows, base_saved, base_batch, chunk=1 << 17):

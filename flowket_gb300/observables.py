@@ -70,7 +70,11 @@ class Observable(BaseObservable):
     def local_values(self, machine, configurations, log_psi=None, base_saved=None):
         """E_loc per sample ((B, 2) float64). With `base_saved` (the sampler's
         or a FK_AR2D_SAVE forward's workspace for these configurations) the
-        connected configurations reuse the base activations (causal reuse)."""
+        connected configurations reuse the base activations (causal reuse).
+        Machines with their own local-energy kernel (the RBM family: ratios
+        from incremental theta updates) evaluate it directly."""
+        if hasattr(machine, "local_energy"):
+            return machine.local_energy(self.operator, configurations)
         spins, mel, bf, rows = self.connections(configurations)
         b = spins.shape[0]
         if log_psi is None:

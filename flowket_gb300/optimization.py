@@ -70,9 +70,13 @@ class VariationalMonteCarlo(MiniBatchGenerator):
         self.causal_reuse = True
 
     def _sample(self):
-        out = self.sampler.sample()
-        if not isinstance(out, tuple):
-            return out, None, None
+        """(spins, log psi or None, activation workspace or None) from the
+        sampler's ``sample_with_log_psi()``, or ``next(sampler)`` for a plain
+        iterator (the reference driver's call, variational_monte_carlo.py:46)."""
+        if hasattr(self.sampler, "sample_with_log_psi"):
+            out = self.sampler.sample_with_log_psi()
+        else:
+            out = (next(self.sampler), None, None)
         if getattr(self.sampler, "machine", self.model) is not self.model:
             # drawn from another machine (the base of a symmetrised ensemble,
             # experiments/run_evaluation.py:12-24): log psi and the local
@@ -122,7 +126,10 @@ class VariationalMonteCarlo(MiniBatchGenerator):
         return stats
 
     def finish_step(self):
-        torch.cuda.current_stream().synchronize()
+        """Waits for the step, raises if a kernel recorded a failure (a
+        timed-out device wait or a non-finite energy) and publishes the
+        energy, variance, local energies and stage times."""
+        _lib.check_device("VariationalMonteCarlo.step")
         ev = self._events
         self.times = {"sampling": ev[0].elapsed_time(ev[1]), "local_energy": ev[1].elapsed_time(ev[2]),
                       "gradient": ev[2].elapsed_time(ev[3]), "update": ev[3].elapsed_time(ev[4])}

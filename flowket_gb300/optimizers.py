@@ -40,13 +40,21 @@ class ComplexValuesStochasticReconfiguration:
     """Stochastic reconfiguration (optimizers/stochastic_reconfiguration/optimizer.py:14-183)
     in sample space on the GPU.
 
-    For a machine with real parameters and complex log psi (the AR network) the
-    update solves S x = F with S = Re<O_c^* O_c> + diag_shift I and
-    F = Re<O_c^* (E - Ebar)>, via the 2B x 2B Gram of Y = [Re O_c | Im O_c]:
-    alpha = (Y^T Y / B + diag_shift I)^-1 [Re E_c; Im E_c], x = Y alpha / B,
-    theta <- theta - lr x. The solve is FP64 CG with the reference's tolerance
-    rule (linear_equations.py:34-137); ``iterative_solver=False`` runs CG to
-    1e-10 instead of a Cholesky factorisation."""
+    Complex parameters (the RBM family, the reference's own use of SR,
+    complex_values_optimizer.py:28-82): S = <O_c^* O_c> + diag_shift I,
+    F = <O_c^* (E - Ebar)>, solved through the B x B Hermitian Gram
+    T = O_c O_c^H: z = (T / B + diag_shift I)^-1 (E - Ebar), x = O_c^H z / B,
+    theta <- theta - lr x (fk_sr_hermitian_embed, fk_sr_solve on the real
+    embedding, fk_sr_complex_backmap).
+
+    Real parameters with a complex log psi (the AR network): S = Re<O_c^* O_c>
+    + diag_shift I and F = Re<O_c^* (E - Ebar)>, via the 2B x 2B Gram of
+    Y = [Re O_c | Im O_c]: alpha = (Y^T Y / B + diag_shift I)^-1 [Re E_c; Im E_c],
+    x = Y alpha / B.
+
+    The solve is FP64 CG with the reference's tolerance rule
+    (linear_equations.py:34-137); ``iterative_solver=False`` runs CG to 1e-10
+    instead of a Cholesky factorisation."""
 
     def __init__(self, machine, predictions_jacobian=None, lr=0.01, diag_shift=0.05, iterative_solver=True,
                  compute_jvp_instead_of_full_jacobian=False, use_cholesky=True, conjugate_gradient_tol=1e-3,
@@ -72,17 +80,51 @@ class ComplexValuesStochasticReconfiguration:
         return self._buf[n]
 
     def update(self, spins, local, w, saved):
-        x = self.direction(spins, local, saved)
         m = self.machine
-        _lib.call("fk_axpy", m.num_params, -self.lr, _lib.ptr(x), _lib.ptr(m.params), _lib.stream_ptr())
+        if getattr(m, "is_complex", False):
+            self._complex_solve(spins, local, self.lr, m.params, None)
+        else:
+            x = self.direction(spins, local, saved)
+            _lib.call("fk_axpy", m.num_params, -self.lr, _lib.ptr(x), _lib.ptr(m.params), _lib.stream_ptr())
         m.params_updated()
         self.iterations += 1
         self.last_stats = self._buf[2 * spins.shape[0]]["stats"]
 
-    def direction(self, spins, local, saved):
-        """The solution x of the SR system (no update), for tests."""
-        lr, self.lr = self.lr, 0.0
+    def _max_iter(self, n, n_complex_params):
+        if self.iterative_solver:
+            return self.max_iter
+        # T / B has rank <= P (complex), its real embedding <= 2P: CG on the
+        # shifted system terminates after at most 2P + 1 distinct eigenvalues
+        return min(self.max_iter, 4 * n_complex_params + 20, n + 20)
+
+    def _complex_solve(self, spins, local, lr, params, x_out):
         m = self.machine
+        b = spins.shape[0]
+        o_re, o_im = m.log_derivatives_split(spins)
+        p = o_re.shape[0]
+        st = _lib.stream_ptr()
+        _lib.call("fk_center_columns", _lib.ptr(o_re), p, b, None, st)
+        _lib.call("fk_center_columns", _lib.ptr(o_im), p, b, None, st)
+        n = 2 * b
+        bf = self._buffers(n, m.device)
+        _lib.call("fk_sr_gram", _lib.ptr(o_re), _lib.ptr(o_im), p, b, _lib.ptr(bf["gram"]), n * n, st)
+        _lib.call("fk_sr_hermitian_embed", _lib.ptr(bf["gram"]), b, st)
+        bf["rhs"][:b] = local[:, 0] - local[:, 0].mean()
+        bf["rhs"][b:] = local[:, 1] - local[:, 1].mean()
+        _lib.call("fk_sr_solve", _lib.ptr(bf["gram"]), n, 1.0 / b, self.diag_shift, _lib.ptr(bf["rhs"]), self.tol,
+                  self._max_iter(n, p), _lib.ptr(bf["alpha"]), _lib.ptr(bf["stats"]), _lib.ptr(bf["ws"]),
+                  bf["ws"].numel(), st)
+        _lib.call("fk_sr_complex_backmap", _lib.ptr(o_re), _lib.ptr(o_im), p, b, _lib.ptr(bf["alpha"]), 1.0 / b,
+                  lr, _lib.ptr(params), _lib.ptr(x_out), st)
+
+    def direction(self, spins, local, saved=None):
+        """The solution x of the SR system (no update): float32 (num_params,);
+        for complex parameters interleaved (re, im)."""
+        m = self.machine
+        if getattr(m, "is_complex", False):
+            x = torch.empty(m.num_params, dtype=torch.float32, device=m.device)
+            self._complex_solve(spins, local, 0.0, None, x)
+            return x
         b = spins.shape[0]
         ones = torch.zeros((b, 2), dtype=torch.float32, device=m.device)
         ones[:, 0] = 1
@@ -105,7 +147,6 @@ class ComplexValuesStochasticReconfiguration:
         x = torch.empty(p, dtype=torch.float32, device=m.device)
         _lib.call("fk_sr_backmap", _lib.ptr(o_re), _lib.ptr(o_im), p, b, _lib.ptr(bf["alpha"]), 1.0 / b, 0.0, None,
                   _lib.ptr(x), st)
-        self.lr = lr
         return x
 
 

@@ -12,7 +12,11 @@
 * ``MetropolisHastingsIndependent``: the learned independent proposal (an
   autoregressive network sampled exactly) with the exact acceptance
   min(1, |psi(s')|^2 q(s) / (|psi(s)|^2 q(s'))).
-__next__ returns an int8 CUDA tensor (B, *shape) of +-1.
+__next__ returns an int8 CUDA tensor (B, *shape) of +-1. As in the reference,
+the Metropolis-Hastings samplers keep their chain state in the attribute
+``sample`` (samplers/metropolis_hastings.py:28); every sampler also has
+``sample_with_log_psi()`` -> (spins, log psi or None, activation workspace or
+None), the call the VMC driver makes.
 """
 import copy
 
@@ -73,6 +77,12 @@ class FastAutoregressiveSampler(Sampler):
         self.last_log_psi = lp
         self.last_workspace = ws
         return spins.view(b, h, w), lp, ws
+
+    def sample_with_log_psi(self):
+        """(spins, log_psi, activation workspace) of one draw: the driver's
+        sampler protocol (the workspace lets the local energy reuse the base
+        activations and the adjoint skip a forward)."""
+        return self.sample()
 
     def __next__(self):
         return self.sample()[0]
@@ -153,7 +163,7 @@ class MetropolisHastingsSampler(Sampler):
         out = torch.empty((self.num_of_chains, spc, m.n), dtype=torch.int8, device=m.device)
         self.accepted.zero_()
         h, w = self._grid()
-        _lib.call("fk_rbm_mh_sweeps", _lib.ptr(m.params), m.n, m.m, h, w, self.kind, _lib.ptr(self.sample),
+        _lib.call("fk_rbm_mh_sweeps", _lib.ptr(m.kernel_params()), m.n, m.m, h, w, self.kind, _lib.ptr(self.sample),
                   _lib.ptr(self.log_psi), self.num_of_chains, warm, spc, self.unused_sampels, self.seed, self.sweep,
                   _lib.ptr(out), _lib.ptr(self.accepted), _lib.stream_ptr())
         self.sweep += warm + spc * (self.unused_sampels + 1)
@@ -345,5 +355,16 @@ class MetropolisHastingsIndependent(Sampler):
         for i in range(spc):
             self.step()
             out[:, i] = self.sample
-        self.acceptance_ratio = int(self.accepted.item()) / self.batch_size
+        self._accepted_pending = (self.accepted, self.batch_size)
         return out.view((self.batch_size,) + tuple(self.input_size))
+
+    def sample_with_log_psi(self):
+        return self.__next__(), None, None
+
+    def update_acceptance_ratio(self):
+        acc, total = self._accepted_pending
+        self.acceptance_ratio = int(acc.item()) / total
+        return self.acceptance_ratio
+
+    def calc_r_hat_value(self, estimated_values):
+        return r_hat_and_correlations(estimated_values, self.num_of_chains)

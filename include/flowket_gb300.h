@@ -35,8 +35,18 @@ extern "C" {
 #define FK_AR2D_SAVE 1          /* forward keeps every activation for the adjoint */
 
 const char* fk_last_error(void);
-/* Reads (and optionally clears) the device error word set by bounded waits. */
+/* Device error word: bits set by kernels instead of faulting or hanging. */
+#define FK_STATUS_TIMEOUT 1     /* a bounded device-side wait gave up (the kernel unwound) */
+#define FK_STATUS_NONFINITE 2   /* a non-finite energy statistic (the reference raises on a
+                                   non-finite wave function, samplers/metropolis_hastings.py:103-105) */
+/* Reads (and optionally clears) the device error word of the current device:
+ * synchronises `stream` and writes the FK_STATUS_* bits set since the last clear. */
 int fk_device_status(int* status, int clear, void* stream);
+/* Self-test of the failure detection (no reference counterpart): one kernel
+ * waits on an mbarrier that nothing arrives at, at most `polls` polls
+ * (1..2^20), so the wait runs out, FK_STATUS_TIMEOUT is set in the device
+ * error word and the kernel returns normally; the context stays usable. */
+int fk_selftest_wait_timeout(int32_t polls, void* stream);
 /* Library build string (arch, version). */
 const char* fk_version(void);
 /* Number of kernel launches this library has issued in this process. */
@@ -218,6 +228,23 @@ int fk_mh_hamiltonian_accept(int8_t* chains, float* lp_chain, const int8_t* cand
                              int32_t n_sites, uint64_t seed, uint64_t sweep, unsigned long long* accepted,
                              void* stream);
 
+/* Tied complex parameters (RBMSym, machines/rbm.py:51-65 with
+ * layers/complex/dense.py:53-85): dst[i] = src[index[i]] over interleaved
+ * complex values (bare -> dense expansion). */
+int fk_gather_complex(const float* src, const int32_t* index, int64_t n, float* dst, void* stream);
+/* out[k][c] = sum_{q = offsets[k]}^{offsets[k+1]-1} in[rows[q]][c] (float32,
+ * fixed order): per-sample log-derivative rows of the dense copies summed
+ * into the bare parameter they copy. n_out <= 65535. */
+int fk_segment_sum_rows(const float* in, const int64_t* offsets, const int32_t* rows, int64_t n_out, int64_t cols,
+                        float* out, void* stream);
+/* Loss gradient for complex parameters stored as (re, im) pairs
+ * (optimization/loss.py:4-5 through layers/complex/base_layer.py:18-35):
+ * from per-sample O = d log psi / d theta, parameter-major [P][batch] re and im,
+ * and the seeds w [batch][2] of sum_b (w_re Re log psi_b + w_im Im log psi_b):
+ * grad[k] = (sum_b w_re Re O + w_im Im O, sum_b w_im Re O - w_re Im O). */
+int fk_complex_param_gradient(const float* o_re, const float* o_im, int64_t n_params, int64_t batch, const float* w,
+                              float* grad, void* stream);
+
 /* ------------------------------------------------------------------ SR (kernel d)
  * Sample-space stochastic reconfiguration
  * (optimizers/stochastic_reconfiguration/optimizer.py:33-124): per-sample
@@ -247,6 +274,17 @@ int fk_sr_solve(const double* gram, int64_t n, double scale, double shift, const
  * from an earlier call is read; results equal fk_sr_solve's. */
 int fk_sr_solve_noalloc(const double* gram, int64_t n, double scale, double shift, const double* rhs, double tol,
                         int32_t max_iter, double* x, double* stats, void* stream);
+/* Complex-parameter SR (optimizer.py:94-114 with complex_values_optimizer.py:28-82):
+ * turns the 2n x 2n Gram of [Re O_c | Im O_c] (fk_sr_gram with o_im, n =
+ * n_samples) in place into the real symmetric embedding [[Tr, -Ti], [Ti, Tr]]
+ * of the Hermitian sample-space Gram T = O_c O_c^H, so that fk_sr_solve on it
+ * with rhs [Re e; Im e] solves T z = e. */
+int fk_sr_hermitian_embed(double* gram, int64_t n_samples, void* stream);
+/* x = scale * O_c^H z for complex parameters (z = [Re z; Im z], 2 n_samples):
+ * x interleaved (re, im) [n_params][2]; params (interleaved) -= lr x when
+ * params != NULL, x written to x_out when != NULL. */
+int fk_sr_complex_backmap(const float* o_re, const float* o_im, int64_t n_params, int64_t n_samples,
+                          const double* z, double scale, float lr, float* params, float* x_out, void* stream);
 /* x = scale * Y alpha (complex_values_optimizer.py:48-58 update direction);
  * params -= lr * x when params != NULL; x written to x_out when != NULL. */
 int fk_sr_backmap(const float* o_re, const float* o_im, int64_t n_params, int64_t n_samples, const double* alpha,

@@ -50,3 +50,32 @@ def rbm_log_derivatives(params, spins):
     t = np.tanh(theta)
     o_w = (s[:, :, None] * t[:, None, :]).reshape(s.shape[0], -1)
     return np.concatenate([s.astype(np.complex128), t, o_w], axis=1)
+
+
+def rbm_sym_bare_vector(bare):
+    """The bare RBMSym parameters as one complex vector [a (1) | b (alpha) | W (shape + (alpha,))]."""
+    return np.concatenate([np.ravel(bare["a"])[:1], np.ravel(bare["b"]), np.ravel(bare["W"])]).astype(np.complex128)
+
+
+def rbm_sym_bare_dict(vec, shape, alpha):
+    vec = np.asarray(vec, dtype=np.complex128)
+    return {"a": vec[0], "b": vec[1:1 + alpha], "W": vec[1 + alpha:].reshape(tuple(shape) + (alpha,))}
+
+
+def rbm_sym_log_derivatives(bare, shape, spins):
+    """O_k = d log psi / d bare_k of RBMSym (rbm.py:51-65). The dense
+    parameters are linear in the bare ones (copies), so by the chain rule
+    d log psi / d bare_k = sum_j O_dense_j * d dense_j / d bare_k, with
+    d dense / d bare_k the expansion of the k-th unit vector."""
+    alpha = np.asarray(bare["b"]).shape[0]
+    vec = rbm_sym_bare_vector(bare)
+    full = rbm_sym_full_params(bare, shape)
+    o_dense = rbm_log_derivatives(full, spins)
+    cols = []
+    for k in range(vec.shape[0]):
+        e = np.zeros_like(vec)
+        e[k] = 1.0
+        u = rbm_sym_full_params(rbm_sym_bare_dict(e, shape, alpha), shape)
+        cols.append(np.concatenate([u["a"], u["b"], u["W"].reshape(-1)]))
+    jac = np.stack(cols, axis=1)
+    return o_dense @ jac

@@ -4,9 +4,13 @@ is not allowed where they solve). It keeps its conjugate-gradient scratch in a
 fixed array inside the library (n <= 8192) and must give the same answer as
 fk_sr_solve, which takes a caller-provided workspace.
 
-This file is collected last on purpose; it runs the entry point alone in a
-fresh process as well as after the other tests."""
-import ctypes
+This file is collected last on purpose, so that a run stopping at the first
+failure has run every other test before it. It checks the entry point after
+the other tests (in the shared session) and as the first library call of a
+fresh child process, where the per-device lookup of the array runs."""
+import os
+import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -65,3 +69,37 @@ def test_noalloc_solve_rejects_sizes_beyond_its_scratch(cuda):
                                  _lib.stream_ptr())
     assert st == -1
     assert b"8192" in lib.fk_last_error()
+
+
+_FRESH = r"""
+import sys
+import numpy as np
+import torch
+sys.path.insert(0, sys.argv[1])
+from flowket_gb300 import _lib
+n, p = 256, 1000
+g = torch.Generator(device="cuda").manual_seed(0)
+y = torch.randn((p, n), generator=g, device="cuda", dtype=torch.float64)
+gram = (y.T @ y).contiguous()
+res = []
+for k in range(2):
+    rhs = torch.randn(n, generator=g, device="cuda", dtype=torch.float64)
+    x0 = torch.empty(n, dtype=torch.float64, device="cuda")
+    _lib.call("fk_sr_solve_noalloc", _lib.ptr(gram), n, 1.0 / p, 0.05, _lib.ptr(rhs), 1e-10, 300, _lib.ptr(x0),
+              None, _lib.stream_ptr())
+    ws = torch.empty(_lib.load().fk_sr_solve_workspace_bytes(n), dtype=torch.uint8, device="cuda")
+    x1 = torch.empty(n, dtype=torch.float64, device="cuda")
+    _lib.call("fk_sr_solve", _lib.ptr(gram), n, 1.0 / p, 0.05, _lib.ptr(rhs), 1e-10, 300, _lib.ptr(x1), None,
+              _lib.ptr(ws), ws.numel(), _lib.stream_ptr())
+    torch.cuda.synchronize()
+    res.append(float((x0 - x1).abs().max() / x1.abs().max()))
+print("max-rel", max(res))
+assert max(res) < 1e-8, res
+"""
+
+
+def test_noalloc_solve_as_first_call_of_a_fresh_process(cuda):
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", _FRESH, root], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "max-rel" in r.stdout
