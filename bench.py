@@ -54,7 +54,13 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--fp32-steps", type=int, default=2)
+    p.add_argument("--fp32-steps", type=int, default=10)
+    p.add_argument("--matched-steps", type=int, default=150,
+                   help="training steps of each path in the bench line's matched-energy leg (0: skip)")
+    p.add_argument("--matched-batch", type=int, default=1024)
+    p.add_argument("--matched-samples", type=int, default=16384)
+    p.add_argument("--cpu-samples", type=int, default=128,
+                   help="samples of one VMC step per timed CPU step (reference arm and cpu_baseline)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--case", default="vmc", choices=["vmc", "forward", "energy4x4", "vmc16", "ising12", "matched"],
                    help="forward: only the batched AR2D forward of the local-energy stage on --configs "
@@ -130,14 +136,12 @@ def vmc16_case(args):
     print(json.dumps(out), flush=True)
 
 
-def matched_case(args):
-    """The metric's "at matched energy": the bench workload (TFIM 10x10 PBC
-    h=3, depth 10, 32 channels, weight norm) trained from the same seeded
-    parameters for `--train-steps` VMC steps of `--batch` samples with Adam
-    (lr 1e-3) on the BF16 path and on the plain FP32 path; each trained model's
-    energy is then estimated from `--samples` fresh samples of its own
-    sampler. Reports both energies, their relative difference and the
-    training throughput of each path."""
+def train_and_evaluate(precision, steps, batch, eval_samples, lr=1e-3):
+    """The bench workload (TFIM 10x10 PBC h=3, depth 10, 32 channels, weight
+    norm) trained from the seeded initial parameters for `steps` VMC steps of
+    `batch` samples with Adam on one path, then its energy estimated from
+    `eval_samples` fresh samples of its own sampler: energy, standard error,
+    local-energy variance, training time and throughput."""
     from flowket_gb300.machines import ConvNetAutoregressive2D
     from flowket_gb300.observables import Observable, energy_stats
     from flowket_gb300.operators import Ising
@@ -145,34 +149,53 @@ def matched_case(args):
     from flowket_gb300.optimizers import Adam
     from flowket_gb300.samplers import FastAutoregressiveSampler
     op = Ising(h=H_FIELD, hilbert_state_shape=SHAPE, pbc=True)
-    out = {"case": "matched", "workload": WORKLOAD, "train_steps": args.train_steps, "batch": args.batch,
-           "eval_samples": args.samples}
+    m = ConvNetAutoregressive2D(SHAPE, DEPTH, CHANNELS, weights_normalization=True, precision=precision, seed=0)
+    vmc = VariationalMonteCarlo(m, op, FastAutoregressiveSampler(m, batch, seed=1234))
+    opt = Adam(m, lr=lr)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(steps):
+        vmc.step(opt, sync=False)
+    b.record()
+    torch.cuda.synchronize()
+    if steps:
+        vmc.finish_step()
+    train_ms = a.elapsed_time(b)
+    sampler = FastAutoregressiveSampler(m, min(eval_samples, 8192), seed=777)
+    obs = Observable(op)
+    loc = []
+    for _ in range(max(1, eval_samples // sampler.batch_size)):
+        spins, lp, saved = sampler.sample()
+        loc.append(obs.local_values(m, spins, log_psi=lp, base_saved=saved).clone())
+    stats, _ = energy_stats(torch.cat(loc))
+    st = stats.tolist()
+    n = sum(x.shape[0] for x in loc)
+    return {"energy": st[0], "stderr": math.sqrt(st[2] / n), "local_energy_variance": st[2], "eval_samples": n,
+            "train_steps": steps, "train_ms": train_ms,
+            "train_samples_per_s": steps * batch / (train_ms / 1e3) if steps else None}
+
+
+def matched_summary(steps, batch, eval_samples):
+    out = {"train_steps": steps, "batch": batch, "eval_samples": eval_samples, "optimizer": "Adam lr 1e-3",
+           "init": "same seeded parameters and sampler seed for both paths"}
     for prec in ("bf16", "fp32"):
-        m = ConvNetAutoregressive2D(SHAPE, DEPTH, CHANNELS, weights_normalization=True, precision=prec, seed=0)
-        vmc = VariationalMonteCarlo(m, op, FastAutoregressiveSampler(m, args.batch, seed=1234))
-        opt = Adam(m, lr=1e-3)
-        torch.cuda.synchronize()
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record()
-        for _ in range(args.train_steps):
-            vmc.step(opt, sync=False)
-        b.record()
-        torch.cuda.synchronize()
-        train_ms = a.elapsed_time(b)
-        sampler = FastAutoregressiveSampler(m, min(args.samples, 8192), seed=777)
-        obs = Observable(op)
-        loc = []
-        for _ in range(max(1, args.samples // sampler.batch_size)):
-            spins, lp, saved = sampler.sample()
-            loc.append(obs.local_values(m, spins, log_psi=lp, base_saved=saved).clone())
-        stats, _ = energy_stats(torch.cat(loc))
-        st = stats.tolist()
-        n = sum(x.shape[0] for x in loc)
-        out[prec] = {"energy": st[0], "stderr": math.sqrt(st[2] / n), "train_ms": train_ms,
-                     "train_samples_per_s": args.train_steps * args.batch / (train_ms / 1e3)}
+        out[prec] = train_and_evaluate(prec, steps, batch, eval_samples)
     e16, e32 = out["bf16"]["energy"], out["fp32"]["energy"]
     out["relative_difference"] = abs(e16 - e32) / abs(e32)
+    out["difference_in_stderr"] = abs(e16 - e32) / math.hypot(out["bf16"]["stderr"], out["fp32"]["stderr"])
+    out["variance_ratio_bf16_over_fp32"] = (out["bf16"]["local_energy_variance"] /
+                                           out["fp32"]["local_energy_variance"])
     out["bf16_over_fp32"] = out["bf16"]["train_samples_per_s"] / out["fp32"]["train_samples_per_s"]
+    return out
+
+
+def matched_case(args):
+    """The metric's "at matched energy" at a chosen length: both paths trained
+    from the same seeded parameters for `--train-steps` VMC steps of `--batch`
+    samples, energies from `--samples` fresh samples each."""
+    out = {"case": "matched", "workload": WORKLOAD}
+    out.update(matched_summary(args.train_steps, args.batch, args.samples))
     print(json.dumps(out), flush=True)
 
 
@@ -379,9 +402,10 @@ def reference_arm(args, rank, world):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    batch = 16
+    batch = args.cpu_samples
+    # warm-up steps only warm the thread pool and allocator: a small sample
     for i in range(args.warmup):
-        cpu_vmc_sample(batch, 100 + i, threads)
+        cpu_vmc_sample(16, 100 + i, threads)
     times = [cpu_vmc_sample(batch, i, threads) for i in range(args.steps)]
     t = float(np.mean(times))
     value = batch / t
@@ -391,7 +415,8 @@ def reference_arm(args, rank, world):
             "config": {"workload": WORKLOAD, "cpu_sample": f"{batch} samples per step"},
             "cpu_baseline": {"value": value, "unit": "samples/s", "cores": threads, "kind": "port",
                              "sample": f"{batch} of the 4096 samples of one VMC step per timed step (oracle "
-                                       "restatement: fast AR sampler, all 101 connections, autograd)"},
+                                       "restatement: fast AR sampler, all 101 connections, autograd); "
+                                       "warm-up steps of 16 samples"},
             "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -407,6 +432,31 @@ def build_problem(precision, seed_offset):
     vmc = VariationalMonteCarlo(m, Ising(h=H_FIELD, hilbert_state_shape=SHAPE, pbc=True),
                                 FastAutoregressiveSampler(m, BATCH, seed=1234 + seed_offset))
     return m, vmc, Adam(m, lr=1e-3)
+
+
+def fp32_peak_tflops(n=8192, reps=5):
+    """cuBLAS SGEMM (TF32 off) throughput: the FP32 CUDA-core denominator."""
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        g = torch.Generator(device="cuda").manual_seed(0)
+        a = torch.randn((n, n), device="cuda", generator=g)
+        b = torch.randn((n, n), device="cuda", generator=g)
+        c = torch.empty((n, n), device="cuda")
+        for _ in range(2):
+            torch.matmul(a, b, out=c)
+        best = float("inf")
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b, out=c)
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        del a, b, c
+        return 2.0 * n ** 3 / (best / 1e3) / 1e12
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
 
 
 def timed_steps(vmc, opt, k):
@@ -498,9 +548,22 @@ def ours_arm(args, rank, world):
         vmc32.energy_observable.record_forward = True
         vmc32.step(opt32)
         vmc32.energy_observable.forward_events.clear()
-        t32, _, _ = timed_steps(vmc32, opt32, args.fp32_steps)
+        t32, fwd32_ms, rows32 = timed_steps(vmc32, opt32, args.fp32_steps)
         fp32 = {"samples_per_s": BATCH / (t32 / args.fp32_steps / 1e3), "ms_per_step": t32 / args.fp32_steps,
-                "energy": vmc32.current_energy.real, "steps": args.fp32_steps}
+                "energy": vmc32.current_energy.real, "steps": args.fp32_steps, "stage_ms": vmc32.times}
+        # roofline of the FP32 path's dominant kernels (the CUDA-core AR2D ops of
+        # the local-energy forward) against cuBLAS SGEMM measured here
+        peak32 = fp32_peak_tflops()
+        ach32 = rows32 * row_frac * flops_per_sample_forward(SHAPE, DEPTH, CHANNELS) / (fwd32_ms / 1e3) / 1e12
+        fp32["roofline"] = {"bound": "fp32 CUDA cores", "achieved": ach32, "peak": peak32, "unit": "TFLOP/s",
+                            "frac": ach32 / peak32, "kernel": "AR2D conv ops (FP32) of the local-energy forward",
+                            "peak_source": "measured in this run: cuBLAS SGEMM 8192^3, TF32 off, best of 5"}
+        del m32, vmc32, opt32
+        torch.cuda.empty_cache()
+
+    matched = None
+    if args.matched_steps > 0 and rank == 0:
+        matched = matched_summary(args.matched_steps, args.matched_batch, args.matched_samples)
 
     peaks = {}
     try:
@@ -534,6 +597,7 @@ def ours_arm(args, rank, world):
                            "l2": "inputs larger than L2 (activation workspaces of several GB per step)"},
                 "energy_bf16": energy_bf16, "fp32_path": fp32,
                 "bf16_over_fp32": (samples_per_s / world) / fp32["samples_per_s"] if fp32 else None,
+                "matched": matched,
                 "stage_ms": vmc.times,
                 "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                              "frac": achieved / peak if achieved else None,
@@ -546,8 +610,8 @@ def ours_arm(args, rank, world):
                 "clocks": clk, "gpu_launches": launches, "e2e": e2e}
         if not args.no_cpu_baseline:
             threads = os.cpu_count() or 1
-            n = 8
-            cpu_vmc_sample(2, 7, threads)
+            n = args.cpu_samples
+            cpu_vmc_sample(16, 7, threads)
             t = cpu_vmc_sample(n, 0, threads)
             line["cpu_baseline"] = {"value": n / t, "unit": "samples/s", "cores": threads, "kind": "port",
                                     "sample": f"{n} samples of one VMC step (oracle restatement on the host: "

@@ -237,6 +237,83 @@ def _ar2d_backward(machine, spins, seeds, saved, per_sample=False):
 ConvNetAutoregressive2D.backward = _ar2d_backward
 
 
+class Ar2dLogPsi(torch.autograd.Function):
+    """log psi of ConvNetAutoregressive2D as a differentiable torch op: the
+    forward kernels produce (B, 2) = (Re, Im) log psi, the hand-written
+    adjoint (fk_ar2d_backward) maps the incoming gradient (B, 2) to the
+    gradient of the flat parameter vector (the role of the reference's
+    Keras gradient through the model, optimization/loss.py:4-5, and of
+    machines/abstract_machine.py:24-28's jacobian hook for the summed case).
+
+    With ``recompute_chunk`` = c the forward keeps no activations: the adjoint
+    re-runs the forward over c samples at a time (FK_AR2D_SAVE into a
+    c-sample workspace) and accumulates the chunks' gradients, so the memory
+    held between forward and backward is the log psi alone and the adjoint's
+    workspace is bounded by c samples instead of B."""
+
+    @staticmethod
+    def forward(ctx, params, machine, spins, recompute_chunk):
+        if recompute_chunk:
+            lp, _, _ = machine.forward(spins, mode=_lib.FK_AR2D_INFER)
+            ctx.saved_ws = None
+        else:
+            # a private workspace (the machine's cached one is reused by the
+            # next forward of the same batch size)
+            nbytes = _lib.load().fk_ar2d_workspace_bytes(ctypes_ref(machine.desc), spins.shape[0],
+                                                         _lib.FK_AR2D_SAVE)
+            ws = torch.empty(nbytes, dtype=torch.uint8, device=machine.device)
+            lp, _, _ = machine.forward(spins, mode=_lib.FK_AR2D_SAVE, workspace=ws)
+            ctx.saved_ws = ws
+        ctx.machine = machine
+        ctx.chunk = recompute_chunk
+        ctx.save_for_backward(spins)
+        return lp.clone()
+
+    @staticmethod
+    def backward(ctx, grad_lp):
+        (spins,) = ctx.saved_tensors
+        m = ctx.machine
+        g = grad_lp.to(torch.float32).contiguous()
+        if ctx.saved_ws is not None:
+            grad = m.backward(spins, g, ctx.saved_ws)
+        else:
+            grad = torch.zeros(m.num_params, dtype=torch.float32, device=m.device)
+            for i in range(0, spins.shape[0], ctx.chunk):
+                x = spins[i:i + ctx.chunk]
+                _, _, ws = m.forward(x, mode=_lib.FK_AR2D_SAVE)
+                grad.add_(m.backward(x, g[i:i + ctx.chunk], ws))
+        return grad, None, None, None
+
+
+def _ar2d_log_psi_autograd(machine, spins, params=None, recompute_chunk=None):
+    """Differentiable log psi (B, 2) (Re, Im) through Ar2dLogPsi. `params`
+    defaults to ``machine.params`` (set ``requires_grad`` on it, or pass a
+    leaf tensor that aliases it)."""
+    s = machine._spins(spins)
+    p = machine.params if params is None else params
+    return Ar2dLogPsi.apply(p, machine, s, recompute_chunk)
+
+
+ConvNetAutoregressive2D.log_psi_autograd = _ar2d_log_psi_autograd
+
+
+def _ar2d_backward_recompute(machine, spins, seeds, chunk=1024):
+    """Summed adjoint without stored activations: the forward is re-run in
+    chunks of `chunk` samples (activation recomputation for lattices whose
+    full-batch activations would not fit next to the rest of the step)."""
+    s = machine._spins(spins)
+    w = torch.as_tensor(seeds, dtype=torch.float32, device=machine.device).reshape(s.shape[0], 2).contiguous()
+    grad = torch.zeros(machine.num_params, dtype=torch.float32, device=machine.device)
+    for i in range(0, s.shape[0], chunk):
+        x = s[i:i + chunk]
+        _, _, ws = machine.forward(x, mode=_lib.FK_AR2D_SAVE)
+        grad.add_(machine.backward(x, w[i:i + chunk], ws))
+    return grad
+
+
+ConvNetAutoregressive2D.backward_recompute = _ar2d_backward_recompute
+
+
 def _ar2d_log_derivatives(machine, spins, saved=None):
     """Per-sample complex O_k = d log psi / d theta_k (num_params, B) complex64
     (the reference's predictions_jacobian, machines/abstract_machine.py:24-28)."""

@@ -128,3 +128,36 @@ def test_tensor_core_adjoint_matches_cuda_core_adjoint(cuda, tmp_path, shape, de
     rel = np.linalg.norm(got - ref) / np.linalg.norm(ref)
     cos = got @ ref / (np.linalg.norm(got) * np.linalg.norm(ref))
     assert rel < 3e-2 and cos > 0.999, (rel, cos)
+
+
+@pytest.mark.parametrize("recompute", [None, 48])
+@pytest.mark.parametrize("precision", ["fp32", "bf16"])
+def test_autograd_function_equals_machine_backward(cuda, precision, recompute):
+    """torch.autograd through Ar2dLogPsi (with and without chunked activation
+    recomputation) gives the gradient of m.backward on the same seeds."""
+    from flowket_gb300 import _lib
+    shape, depth, f, wn = (4, 4), 3, 32, True
+    m, s, sc, w, saved = _setup(shape, depth, f, wn, precision, b=150)
+    want = m.backward(sc, w, saved).cpu().numpy().astype(np.float64)
+    p = m.params.detach().requires_grad_(True)
+    lp = m.log_psi_autograd(sc, params=p, recompute_chunk=recompute)
+    loss = (lp * torch.as_tensor(w).cuda()).sum()
+    loss.backward()
+    got = p.grad.cpu().numpy().astype(np.float64)
+    if recompute is None:
+        # same activations, same adjoint: bitwise
+        np.testing.assert_array_equal(got, want)
+    rel = np.linalg.norm(got - want) / np.linalg.norm(want)
+    assert rel < 1e-5, rel
+    # the oracle's gradient agrees as well (FP32 path)
+    if precision == "fp32":
+        ref = _flat(m, ar2d.weighted_gradient(m.params_dict_cpu(), s, depth, wn, w[:, 0], w[:, 1]))
+        assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-4
+
+
+def test_backward_recompute_equals_saved_adjoint(cuda):
+    shape, depth, f, wn = (10, 10), 10, 32, True
+    m, s, sc, w, saved = _setup(shape, depth, f, wn, "bf16", b=256)
+    want = m.backward(sc, w, saved).cpu().numpy().astype(np.float64)
+    got = m.backward_recompute(sc, w, chunk=128).cpu().numpy().astype(np.float64)
+    assert np.linalg.norm(got - want) / np.linalg.norm(want) < 1e-5

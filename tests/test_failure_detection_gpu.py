@@ -55,8 +55,10 @@ def test_nonfinite_weight_injection_is_reported(cuda, precision):
     m, vmc, opt = _ar_problem(precision)
     vmc.step(opt)
     good = m.params.clone()
+    # a non-finite output-layer bias makes every log psi non-finite (a NaN
+    # inside a hidden layer can be absorbed: ReLU as max(x, 0) maps NaN to 0)
     with torch.no_grad():
-        m.params[m.num_params // 2] = float("nan")
+        m.named_params()["out.bias"][0] = float("nan")
     m.params_updated()
     with pytest.raises(_lib.NonFiniteError):
         vmc.step(opt)
