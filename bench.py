@@ -179,14 +179,17 @@ def train_and_evaluate(precision, steps, batch, eval_samples, lr=1e-3):
 def matched_summary(steps, batch, eval_samples):
     out = {"train_steps": steps, "batch": batch, "eval_samples": eval_samples, "optimizer": "Adam lr 1e-3",
            "init": "same seeded parameters and sampler seed for both paths"}
-    for prec in ("bf16", "fp32"):
+    for prec in ("bf16", "fp16", "fp32"):
         out[prec] = train_and_evaluate(prec, steps, batch, eval_samples)
-    e16, e32 = out["bf16"]["energy"], out["fp32"]["energy"]
-    out["relative_difference"] = abs(e16 - e32) / abs(e32)
-    out["difference_in_stderr"] = abs(e16 - e32) / math.hypot(out["bf16"]["stderr"], out["fp32"]["stderr"])
-    out["variance_ratio_bf16_over_fp32"] = (out["bf16"]["local_energy_variance"] /
-                                           out["fp32"]["local_energy_variance"])
-    out["bf16_over_fp32"] = out["bf16"]["train_samples_per_s"] / out["fp32"]["train_samples_per_s"]
+    e32 = out["fp32"]["energy"]
+    for prec in ("bf16", "fp16"):
+        e = out[prec]["energy"]
+        out[prec]["relative_difference_to_fp32"] = abs(e - e32) / abs(e32)
+        out[prec]["difference_in_stderr"] = abs(e - e32) / math.hypot(out[prec]["stderr"], out["fp32"]["stderr"])
+        out[prec]["variance_ratio_to_fp32"] = out[prec]["local_energy_variance"] / out["fp32"]["local_energy_variance"]
+        out[prec]["speedup_over_fp32"] = out[prec]["train_samples_per_s"] / out["fp32"]["train_samples_per_s"]
+    out["relative_difference"] = out["bf16"]["relative_difference_to_fp32"]
+    out["bf16_over_fp32"] = out["bf16"]["speedup_over_fp32"]
     return out
 
 

@@ -14,6 +14,8 @@ LIB_PATH = os.path.join(_HERE, "libflowket_gb300.so")
 
 FK_PRECISION_FP32 = 0
 FK_PRECISION_BF16 = 1
+FK_PRECISION_FP16 = 2
+PRECISIONS = {"fp32": FK_PRECISION_FP32, "bf16": FK_PRECISION_BF16, "fp16": FK_PRECISION_FP16}
 FK_AR2D_INFER = 0
 FK_AR2D_SAVE = 1
 

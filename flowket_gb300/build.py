@@ -1,7 +1,8 @@
 """In-tree build of libflowket_gb300.so for sm_103a (nvcc, no cmake).
 
 Every translation unit under csrc/ is compiled in parallel to
-_build/*.o and linked into flowket_gb300/libflowket_gb300.so.
+_build/*.o (the AR2D machine's twice: BF16 and FP16 tensor-core operands)
+and linked into flowket_gb300/libflowket_gb300.so.
 """
 import concurrent.futures
 import os
@@ -37,17 +38,33 @@ def _stale(obj, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+# Translation units of the AR2D machine: compiled a second time with
+# FK_TC_FP16 (FP16 tensor-core operands, namespace fk16, entry points
+# fk_ar2d_*_tc_fp16).
+TWO_FORMATS = ("fk_ar2d.cu", "fk_ar2d_pipe.cu", "fk_ar2d_bwd.cu", "fk_ar2d_bwd_tc.cu")
+
+
+def objects():
+    """(source, object, extra flags) of every compilation."""
+    out = []
+    for src in sources():
+        base = os.path.basename(src)[:-3]
+        out.append((src, os.path.join(BUILD, base + ".o"), []))
+        if os.path.basename(src) in TWO_FORMATS:
+            out.append((src, os.path.join(BUILD, base + "_fp16.o"), ["-DFK_TC_FP16"]))
+    return out
+
+
 def build(verbose=False, force=False):
     nvcc = _nvcc()
     os.makedirs(BUILD, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     headers.append(os.path.join(ROOT, "include", "flowket_gb300.h"))
     jobs = []
-    for src in sources():
-        obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
+    for src, obj, extra in objects():
         if force or _stale(obj, [src] + headers):
-            jobs.append([nvcc] + ARCH + FLAGS + ["-c", src, "-o", obj])
-    objs = [os.path.join(BUILD, os.path.basename(s)[:-3] + ".o") for s in sources()]
+            jobs.append([nvcc] + ARCH + FLAGS + extra + ["-c", src, "-o", obj])
+    objs = [obj for _, obj, _ in objects()]
 
     def run(cmd):
         if verbose:

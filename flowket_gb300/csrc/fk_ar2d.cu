@@ -28,7 +28,7 @@
 #include <stdlib.h>
 #include <string.h>
 
-namespace fk {
+namespace FK_NS {
 
 // ============================================================== layout (host)
 int build_layout(const fk_ar2d_desc* d, NetLayout* L) {
@@ -38,7 +38,8 @@ int build_layout(const fk_ar2d_desc* d, NetLayout* L) {
   }
   if (d->height < 1 || d->width < 1 || d->height * d->width > 4096 || d->depth < 2 || d->depth > 20 ||
       !(d->channels == 16 || d->channels == 32 || d->channels == 64) ||
-      !(d->precision == FK_PRECISION_FP32 || d->precision == FK_PRECISION_BF16)) {
+      !(d->precision == FK_PRECISION_FP32 || d->precision == FK_PRECISION_BF16 ||
+        d->precision == FK_PRECISION_FP16)) {
     set_error("fk_ar2d: unsupported shape (H=%d W=%d depth=%d channels=%d precision=%d); "
               "supported: depth 2..20, channels 16/32/64",
               d->height, d->width, d->depth, d->channels, d->precision);
@@ -75,17 +76,17 @@ int build_layout(const fk_ar2d_desc* d, NetLayout* L) {
       p += cout;
     }
     c.w_off = w;
-    if (L->precision == FK_PRECISION_BF16) {
+    if (L->precision != FK_PRECISION_FP32) {
       w += ((int64_t)c.Kpad * c.Npad * 2 + 255) / 256 * 256;
     }
     c.ws_off = -1;
     c.wt_off = -1;
-    if (L->precision == FK_PRECISION_BF16 && kw == 3 && cin == F && F <= 32) {
+    if (L->precision != FK_PRECISION_FP32 && kw == 3 && cin == F && F <= 32) {
       c.ws_off = w;
       w += ((int64_t)kh * cin * 3 * cout * 2 + 255) / 256 * 256;
       c.wt_off = w;
       w += ((int64_t)kh * cout * 3 * cin * 2 + 255) / 256 * 256;
-    } else if (L->precision == FK_PRECISION_BF16 && kh == 1 && kw == 1 && cin == F && cout == F / 2 && F <= 32) {
+    } else if (L->precision != FK_PRECISION_FP32 && kh == 1 && kw == 1 && cin == F && cout == F / 2 && F <= 32) {
       c.wt_off = w;
       w += ((int64_t)cout * cin * 2 + 255) / 256 * 256;
     }
@@ -108,7 +109,7 @@ int build_layout(const fk_ar2d_desc* d, NetLayout* L) {
   return FK_OK;
 }
 
-static inline int64_t esize(const NetLayout& L) { return L.precision == FK_PRECISION_BF16 ? 2 : 4; }
+static inline int64_t esize(const NetLayout& L) { return L.precision != FK_PRECISION_FP32 ? 2 : 4; }
 
 int64_t tensor_bytes(const NetLayout& L, int64_t tiles, int channels) {
   int64_t b = tiles * L.P * (int64_t)kTile * channels * esize(L);
@@ -184,7 +185,7 @@ __global__ void pack_kernel(const __grid_constant__ PackArgs a) {
     for (int i = threadIdx.x; i < total; i += blockDim.x) w[i] = v[i] * scale[i % c.cout];
   }
   if (a.bf16) {
-    __nv_bfloat16* w = reinterpret_cast<__nv_bfloat16*>(a.packed + c.w_off);
+    tc16* w = reinterpret_cast<tc16*>(a.packed + c.w_off);
     int total = c.Kpad * c.Npad;
     for (int i = threadIdx.x; i < total; i += blockDim.x) {
       // element (k, n) of the no-swizzle K-major operand at ((k/8)*Npad + n)*8 + k%8
@@ -193,13 +194,13 @@ __global__ void pack_kernel(const __grid_constant__ PackArgs a) {
       int n = rem / 8, e = rem % 8;
       int k = kg * 8 + e;
       float x = (k < c.K && n < c.cout) ? v[(int64_t)k * c.cout + n] * scale[n] : 0.f;
-      w[i] = __float2bfloat16_rn(x);
+      w[i] = to_tc16(x);
     }
   }
   if (a.bf16 && c.ws_off >= 0) {
     // column-scatter operand: element (kernel row i, k, n = s*cout + co) at
     // ((i*(cin/8) + k/8)*3*cout + n)*8 + k%8, value W[i][2 - s][k][co]
-    __nv_bfloat16* w = reinterpret_cast<__nv_bfloat16*>(a.packed + c.ws_off);
+    tc16* w = reinterpret_cast<tc16*>(a.packed + c.ws_off);
     const int n3 = 3 * c.cout;
     const int total = c.kh * c.cin * n3;
     for (int i = threadIdx.x; i < total; i += blockDim.x) {
@@ -210,13 +211,13 @@ __global__ void pack_kernel(const __grid_constant__ PackArgs a) {
       const int k = (kg % (c.cin / 8)) * 8 + e;
       const int s = n / c.cout, co = n % c.cout;
       const int t = row * c.kw + (2 - s);
-      w[i] = __float2bfloat16_rn(v[((int64_t)t * c.cin + k) * c.cout + co] * scale[co]);
+      w[i] = to_tc16(v[((int64_t)t * c.cin + k) * c.cout + co] * scale[co]);
     }
   }
   if (a.bf16 && c.wt_off >= 0) {
     // transposed operand: element (kernel row i, k = co, n = j*cin + ci) at
     // ((i*(cout/8) + co/8)*kw*cin + n)*8 + co%8, value W[i][j][ci][co]
-    __nv_bfloat16* w = reinterpret_cast<__nv_bfloat16*>(a.packed + c.wt_off);
+    tc16* w = reinterpret_cast<tc16*>(a.packed + c.wt_off);
     const int nn = c.kw * c.cin;
     const int total = c.kh * c.cout * nn;
     for (int i = threadIdx.x; i < total; i += blockDim.x) {
@@ -227,7 +228,7 @@ __global__ void pack_kernel(const __grid_constant__ PackArgs a) {
       const int co = (kg % (c.cout / 8)) * 8 + e;
       const int j = n / c.cin, ci = n % c.cin;
       const int t = row * c.kw + j;
-      w[i] = __float2bfloat16_rn(v[((int64_t)t * c.cin + ci) * c.cout + co] * scale[co]);
+      w[i] = to_tc16(v[((int64_t)t * c.cin + ci) * c.cout + co] * scale[co]);
     }
   }
 }
@@ -404,7 +405,7 @@ template <int F>
 __device__ void tc_main(const OpArgs& a, TcSmem& s, TcState& st, int64_t tile, int m, int r, int c, int H, int W,
                         int P, float* acc) {
   using C = TcCfg<F>;
-  const uint32_t idesc = umma_idesc_bf16(128, F);
+  const uint32_t idesc = umma_idesc_tc16(128, F);
   const int chain_bytes = F * ((a.kind == kConvC) ? 16 : C::kChainNpad) * 2;
   const bool has_chain = !(a.kind == kConvC && !a.last);
   const char* wbase = static_cast<const char*>(a.main.w);
@@ -421,8 +422,8 @@ __device__ void tc_main(const OpArgs& a, TcSmem& s, TcState& st, int64_t tile, i
       int rr = r + dr, cc = c + dc;
       if (rr >= 0 && rr < H && cc >= 0 && cc < W) v[t] = spin_at(a.spins, a.batch, P, tile * kTile + m, rr * W + cc);
     }
-    st8(reinterpret_cast<__nv_bfloat16*>(s.a_ptr + m * 16), v);
-    st8(reinterpret_cast<__nv_bfloat16*>(s.a_ptr + 2048 + m * 16), v + 8);
+    st8(reinterpret_cast<tc16*>(s.a_ptr + m * 16), v);
+    st8(reinterpret_cast<tc16*>(s.a_ptr + 2048 + m * 16), v + 8);
     fence_proxy_async_smem();
     if (threadIdx.x == 0) {
       uint32_t wbytes = 2 * F * 16;
@@ -467,7 +468,7 @@ __device__ void tc_main(const OpArgs& a, TcSmem& s, TcState& st, int64_t tile, i
         uint32_t bytes = ng * (C::kTapBytesA + wslice) + ((g0 == 0 && has_chain) ? chain_bytes : 0);
         mbar_arrive_expect_tx(s.bar_load, bytes);
         for (int j = 0; j < ng; ++j) {
-          const __nv_bfloat16* src = blk<__nv_bfloat16>(a.in, tile, P, pix[g0 + j], F);
+          const tc16* src = blk<tc16>(a.in, tile, P, pix[g0 + j], F);
           bulk_g2s(s.a_ptr + j * C::kTapBytesA, src, C::kTapBytesA, s.bar_load);
           bulk_g2s(s.w_ptr + j * wslice, wbase + (int64_t)taps[g0 + j] * wslice, wslice, s.bar_load);
         }
@@ -496,7 +497,7 @@ __device__ void tc_main(const OpArgs& a, TcSmem& s, TcState& st, int64_t tile, i
 // out[0..NCPAD) = in[0..KC) x Wchain on tensor cores (weights already in smem).
 template <int KC, int NCPAD>
 __device__ void tc_chain(TcSmem& s, TcState& st, int m, const float* in, float* out) {
-  __nv_bfloat16* ca = reinterpret_cast<__nv_bfloat16*>(s.ca_ptr);
+  tc16* ca = reinterpret_cast<tc16*>(s.ca_ptr);
 #pragma unroll
   for (int g = 0; g < KC / 8; ++g) st8(ca + ((int64_t)g * kTile + m) * 8, in + 8 * g);
   fence_proxy_async_smem();
@@ -504,7 +505,7 @@ __device__ void tc_chain(TcSmem& s, TcState& st, int m, const float* in, float* 
   __syncthreads();
   if (threadIdx.x == 0) {
     tc_fence_after();
-    const uint32_t idesc = umma_idesc_bf16(128, NCPAD);
+    const uint32_t idesc = umma_idesc_tc16(128, NCPAD);
 #pragma unroll
     for (int ks = 0; ks < KC / 16; ++ks) {
       uint64_t ad = umma_sdesc(s.ca + ks * 2 * 2048, 2048, 128);
@@ -690,7 +691,7 @@ __device__ void run_op(const OpArgs& a, Engine<F, TC>& eng, int64_t tile, int r,
 // Grid: one CTA per (tile, row); the CTA walks the row's pixels.
 template <int F, bool TC>
 __global__ void __launch_bounds__(128) op_row_kernel(const __grid_constant__ OpArgs a, int H, int W, int* err) {
-  using T = typename std::conditional<TC, __nv_bfloat16, float>::type;
+  using T = typename std::conditional<TC, tc16, float>::type;
   extern __shared__ __align__(1024) uint8_t smem[];
   const int P = H * W;
   int64_t item = blockIdx.x;
@@ -767,7 +768,7 @@ struct FirstCfg {
 template <int F>
 __global__ void __launch_bounds__(128) first_row_kernel(const __grid_constant__ OpArgs a, int H, int W, int* err) {
   using C = FirstCfg<F>;
-  using T = __nv_bfloat16;
+  using T = tc16;
   constexpr int F2 = F / 2;
   constexpr int NC = C::kNC;
   extern __shared__ __align__(1024) uint8_t smem[];
@@ -831,7 +832,7 @@ __global__ void __launch_bounds__(128) first_row_kernel(const __grid_constant__ 
   ok = mbar_wait(&bar[0], 0, e);
   if (m == 0 && ok) {
     tc_fence_after();
-    const uint32_t idesc = umma_idesc_bf16(128, F);
+    const uint32_t idesc = umma_idesc_tc16(128, F);
     const uint64_t bd = umma_sdesc(smem_u32(wsm), F * 16, 128);
     for (int c = 0; c < W; ++c)
       umma_bf16(tmem + c * F, umma_sdesc(smem_u32(abuf + c * 4096), 2048, 128), bd, idesc, 0u);
@@ -881,7 +882,7 @@ __global__ void __launch_bounds__(128) first_row_kernel(const __grid_constant__ 
   __syncthreads();
   tc_fence_after();
   if (m == 0 && ok) {
-    const uint32_t idesc = umma_idesc_bf16(128, NC);
+    const uint32_t idesc = umma_idesc_tc16(128, NC);
     for (int c = 0; c < W; ++c) {
 #pragma unroll
       for (int ks = 0; ks < F / 16; ++ks)
@@ -1184,7 +1185,7 @@ static_assert(SiteCfg<32>::kSmem <= 227 * 1024, "sampler shared memory");
 // some time after the commit that follows it may have been observed).
 template <int F>
 __device__ bool v_row_op(const SampOp& a, TcSmem& s, TcState& st, int64_t tile, int r, int H, int W) {
-  using T = __nv_bfloat16;
+  using T = tc16;
   using SC = SiteCfg<F>;
   constexpr int F2 = F / 2;
   constexpr int NC = SC::kNC;
@@ -1219,8 +1220,8 @@ __device__ bool v_row_op(const SampOp& a, TcSmem& s, TcState& st, int64_t tile, 
   if (!tc_wait(s.bar_load, st.ph_load, st)) return false;
   const uint64_t a0 = umma_sdesc(s.a, 2048, 128);
   const uint64_t w0 = umma_sdesc(s.w, 3 * F * 16, 128);
-  const uint32_t idesc1 = umma_idesc_bf16(128, F), idesc2 = umma_idesc_bf16(128, 2 * F),
-                 idesc3 = umma_idesc_bf16(128, 3 * F);
+  const uint32_t idesc1 = umma_idesc_tc16(128, F), idesc2 = umma_idesc_tc16(128, 2 * F),
+                 idesc3 = umma_idesc_tc16(128, 3 * F);
   bool ok = true;
   for (int x = 0; x < W && ok && m == 0; ++x) {
     const int sl = x % NSL;
@@ -1317,7 +1318,7 @@ __device__ bool v_row_op(const SampOp& a, TcSmem& s, TcState& st, int64_t tile, 
     __syncthreads();
     tc_fence_after();
     if (m == 0) {
-      const uint32_t idesc = umma_idesc_bf16(128, NC);
+      const uint32_t idesc = umma_idesc_tc16(128, NC);
       for (int c = c0; c < c1; ++c) {
 #pragma unroll
         for (int ks = 0; ks < F / 16; ++ks)
@@ -1381,7 +1382,7 @@ template <int F>
 __device__ void site_prefetch(const SampOp& a, TcSmem& s, SiteBufs& b, int64_t tile, int r, int c, int H, int W,
                               bool own_full = false) {
   using SC = SiteCfg<F>;
-  using T = __nv_bfloat16;
+  using T = tc16;
   const int P = H * W;
   const bool isC = a.kind == kConvC;
   uint64_t* bar = isC ? s.bar_load : b.bar_h;
@@ -1420,7 +1421,7 @@ __device__ void site_prefetch(const SampOp& a, TcSmem& s, SiteBufs& b, int64_t t
 template <int KC, int NCPAD>
 __device__ bool site_chain(TcSmem& s, TcState& st, uint32_t cw, const float* in, float* out) {
   const int m = threadIdx.x;
-  __nv_bfloat16* ca = reinterpret_cast<__nv_bfloat16*>(s.ca_ptr);
+  tc16* ca = reinterpret_cast<tc16*>(s.ca_ptr);
 #pragma unroll
   for (int g = 0; g < KC / 8; ++g) st8(ca + ((int64_t)g * kTile + m) * 8, in + 8 * g);
   fence_proxy_async_smem();
@@ -1428,7 +1429,7 @@ __device__ bool site_chain(TcSmem& s, TcState& st, uint32_t cw, const float* in,
   __syncthreads();
   if (m == 0) {
     tc_fence_after();
-    const uint32_t idesc = umma_idesc_bf16(128, NCPAD);
+    const uint32_t idesc = umma_idesc_tc16(128, NCPAD);
 #pragma unroll
     for (int ks = 0; ks < KC / 16; ++ks)
       umma_bf16(st.tmem + kChainCol, umma_sdesc(s.ca + ks * 2 * 2048, 2048, 128),
@@ -1449,7 +1450,7 @@ __device__ bool site_op(const SampOp& a, TcSmem& s, TcState& st, SiteBufs& b, in
                         int W, const SampOp* nx, int nc, bool keep_res, bool site_end, HeadOut* head,
                         int head_mask) {
   using SC = SiteCfg<F>;
-  using T = __nv_bfloat16;
+  using T = tc16;
   constexpr int F2 = F / 2;
   constexpr int NC2 = SC::kNC;
   const int P = H * W;
@@ -1478,7 +1479,7 @@ __device__ bool site_op(const SampOp& a, TcSmem& s, TcState& st, SiteBufs& b, in
     tc_fence_after();
     const uint64_t a0 = umma_sdesc(smem_u32(A), 2048, 128);
     const uint64_t w0 = umma_sdesc(smem_u32(Wt), F * 16, 128);
-    const uint32_t idesc = umma_idesc_bf16(128, F);
+    const uint32_t idesc = umma_idesc_tc16(128, F);
     if (a.first()) {
       umma_bf16(st.tmem, a0, w0, idesc, 0u);
     } else {
@@ -1578,7 +1579,7 @@ struct SampleArgs {
 
 template <int F, bool TC>
 __global__ void __launch_bounds__(128) sample_kernel(const __grid_constant__ SampleArgs a, int H, int W, int* err) {
-  using T = typename std::conditional<TC, __nv_bfloat16, float>::type;
+  using T = typename std::conditional<TC, tc16, float>::type;
   extern __shared__ __align__(1024) uint8_t smem[];
   const int P = H * W;
   const int64_t tile = blockIdx.x;
@@ -1968,7 +1969,7 @@ template <int F, bool TC>
 static int connections_impl(const NetLayout& L, const void* packed, const int8_t* configs, const int32_t* owner,
                             const int16_t* cflips, int64_t n_rows, const Tensors& B, float* log_psi,
                             const Tensors& T, const ConnScratch& S, int64_t chunk, cudaStream_t s) {
-  using Tv = typename std::conditional<TC, __nv_bfloat16, float>::type;
+  using Tv = typename std::conditional<TC, tc16, float>::type;
   int* err = device_error_word();
   FK_CUDA(cudaMemsetAsync(S.hist, 0, (L.H + 1) * 4, s));
   conn_rk_kernel<<<(unsigned)((n_rows + 255) / 256), 256, 0, s>>>(reinterpret_cast<const short2*>(cflips), n_rows,
@@ -2016,12 +2017,14 @@ static int connections_impl(const NetLayout& L, const void* packed, const int8_t
   return FK_OK;
 }
 
-}  // namespace fk
+}  // namespace FK_NS
 
-using namespace fk;
+using namespace FK_NS;
 
 extern "C" {
 
+#ifndef FK_TC_FP16
+// Layout queries: the same for both 16-bit formats, compiled once.
 int64_t fk_ar2d_num_params(const fk_ar2d_desc* desc) {
   NetLayout L;
   if (build_layout(desc, &L) != FK_OK) return -1;
@@ -2033,8 +2036,10 @@ int64_t fk_ar2d_packed_bytes(const fk_ar2d_desc* desc) {
   if (build_layout(desc, &L) != FK_OK) return -1;
   return L.packed_bytes;
 }
+#endif
 
-int fk_ar2d_pack(const fk_ar2d_desc* desc, const float* params, void* packed, void* stream) {
+int FK_AR2D_ENTRY(fk_ar2d_pack)(const fk_ar2d_desc* desc, const float* params, void* packed, void* stream) {
+  FK_DISPATCH_FP16(desc, fk_ar2d_pack_tc_fp16(desc, params, packed, stream));
   NetLayout L;
   int st = build_layout(desc, &L);
   if (st != FK_OK) return st;
@@ -2043,7 +2048,7 @@ int fk_ar2d_pack(const fk_ar2d_desc* desc, const float* params, void* packed, vo
   a->params = params;
   a->packed = static_cast<char*>(packed);
   a->n_convs = L.n_convs;
-  a->bf16 = L.precision == FK_PRECISION_BF16;
+  a->bf16 = L.precision != FK_PRECISION_FP32;
   memcpy(a->conv, L.conv, sizeof(L.conv));
   pack_kernel<<<L.n_convs, 256, 0, static_cast<cudaStream_t>(stream)>>>(*a);
   delete a;
@@ -2051,15 +2056,19 @@ int fk_ar2d_pack(const fk_ar2d_desc* desc, const float* params, void* packed, vo
   return FK_OK;
 }
 
+#ifndef FK_TC_FP16
 int64_t fk_ar2d_workspace_bytes(const fk_ar2d_desc* desc, int64_t batch, int32_t mode) {
   NetLayout L;
   if (build_layout(desc, &L) != FK_OK || batch < 0) return -1;
   return workspace_layout(L, batch, mode, nullptr, nullptr);
 }
+#endif
 
-int fk_ar2d_forward(const fk_ar2d_desc* desc, const void* packed, const int8_t* spins, int64_t batch,
-                    float* log_psi, float* cond, void* workspace, int64_t workspace_bytes, int32_t mode,
-                    void* stream) {
+int FK_AR2D_ENTRY(fk_ar2d_forward)(const fk_ar2d_desc* desc, const void* packed, const int8_t* spins, int64_t batch,
+                                   float* log_psi, float* cond, void* workspace, int64_t workspace_bytes,
+                                   int32_t mode, void* stream) {
+  FK_DISPATCH_FP16(desc, fk_ar2d_forward_tc_fp16(desc, packed, spins, batch, log_psi, cond, workspace,
+                                                 workspace_bytes, mode, stream));
   NetLayout L;
   int st = build_layout(desc, &L);
   if (st != FK_OK) return st;
@@ -2071,7 +2080,7 @@ int fk_ar2d_forward(const fk_ar2d_desc* desc, const void* packed, const int8_t* 
   FK_CHECK_ARG(workspace && workspace_bytes >= need, "fk_ar2d_forward: workspace %lld < %lld bytes",
                (long long)workspace_bytes, (long long)need);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const bool tc = L.precision == FK_PRECISION_BF16;
+  const bool tc = L.precision != FK_PRECISION_FP32;
   switch (L.F) {
     case 16: return tc ? forward_impl<16, true>(L, packed, spins, batch, log_psi, cond, T, mode, s)
                        : forward_impl<16, false>(L, packed, spins, batch, log_psi, cond, T, mode, s);
@@ -2082,8 +2091,11 @@ int fk_ar2d_forward(const fk_ar2d_desc* desc, const void* packed, const int8_t* 
   }
 }
 
-int fk_ar2d_sample(const fk_ar2d_desc* desc, const void* packed, int64_t batch, uint64_t seed, uint64_t offset,
-                   int8_t* spins, float* log_psi, void* workspace, int64_t workspace_bytes, void* stream) {
+int FK_AR2D_ENTRY(fk_ar2d_sample)(const fk_ar2d_desc* desc, const void* packed, int64_t batch, uint64_t seed,
+                                  uint64_t offset, int8_t* spins, float* log_psi, void* workspace,
+                                  int64_t workspace_bytes, void* stream) {
+  FK_DISPATCH_FP16(desc, fk_ar2d_sample_tc_fp16(desc, packed, batch, seed, offset, spins, log_psi, workspace,
+                                                workspace_bytes, stream));
   NetLayout L;
   int st = build_layout(desc, &L);
   if (st != FK_OK) return st;
@@ -2094,7 +2106,7 @@ int fk_ar2d_sample(const fk_ar2d_desc* desc, const void* packed, int64_t batch, 
   FK_CHECK_ARG(workspace && workspace_bytes >= need, "fk_ar2d_sample: workspace %lld < %lld bytes",
                (long long)workspace_bytes, (long long)need);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const bool tc = L.precision == FK_PRECISION_BF16;
+  const bool tc = L.precision != FK_PRECISION_FP32;
   switch (L.F) {
     case 16: return tc ? sample_impl<16, true>(L, packed, batch, seed, offset, spins, log_psi, T, s)
                        : sample_impl<16, false>(L, packed, batch, seed, offset, spins, log_psi, T, s);
@@ -2106,16 +2118,22 @@ int fk_ar2d_sample(const fk_ar2d_desc* desc, const void* packed, int64_t batch, 
 }
 
 
+#ifndef FK_TC_FP16
 int64_t fk_ar2d_connections_workspace_bytes(const fk_ar2d_desc* desc, int64_t max_rows, int64_t chunk) {
   NetLayout L;
   if (build_layout(desc, &L) != FK_OK || max_rows < 0 || chunk <= 0) return -1;
   return conn_layout(L, max_rows, chunk, nullptr, nullptr, nullptr);
 }
+#endif
 
-int fk_ar2d_forward_connections(const fk_ar2d_desc* desc, const void* packed, const int8_t* configs,
-                                const int32_t* owner, const int16_t* cflips, int64_t n_rows, const void* base_saved,
-                                int64_t base_saved_bytes, int64_t base_batch, float* log_psi, void* workspace,
-                                int64_t workspace_bytes, int64_t chunk, void* stream) {
+int FK_AR2D_ENTRY(fk_ar2d_forward_connections)(const fk_ar2d_desc* desc, const void* packed, const int8_t* configs,
+                                               const int32_t* owner, const int16_t* cflips, int64_t n_rows,
+                                               const void* base_saved, int64_t base_saved_bytes, int64_t base_batch,
+                                               float* log_psi, void* workspace, int64_t workspace_bytes,
+                                               int64_t chunk, void* stream) {
+  FK_DISPATCH_FP16(desc, fk_ar2d_forward_connections_tc_fp16(desc, packed, configs, owner, cflips, n_rows, base_saved,
+                                                             base_saved_bytes, base_batch, log_psi, workspace,
+                                                             workspace_bytes, chunk, stream));
   NetLayout L;
   int st = build_layout(desc, &L);
   if (st != FK_OK) return st;
@@ -2133,7 +2151,7 @@ int fk_ar2d_forward_connections(const fk_ar2d_desc* desc, const void* packed, co
   FK_CHECK_ARG(workspace && workspace_bytes >= wneed, "fk_ar2d_forward_connections: workspace %lld < %lld bytes",
                (long long)workspace_bytes, (long long)wneed);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const bool tc = L.precision == FK_PRECISION_BF16;
+  const bool tc = L.precision != FK_PRECISION_FP32;
   switch (L.F) {
     case 16: return tc ? connections_impl<16, true>(L, packed, configs, owner, cflips, n_rows, B, log_psi, T, S, chunk, s)
                        : connections_impl<16, false>(L, packed, configs, owner, cflips, n_rows, B, log_psi, T, S, chunk, s);

@@ -12,9 +12,65 @@
 // reference's ZeroPadding2D).
 #pragma once
 
+#include <cuda_fp16.h>
+
 #include "fk_common.cuh"
 
-namespace fk {
+// The 16-bit operand format of the tensor-core path. Every translation unit of
+// the AR2D machine is compiled twice: as is (BF16 operands, namespace fk,
+// entry points fk_ar2d_*) and with FK_TC_FP16 defined (FP16 operands,
+// namespace fk16, entry points fk_ar2d_*_tc_fp16, which the BF16 build's
+// entry points call for FK_PRECISION_FP16). Both formats feed the same
+// kind::f16 MMAs with FP32 accumulation at the same rate; FP16 keeps 10
+// mantissa bits of every stored activation instead of 7.
+#ifdef FK_TC_FP16
+#define FK_NS fk16
+#define FK_AR2D_ENTRY(name) name##_tc_fp16
+#else
+#define FK_NS fk
+#define FK_AR2D_ENTRY(name) name
+#endif
+
+namespace FK_NS {
+
+using namespace ::fk;
+
+#ifdef FK_TC_FP16
+using tc16 = __half;
+constexpr uint32_t kTcFormatBits = 0u;           // A and B: F16
+constexpr uint32_t kTcOnePair = 0x3C003C00u;     // two fp16 1.0
+__device__ __forceinline__ uint32_t pack_tc16x2(float a, float b) {
+  __half2 h = __floats2half2_rn(a, b);
+  return *reinterpret_cast<uint32_t*>(&h);
+}
+__device__ __forceinline__ void unpack_tc16x8(uint4 u, float* f) {
+  const __half2* h = reinterpret_cast<const __half2*>(&u);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    float2 t = __half22float2(h[i]);
+    f[2 * i] = t.x;
+    f[2 * i + 1] = t.y;
+  }
+}
+__device__ __forceinline__ tc16 to_tc16(float x) { return __float2half_rn(x); }
+#else
+using tc16 = __nv_bfloat16;
+constexpr uint32_t kTcFormatBits = (1u << 7) | (1u << 10);  // A and B: BF16
+constexpr uint32_t kTcOnePair = 0x3F803F80u;                // two bf16 1.0
+__device__ __forceinline__ uint32_t pack_tc16x2(float a, float b) { return pack_bf16x2(a, b); }
+__device__ __forceinline__ void unpack_tc16x8(uint4 u, float* f) { unpack_bf16x8(u, f); }
+__device__ __forceinline__ tc16 to_tc16(float x) { return __float2bfloat16_rn(x); }
+#endif
+
+// Instruction descriptor of tcgen05.mma kind::f16 for this build's operand
+// format: D fp32, both operands K-major, shape M x N (x K=16).
+__host__ __device__ constexpr uint32_t umma_idesc_tc16(int m, int n) {
+  return (1u << 4) | kTcFormatBits | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+// Same with both operands MN-major.
+__host__ __device__ constexpr uint32_t umma_idesc_tc16_mn(int m, int n) {
+  return umma_idesc_tc16(m, n) | (1u << 15) | (1u << 16);
+}
 
 constexpr int kTile = 128;  // samples per tile = MMA M
 
@@ -115,19 +171,19 @@ __device__ __forceinline__ void ld8(const float* p, float* v) {
   v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
   v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
 }
-__device__ __forceinline__ void ld8(const __nv_bfloat16* p, float* v) {
-  unpack_bf16x8(*reinterpret_cast<const uint4*>(p), v);
+__device__ __forceinline__ void ld8(const tc16* p, float* v) {
+  unpack_tc16x8(*reinterpret_cast<const uint4*>(p), v);
 }
 __device__ __forceinline__ void st8(float* p, const float* v) {
   reinterpret_cast<float4*>(p)[0] = make_float4(v[0], v[1], v[2], v[3]);
   reinterpret_cast<float4*>(p)[1] = make_float4(v[4], v[5], v[6], v[7]);
 }
-__device__ __forceinline__ void st8(__nv_bfloat16* p, const float* v) {
+__device__ __forceinline__ void st8(tc16* p, const float* v) {
   uint4 u;
-  u.x = pack_bf16x2(v[0], v[1]);
-  u.y = pack_bf16x2(v[2], v[3]);
-  u.z = pack_bf16x2(v[4], v[5]);
-  u.w = pack_bf16x2(v[6], v[7]);
+  u.x = pack_tc16x2(v[0], v[1]);
+  u.y = pack_tc16x2(v[2], v[3]);
+  u.z = pack_tc16x2(v[4], v[5]);
+  u.w = pack_tc16x2(v[6], v[7]);
   *reinterpret_cast<uint4*>(p) = u;
 }
 
@@ -143,14 +199,14 @@ __device__ __forceinline__ void load_row(const T* block, int m, int c0, int n, f
 
 // Raw 16-byte chunks of thread row m's n channels (bf16), unpacked later.
 template <int N>
-__device__ __forceinline__ void load_raw(const __nv_bfloat16* block, int m, uint4* r) {
+__device__ __forceinline__ void load_raw(const tc16* block, int m, uint4* r) {
 #pragma unroll
   for (int g = 0; g < N / 8; ++g) r[g] = *reinterpret_cast<const uint4*>(block + ((int64_t)g * kTile + m) * 8);
 }
 template <int N>
 __device__ __forceinline__ void unpack_raw(const uint4* r, float* v) {
 #pragma unroll
-  for (int g = 0; g < N / 8; ++g) unpack_bf16x8(r[g], v + 8 * g);
+  for (int g = 0; g < N / 8; ++g) unpack_tc16x8(r[g], v + 8 * g);
 }
 
 // Tap offsets of the three ops (kernel element t = i*kw + j).
@@ -229,4 +285,35 @@ int launch_wgrad_tc(const WgTcArgs& a, int kw, int kcol0, float* dW, float* db, 
 int launch_bias_sum(const void* G, int64_t tiles, int H, int W, int g0, int n, int64_t batch, float* part, float* db,
                     cudaStream_t s);
 
-}  // namespace fk
+}  // namespace FK_NS
+
+#ifndef FK_TC_FP16
+// The FP16-operand build of the entry points (FK_PRECISION_FP16), called by
+// the entry points of this build; not part of the public header.
+extern "C" {
+int fk_ar2d_pack_tc_fp16(const fk_ar2d_desc* desc, const float* params, void* packed, void* stream);
+int fk_ar2d_forward_tc_fp16(const fk_ar2d_desc* desc, const void* packed, const int8_t* spins, int64_t batch,
+                            float* log_psi, float* cond, void* workspace, int64_t workspace_bytes, int32_t mode,
+                            void* stream);
+int fk_ar2d_sample_tc_fp16(const fk_ar2d_desc* desc, const void* packed, int64_t batch, uint64_t seed,
+                           uint64_t offset, int8_t* spins, float* log_psi, void* workspace, int64_t workspace_bytes,
+                           void* stream);
+int fk_ar2d_forward_connections_tc_fp16(const fk_ar2d_desc* desc, const void* packed, const int8_t* configs,
+                                        const int32_t* owner, const int16_t* cflips, int64_t n_rows,
+                                        const void* base_saved, int64_t base_saved_bytes, int64_t base_batch,
+                                        float* log_psi, void* workspace, int64_t workspace_bytes, int64_t chunk,
+                                        void* stream);
+int fk_ar2d_backward_tc_fp16(const fk_ar2d_desc* desc, const void* packed, const float* params, const int8_t* spins,
+                             int64_t batch, const float* w, const void* saved, int64_t saved_bytes, void* workspace,
+                             int64_t workspace_bytes, float* grad, float* per_sample, void* stream);
+}
+#define FK_DISPATCH_FP16(desc, call) \
+  do {                                \
+    if ((desc) && (desc)->precision == FK_PRECISION_FP16) return call; \
+  } while (0)
+#else
+#define FK_DISPATCH_FP16(desc, call) \
+  do {                                \
+  } while (0)
+#endif
+

@@ -24,7 +24,7 @@
 #include <stdlib.h>
 #include <string.h>
 
-namespace fk {
+namespace FK_NS {
 
 __device__ __forceinline__ void load_g(const float* t, int64_t tile, int P, int pix, int C, int m, int c0, int n,
                                        float* v) {
@@ -729,13 +729,13 @@ static bool use_tc_adjoint(const NetLayout& L) {
     const char* e = getenv("FK_AR2D_ENGINE");
     v = (e && strcmp(e, "rowwise") == 0) ? 0 : 1;
   }
-  return v == 1 && L.precision == FK_PRECISION_BF16 && L.F == 32 && pipe_supported(L.F, L.W);
+  return v == 1 && L.precision != FK_PRECISION_FP32 && L.F == 32 && pipe_supported(L.F, L.W);
 }
 
 static int backward_tc(const NetLayout& L, const void* packed, const float* params, const int8_t* spins,
                        int64_t batch, const float* seeds, const Tensors& A, const TcBwdTensors& G, float* grad,
                        cudaStream_t s) {
-  using T = __nv_bfloat16;
+  using T = tc16;
   constexpr int F = 32;
   const int64_t tiles = (batch + kTile - 1) / kTile;
   const unsigned rows = (unsigned)(tiles * L.H);
@@ -862,23 +862,28 @@ static int backward_tc(const NetLayout& L, const void* packed, const float* para
   return FK_OK;
 }
 
-}  // namespace fk
+}  // namespace FK_NS
 
-using namespace fk;
+using namespace FK_NS;
 
 extern "C" {
 
+#ifndef FK_TC_FP16
 int64_t fk_ar2d_backward_workspace_bytes(const fk_ar2d_desc* desc, int64_t batch) {
   NetLayout L;
   if (build_layout(desc, &L) != FK_OK || batch < 0) return -1;
   const int64_t b = bwd_layout(L, batch, nullptr, nullptr);
-  const int64_t t = (L.precision == FK_PRECISION_BF16 && L.F == 32) ? tc_bwd_layout(L, batch, nullptr, nullptr) : 0;
+  const int64_t t = (L.precision != FK_PRECISION_FP32 && L.F == 32) ? tc_bwd_layout(L, batch, nullptr, nullptr) : 0;
   return b > t ? b : t;
 }
+#endif
 
-int fk_ar2d_backward(const fk_ar2d_desc* desc, const void* packed, const float* params, const int8_t* spins,
-                     int64_t batch, const float* w, const void* saved, int64_t saved_bytes, void* workspace,
-                     int64_t workspace_bytes, float* grad, float* per_sample, void* stream) {
+int FK_AR2D_ENTRY(fk_ar2d_backward)(const fk_ar2d_desc* desc, const void* packed, const float* params,
+                                    const int8_t* spins, int64_t batch, const float* w, const void* saved,
+                                    int64_t saved_bytes, void* workspace, int64_t workspace_bytes, float* grad,
+                                    float* per_sample, void* stream) {
+  FK_DISPATCH_FP16(desc, fk_ar2d_backward_tc_fp16(desc, packed, params, spins, batch, w, saved, saved_bytes,
+                                                  workspace, workspace_bytes, grad, per_sample, stream));
   NetLayout L;
   int st = build_layout(desc, &L);
   if (st != FK_OK) return st;
@@ -903,13 +908,13 @@ int fk_ar2d_backward(const fk_ar2d_desc* desc, const void* packed, const float* 
                (long long)workspace_bytes, (long long)gneed);
   float* O = per_sample;
   float* g = per_sample ? nullptr : grad;
-  const bool bf = L.precision == FK_PRECISION_BF16;
+  const bool bf = L.precision != FK_PRECISION_FP32;
   switch (L.F) {
-    case 16: return bf ? backward_impl<16, __nv_bfloat16>(L, packed, params, spins, batch, w, A, G, g, O, s)
+    case 16: return bf ? backward_impl<16, tc16>(L, packed, params, spins, batch, w, A, G, g, O, s)
                        : backward_impl<16, float>(L, packed, params, spins, batch, w, A, G, g, O, s);
-    case 32: return bf ? backward_impl<32, __nv_bfloat16>(L, packed, params, spins, batch, w, A, G, g, O, s)
+    case 32: return bf ? backward_impl<32, tc16>(L, packed, params, spins, batch, w, A, G, g, O, s)
                        : backward_impl<32, float>(L, packed, params, spins, batch, w, A, G, g, O, s);
-    default: return bf ? backward_impl<64, __nv_bfloat16>(L, packed, params, spins, batch, w, A, G, g, O, s)
+    default: return bf ? backward_impl<64, tc16>(L, packed, params, spins, batch, w, A, G, g, O, s)
                        : backward_impl<64, float>(L, packed, params, spins, batch, w, A, G, g, O, s);
   }
 }

@@ -30,7 +30,7 @@
 
 #include <string.h>
 
-namespace fk {
+namespace FK_NS {
 
 template <int F>
 struct BwdCfg {
@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) bwd_op_kernel(const __grid_co
                                                                  int64_t n_items, int* err) {
   using C = PipeCfg<F>;
   using BC = BwdCfg<F>;
-  using T = __nv_bfloat16;
+  using T = tc16;
   constexpr int F2 = F / 2;
   constexpr int NB = C::kNB;
   constexpr int NS = C::kNS;
@@ -118,7 +118,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) bwd_op_kernel(const __grid_co
     // Two MMAs per output: x half (K = gCatm channels 0..F/2) into chain
     // accumulator 2b, y half (channels F/2..F) into 2b + 1.
     if (chain && lane == 0) {
-      const uint32_t idesc_c = umma_idesc_bf16(128, F);
+      const uint32_t idesc_c = umma_idesc_tc16(128, F);
       const uint64_t ca0 = umma_sdesc(smem_u32(casm), 2048, 128);
       const uint64_t cw0 = umma_sdesc(smem_u32(cwsm), F * 16, 128);
       pwait(wbar, 0, err, abort);
@@ -280,7 +280,7 @@ __global__ void __launch_bounds__(kWgThreads, 1) wgrad_tc_kernel(const __grid_co
                                                                  int64_t n_items, int* err) {
   using C = WgCfg<F>;
   static_assert(F == 32, "the stacked-row MMA needs 4 blocks of 32 channels (M = 128)");
-  using T = __nv_bfloat16;
+  using T = tc16;
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t* xr = smem;                            // [kNX][4][kBlk]
   uint8_t* gr = smem + C::kNX * 4 * C::kBlk;     // [kNG + 2][kBlk]
@@ -324,7 +324,7 @@ __global__ void __launch_bounds__(kWgThreads, 1) wgrad_tc_kernel(const __grid_co
     const uint32_t tl = tmem + ((uint32_t)((warp % 4) * 32) << 16);
     for (int c0 = 0; c0 < 96; c0 += 16) tmem_zero16(tl + c0);
     tmem_st_wait();
-    const uint4 one8 = make_uint4(0x3F803F80u, 0x3F803F80u, 0x3F803F80u, 0x3F803F80u);  // bf16 1.0 x 8
+    const uint4 one8 = make_uint4(kTcOnePair, kTcOnePair, kTcOnePair, kTcOnePair);  // 1.0 x 8 in the 16-bit format
     for (int i = threadIdx.x - 128; i < C::kNX * (C::kBlk / 16); i += 128) {
       const int slot = i / (C::kBlk / 16), e = i % (C::kBlk / 16);
       reinterpret_cast<uint4*>(xr + (slot * 4 + 3) * C::kBlk)[e] = one8;
@@ -403,7 +403,7 @@ __global__ void __launch_bounds__(kWgThreads, 1) wgrad_tc_kernel(const __grid_co
           const int cb = x - dc0 < W - 1 ? x - dc0 : W - 1;
           if (ca <= cb) {
             const uint32_t gs = (gbase + (uint32_t)(ca - y_min)) % C::kNG;
-            const uint32_t idesc = umma_idesc_bf16_mn(128, (cb - ca + 1) * n);
+            const uint32_t idesc = umma_idesc_tc16_mn(128, (cb - ca + 1) * n);
             const uint32_t d = tmem + (uint32_t)((ca - wlo) * n);
             const uint32_t xs = gx % C::kNX;
 #pragma unroll
@@ -487,7 +487,7 @@ __global__ void wgrad_reduce_kernel(const float* part, int parts, int x_rows, in
 // Bias gradient, step 1: per tile (one CTA, thread = sample) the sum over
 // pixels of G[.., g0 + co], reduced over the tile's samples; step 2 sums the
 // tiles in order.
-__global__ void __launch_bounds__(128) bias_tile_kernel(const __nv_bfloat16* G, int P, int W, int g0, int n,
+__global__ void __launch_bounds__(128) bias_tile_kernel(const tc16* G, int P, int W, int g0, int n,
                                                         int64_t batch, float* part) {
   constexpr int F = 32;
   __shared__ float red[4][32];
@@ -501,7 +501,7 @@ __global__ void __launch_bounds__(128) bias_tile_kernel(const __nv_bfloat16* G, 
   if (tile * kTile + m < batch) {
     for (int pix = r * W; pix < (r + 1) * W; ++pix) {
       float v[F];
-      load_row(blk<__nv_bfloat16>(G, tile, P, pix, F), m, 0, F, v);
+      load_row(blk<tc16>(G, tile, P, pix, F), m, 0, F, v);
 #pragma unroll
       for (int c = 0; c < F; ++c) s[c] += v[c];
     }
@@ -588,11 +588,11 @@ int launch_wgrad_tc(const WgTcArgs& a, int kw, int kcol0, float* dW, float* db, 
 
 int launch_bias_sum(const void* G, int64_t tiles, int H, int W, int g0, int n, int64_t batch, float* part, float* db,
                     cudaStream_t s) {
-  bias_tile_kernel<<<(unsigned)(tiles * H), 128, 0, s>>>(static_cast<const __nv_bfloat16*>(G), H * W, W, g0, n, batch,
+  bias_tile_kernel<<<(unsigned)(tiles * H), 128, 0, s>>>(static_cast<const tc16*>(G), H * W, W, g0, n, batch,
                                                          part);
   FK_CUDA(launched());
   bias_reduce_kernel<<<1, 32, 0, s>>>(part, tiles * H, n, db);
   return check_cuda(launched(), "bias_reduce_kernel");
 }
 
-}  // namespace fk
+}  // namespace FK_NS

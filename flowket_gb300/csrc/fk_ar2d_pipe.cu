@@ -21,7 +21,7 @@
 // bitwise the same result.
 #include "fk_pipe.cuh"
 
-namespace fk {
+namespace FK_NS {
 
 // Forward-specific shared memory on top of the pipeline's ring and weights.
 template <int F>
@@ -43,7 +43,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) op_pipe_kernel(const __grid_c
   // on the device.
   using C = PipeCfg<F>;
   using FC = FwdCfg<F>;
-  using T = __nv_bfloat16;
+  using T = tc16;
   constexpr int F2 = F / 2;
   constexpr int NC2 = F2 < 16 ? 16 : F2;
   constexpr int NB = C::kNB;
@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) op_pipe_kernel(const __grid_c
     // The chained 1x1 MMA of each output, on the epilogue's staged bf16
     // activations, into one of NB chained accumulators.
     if (has_chain && lane == 0) {
-      const uint32_t idesc_c = umma_idesc_bf16(128, cnp);
+      const uint32_t idesc_c = umma_idesc_tc16(128, cnp);
       const uint64_t ca0 = umma_sdesc(smem_u32(casm), 2048, 128);
       const uint64_t cw0 = umma_sdesc(smem_u32(cwsm), cnp * 16, 128);
       pwait(wbar, 0, err, abort);
@@ -381,4 +381,4 @@ static_assert(FwdCfg<32>::kSmemBase + 16 * kTile * 8 <= 227 * 1024, "pipelined e
 static_assert(FwdCfg<16>::kSmemBase + 16 * kTile * 8 <= 227 * 1024, "pipelined engine exceeds shared memory");
 static_assert(3 * 32 <= 256 && PipeCfg<16>::kNS * 16 <= 256, "TMEM layout");
 
-}  // namespace fk
+}  // namespace FK_NS

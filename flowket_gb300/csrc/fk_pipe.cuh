@@ -26,7 +26,7 @@
 
 #include "fk_ar2d.cuh"
 
-namespace fk {
+namespace FK_NS {
 
 template <int F>
 struct PipeCfg {
@@ -145,7 +145,7 @@ __device__ void pipe_producer(const PipeGeom& g, const PipeItems& items, const v
       mbar_arrive_expect_tx(&full[slot], (uint32_t)(k_hi - k_lo + 1) * C::kBlk);
       for (int k = k_lo; k <= k_hi; ++k)
         bulk_g2s(ring + (slot * 3 + k) * C::kBlk,
-                 blk<__nv_bfloat16>(in, tile, P, (r + g.row0 + k) * g.W + x, F), C::kBlk, &full[slot]);
+                 blk<tc16>(in, tile, P, (r + g.row0 + k) * g.W + x, F), C::kBlk, &full[slot]);
     }
   }
 }
@@ -241,9 +241,9 @@ __device__ void pipe_issuer(const PipeGeom& g, const PipeItems& items, uint8_t* 
   constexpr int NR = C::kNcol;
   constexpr int NS = C::kNS;
   const int lane = threadIdx.x % 32;
-  const uint32_t idesc1 = umma_idesc_bf16(128, F);
-  const uint32_t idesc2 = umma_idesc_bf16(128, 2 * F);
-  const uint32_t idesc3 = umma_idesc_bf16(128, 3 * F);
+  const uint32_t idesc1 = umma_idesc_tc16(128, F);
+  const uint32_t idesc2 = umma_idesc_tc16(128, 2 * F);
+  const uint32_t idesc3 = umma_idesc_tc16(128, 3 * F);
   const uint64_t a0 = umma_sdesc(smem_u32(ring), 2048, 128);
   const uint64_t w0 = umma_sdesc(smem_u32(wsm), 3 * F * 16, 128);
   constexpr uint32_t kBlk16 = C::kBlk >> 4;           // one ring block
@@ -327,4 +327,4 @@ __device__ void pipe_issuer(const PipeGeom& g, const PipeItems& items, uint8_t* 
   }
 }
 
-}  // namespace fk
+}  // namespace FK_NS

@@ -30,6 +30,8 @@ extern "C" {
 
 #define FK_PRECISION_FP32 0     /* plain FP32 CUDA-core path */
 #define FK_PRECISION_BF16 1     /* BF16 tcgen05 tensor-core path, FP32 accumulate */
+#define FK_PRECISION_FP16 2     /* the same tensor-core path with FP16 operands and stored
+                                   activations (10 mantissa bits instead of 7), FP32 accumulate */
 
 #define FK_AR2D_INFER 0         /* forward keeps only a rolling set of activations */
 #define FK_AR2D_SAVE 1          /* forward keeps every activation for the adjoint */
@@ -108,7 +110,7 @@ typedef struct fk_ar2d_desc {
   int32_t depth;                 /* ConvNetAutoregressive2D depth, >= 2 */
   int32_t channels;              /* num_of_channels: 16, 32 or 64 */
   int32_t weights_normalization; /* 1 = WeightNormalization(exponential_norm=True) */
-  int32_t precision;             /* FK_PRECISION_FP32 or FK_PRECISION_BF16 */
+  int32_t precision;             /* FK_PRECISION_FP32, FK_PRECISION_BF16 or FK_PRECISION_FP16 */
   int32_t equal_up_down_spins;   /* 1 = EqualUpDownSpins mask before the normalisation
                                     (abstract_machine.py:52-53, layers/spins_invariants.py:13-22):
                                     outcome k of a site gets log-amplitude -inf once N/2 earlier

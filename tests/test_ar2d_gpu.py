@@ -68,7 +68,7 @@ def test_conditionals_fp32(cuda):
     np.testing.assert_allclose(got, 2 * re.numpy(), atol=2e-5)
 
 
-@pytest.mark.parametrize("precision", ["fp32", "bf16"])
+@pytest.mark.parametrize("precision", ["fp32", "bf16", "fp16"])
 def test_distribution_normalised_4x4(cuda, precision):
     """tests/test_autoregressive.py:18-30 on the GPU path: sum |psi|^2 = 1."""
     m = _machine((4, 4), 4, 16, False, precision)
@@ -78,7 +78,7 @@ def test_distribution_normalised_4x4(cuda, precision):
     assert total == pytest.approx(1.0, abs=1e-5 if precision == "fp32" else 1e-3)
 
 
-@pytest.mark.parametrize("precision", ["fp32", "bf16"])
+@pytest.mark.parametrize("precision", ["fp32", "bf16", "fp16"])
 def test_sampler_reproduces_oracle_draw(cuda, precision):
     """Same Philox uniforms -> the same samples as the oracle's raster sampler
     run on this machine's own conditionals; sampler log psi == forward log psi."""
@@ -109,7 +109,7 @@ def test_sampler_reproduces_oracle_draw(cuda, precision):
     assert np.array_equal(fwd, samp)
 
 
-@pytest.mark.parametrize("precision", ["fp32", "bf16"])
+@pytest.mark.parametrize("precision", ["fp32", "bf16", "fp16"])
 def test_sampler_matches_exact_distribution(cuda, precision):
     """tests/test_samplers.py:49-82: closeness statistic z <= sqrt(n) against
     |psi|^2 enumerated with the same machine."""
@@ -128,8 +128,9 @@ def test_sampler_matches_exact_distribution(cuda, precision):
     assert z <= np.sqrt(n), z
 
 
+@pytest.mark.parametrize("precision", ["bf16", "fp16"])
 @pytest.mark.parametrize("f", [16, 32])
-def test_pipelined_engine_equals_per_pixel_engine(cuda, f, tmp_path):
+def test_pipelined_engine_equals_per_pixel_engine(cuda, f, precision, tmp_path):
     """The persistent pipelined tensor-core engine and the per-pixel engine
     give bitwise the same log psi (same MMA sequence, same epilogue)."""
     import subprocess
@@ -137,39 +138,42 @@ def test_pipelined_engine_equals_per_pixel_engine(cuda, f, tmp_path):
     code = (
         "import sys, numpy as np, torch; sys.path.insert(0, %r);"
         "from flowket_gb300.machines import ConvNetAutoregressive2D;"
-        "m = ConvNetAutoregressive2D((5, 7), 4, %d, weights_normalization=True, precision='bf16', seed=3);"
+        "m = ConvNetAutoregressive2D((5, 7), 4, %d, weights_normalization=True, precision=%r, seed=3);"
         "s = torch.as_tensor(np.random.default_rng(9).choice([-1, 1], size=(700, 5, 7)).astype(np.int8)).cuda();"
         "np.save(%r, m.log_psi(s).cpu().numpy())"
-    ) % (str(__import__("os").path.dirname(__import__("os").path.dirname(__file__))), f, str(tmp_path / "a.npy"))
+    ) % (str(__import__("os").path.dirname(__import__("os").path.dirname(__file__))), f, precision,
+         str(tmp_path / "a.npy"))
     env = dict(__import__("os").environ, FK_AR2D_ENGINE="rowwise")
     subprocess.run([sys.executable, "-c", code], check=True, env=env)
     ref = np.load(tmp_path / "a.npy")
-    m = _machine((5, 7), 4, f, True, "bf16", seed=3)
+    m = _machine((5, 7), 4, f, True, precision, seed=3)
     s = torch.as_tensor(np.random.default_rng(9).choice([-1, 1], size=(700, 5, 7)).astype(np.int8)).cuda()
     got = m.log_psi(s).cpu().numpy()
     assert np.array_equal(got, ref)
 
 
+@pytest.mark.parametrize("precision", ["bf16", "fp16"])
 @pytest.mark.parametrize("shape,f", [((3, 20), 32), ((2, 40), 16)])
-def test_sampler_wide_rows_equals_forward(cuda, shape, f):
+def test_sampler_wide_rows_equals_forward(cuda, shape, f, precision):
     """Rows wider than the TMEM holds at once (W * F > 512): the sampler's
     row-end V ops fall back to one op per pixel; log psi stays bitwise equal
     to the forward's and the draw follows the model (normalised conditionals)."""
     from flowket_gb300.samplers import FastAutoregressiveSampler
-    m = _machine(shape, 3, f, True, "bf16")
+    m = _machine(shape, 3, f, True, precision)
     spins, lp, _ = FastAutoregressiveSampler(m, 200, seed=5).sample()
     fwd, _, _ = m.forward(spins)
     assert torch.equal(fwd, lp)
     assert torch.all(torch.isfinite(lp))
 
 
+@pytest.mark.parametrize("precision", ["bf16", "fp16"])
 @pytest.mark.parametrize("updown", [False, True])
-def test_sampler_f64_equals_forward(cuda, updown):
+def test_sampler_f64_equals_forward(cuda, updown, precision):
     """F = 64 runs the sampler's per-pixel ops; log psi bitwise equal to the
     forward's, with and without the EqualUpDownSpins mask."""
     from flowket_gb300.machines import ConvNetAutoregressive2D
     from flowket_gb300.samplers import FastAutoregressiveSampler
-    m = ConvNetAutoregressive2D((4, 4), 2, 64, weights_normalization=True, precision="bf16", seed=3,
+    m = ConvNetAutoregressive2D((4, 4), 2, 64, weights_normalization=True, precision=precision, seed=3,
                                 equal_up_down_spins=updown)
     spins, lp, _ = FastAutoregressiveSampler(m, 256, seed=9).sample()
     fwd, _, _ = m.forward(spins)

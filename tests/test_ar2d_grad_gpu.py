@@ -77,7 +77,7 @@ def test_per_sample_rows_match_autograd(cuda):
     np.testing.assert_allclose(o.real @ w[:, 0] + o.imag @ w[:, 1], summed, rtol=1e-3, atol=1e-5)
 
 
-@pytest.mark.parametrize("precision", ["fp32", "bf16"])
+@pytest.mark.parametrize("precision", ["fp32", "bf16", "fp16"])
 def test_sampler_activations_feed_the_adjoint(cuda, precision):
     """The sampler's workspace holds the same activations as a forward pass."""
     from flowket_gb300 import _lib
@@ -92,8 +92,9 @@ def test_sampler_activations_feed_the_adjoint(cuda, precision):
     assert torch.equal(g1, g2)
 
 
+@pytest.mark.parametrize("precision", ["bf16", "fp16"])
 @pytest.mark.parametrize("shape,depth", [((5, 7), 4), ((10, 10), 10)])
-def test_tensor_core_adjoint_matches_cuda_core_adjoint(cuda, tmp_path, shape, depth):
+def test_tensor_core_adjoint_matches_cuda_core_adjoint(cuda, tmp_path, shape, depth, precision):
     """F = 32, BF16: the tcgen05 adjoint (bf16 gradients between ops,
     deterministic sums) against the CUDA-core adjoint on the same saved
     activations (FK_AR2D_ENGINE=rowwise selects the CUDA-core adjoint and the
@@ -104,19 +105,19 @@ def test_tensor_core_adjoint_matches_cuda_core_adjoint(cuda, tmp_path, shape, de
         "import numpy as np, torch;"
         "from flowket_gb300 import _lib;"
         "from flowket_gb300.machines import ConvNetAutoregressive2D;"
-        "m = ConvNetAutoregressive2D(%r, %d, 32, weights_normalization=True, precision='bf16', seed=5);"
+        "m = ConvNetAutoregressive2D(%r, %d, 32, weights_normalization=True, precision=%r, seed=5);"
         "rng = np.random.default_rng(6);"
         "s = torch.as_tensor(rng.choice([-1, 1], size=(300,) + %r).astype(np.int8)).cuda();"
         "w = torch.as_tensor(rng.normal(size=(300, 2)).astype(np.float32)).cuda();"
         "_, _, saved = m.forward(s, mode=_lib.FK_AR2D_SAVE);"
         "np.save(%r, m.backward(s, w, saved).cpu().numpy())"
-    ) % (root, shape, depth, shape, str(tmp_path / "g.npy"))
+    ) % (root, shape, depth, precision, shape, str(tmp_path / "g.npy"))
     env = dict(os.environ, FK_AR2D_ENGINE="rowwise")
     subprocess.run([sys.executable, "-c", code], check=True, env=env)
     ref = np.load(tmp_path / "g.npy").astype(np.float64)
     from flowket_gb300 import _lib
     from flowket_gb300.machines import ConvNetAutoregressive2D
-    m = ConvNetAutoregressive2D(shape, depth, 32, weights_normalization=True, precision="bf16", seed=5)
+    m = ConvNetAutoregressive2D(shape, depth, 32, weights_normalization=True, precision=precision, seed=5)
     rng = np.random.default_rng(6)
     s = torch.as_tensor(rng.choice([-1, 1], size=(300,) + shape).astype(np.int8)).cuda()
     w = torch.as_tensor(rng.normal(size=(300, 2)).astype(np.float32)).cuda()
@@ -131,7 +132,7 @@ def test_tensor_core_adjoint_matches_cuda_core_adjoint(cuda, tmp_path, shape, de
 
 
 @pytest.mark.parametrize("recompute", [None, 48])
-@pytest.mark.parametrize("precision", ["fp32", "bf16"])
+@pytest.mark.parametrize("precision", ["fp32", "bf16", "fp16"])
 def test_autograd_function_equals_machine_backward(cuda, precision, recompute):
     """torch.autograd through Ar2dLogPsi (with and without chunked activation
     recomputation) gives the gradient of m.backward on the same seeds."""

@@ -62,7 +62,8 @@ def test_vmc_step_decreases_energy_heisenberg_4x4(cuda):
     assert set(vmc.times) == {"sampling", "local_energy", "gradient", "update"}
 
 
-@pytest.mark.parametrize("precision,which", [("bf16", 0), ("bf16", 1), ("fp32", 2), ("bf16", 2)])
+@pytest.mark.parametrize("precision,which", [("bf16", 0), ("bf16", 1), ("fp32", 2), ("bf16", 2), ("fp16", 0),
+                                             ("fp16", 2)])
 def test_causal_reuse_equals_full_forward(cuda, precision, which):
     """Connected configurations evaluated from the base samples' saved
     activations (rows >= first flipped row only) give bitwise the full forward."""
