@@ -62,12 +62,15 @@ def parse():
     p.add_argument("--cpu-samples", type=int, default=128,
                    help="samples of one VMC step per timed CPU step (reference arm and cpu_baseline)")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--case", default="vmc", choices=["vmc", "forward", "energy4x4", "vmc16", "ising12", "matched"],
+    p.add_argument("--case", default="vmc", choices=["vmc", "forward", "energy4x4", "vmc16", "ising12", "matched",
+                                                     "j1j2sr", "chain64"],
                    help="forward: only the batched AR2D forward of the local-energy stage on --configs "
                         "connected configurations (the small case used for ncu captures); energy4x4: train "
                         "the 4x4 Heisenberg model (depth 5, 16 channels) and compare its exact energy "
                         "(enumeration of all 2^16 states) with Lanczos, in --precision")
-    p.add_argument("--precision", default="bf16", choices=["bf16", "fp32"])
+    p.add_argument("--precision", default="bf16", choices=["bf16", "fp16", "fp32"])
+    p.add_argument("--sr-steps", type=int, default=20)
+    p.add_argument("--sweeps", type=int, default=2000)
     p.add_argument("--train-steps", type=int, default=24000)
     p.add_argument("--train-batch", type=int, default=2048)
     p.add_argument("--configs", type=int, default=32768)
@@ -199,6 +202,109 @@ def matched_case(args):
     samples, energies from `--samples` fresh samples each."""
     out = {"case": "matched", "workload": WORKLOAD}
     out.update(matched_summary(args.train_steps, args.batch, args.samples))
+    print(json.dumps(out), flush=True)
+
+
+def j1j2sr_case(args):
+    """J1-J2 10x10 periodic, J2/J1 = 0.5 (operators/j1j2.py edge list);
+    ConvNetAutoregressive2D depth 20, 32 channels (weight norm), Re and Im
+    heads; 1024 exact samples per step; stochastic reconfiguration
+    (diag_shift 1e-3, lr 0.05, FP32 Gram reduced in FP64, FP64 CG). Runs
+    `--sr-steps` full steps (sampling, local energy over the used
+    connections, per-sample log-derivatives, Gram, solve, update) on each
+    precision from the same seeded parameters: ms per step, stage split,
+    energy and variance per step."""
+    from flowket_gb300.machines import ConvNetAutoregressive2D
+    from flowket_gb300.operators import J1J2
+    from flowket_gb300.optimization import VariationalMonteCarlo
+    from flowket_gb300.optimizers import ComplexValuesStochasticReconfiguration
+    from flowket_gb300.samplers import FastAutoregressiveSampler
+    shape, b = (10, 10), 1024
+    op = J1J2(hilbert_state_shape=shape, j2=0.5, pbc=True)
+    out = {"case": "j1j2sr", "workload": "J1-J2 10x10 PBC J2=0.5; ConvNetAutoregressive2D depth 20 F32 (weight "
+                                         "norm); 1024 samples/step; SR diag_shift 1e-3 lr 0.05", "steps": args.sr_steps}
+    for prec in ("bf16", "fp16", "fp32"):
+        m = ConvNetAutoregressive2D(shape, 20, 32, weights_normalization=True, precision=prec, seed=0)
+        vmc = VariationalMonteCarlo(m, op, FastAutoregressiveSampler(m, b, seed=1234))
+        opt = ComplexValuesStochasticReconfiguration(m, lr=0.05, diag_shift=1e-3)
+        vmc.step(opt)
+        energies, variances, ms, stages = [], [], [], []
+        for _ in range(args.sr_steps):
+            a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            vmc.step(opt)
+            e.record()
+            torch.cuda.synchronize()
+            ms.append(a.elapsed_time(e))
+            stages.append(vmc.times)
+            energies.append(vmc.current_energy.real)
+            variances.append(vmc.current_local_energy_variance)
+        out[prec] = {"ms_per_step": float(np.mean(ms)), "steps_per_s": 1e3 / float(np.mean(ms)),
+                     "samples_per_s": b / (float(np.mean(ms)) / 1e3),
+                     "stage_ms": {k: float(np.mean([st[k] for st in stages])) for k in stages[0]},
+                     "energy_first": energies[0], "energy_last": energies[-1], "energies": energies,
+                     "variance_last": variances[-1], "cg_iterations_last": float(opt.last_stats[0].item()),
+                     "num_params": m.num_params}
+        del m, vmc, opt
+        torch.cuda.empty_cache()
+    out["bf16_over_fp32"] = out["fp32"]["ms_per_step"] / out["bf16"]["ms_per_step"]
+    out["fp16_over_fp32"] = out["fp32"]["ms_per_step"] / out["fp16"]["ms_per_step"]
+    print(json.dumps(out), flush=True)
+
+
+def chain64_case(args):
+    """Heisenberg chain L=64 periodic (Marshall sign); RBM alpha=4 with
+    complex weights N(0, 0.01); 256 Metropolis-Hastings chains with local
+    exchange moves, `--sweeps` sweeps per chain (one proposal per chain per
+    sweep, a sample recorded every 20 sweeps), the plain sampler; then the
+    learned independent proposal (ConvNetAutoregressive2D on 1 x 64, depth 4,
+    16 channels, BF16) fitted to the plain chains' samples by maximum
+    likelihood with the project's forward, adjoint and Adam kernels, run for
+    the same number of recorded samples with the exact |psi|^2 q ratio
+    acceptance. Reports each sampler's energy, its error bar with the
+    integrated autocorrelation time (metropolis_hastings.py:67-89), the
+    acceptance ratio and the time."""
+    from flowket_gb300.machines import RBM, ConvNetAutoregressive2D
+    from flowket_gb300.operators import Heisenberg
+    from flowket_gb300.samplers import (MetropolisHastingsExchange, MetropolisHastingsIndependent,
+                                        r_hat_and_correlations)
+    L, chains, every = 64, 256, 20
+    spc = max(2, args.sweeps // every)
+    op = Heisenberg(hilbert_state_shape=(L,), pbc=True)
+    m = RBM((L,), alpha=4, stddev=0.01, seed=0)
+    out = {"case": "chain64", "workload": "Heisenberg chain L=64 PBC; RBM alpha=4 complex N(0, 0.01); 256 chains",
+           "sweeps_per_chain": spc * every, "samples_per_chain": spc}
+
+    def summary(samples, seconds, acc):
+        e = m.local_energy(op, samples)[:, 0]
+        r_hat, var, cs, ess = r_hat_and_correlations(e, chains)
+        tau = 1 + 2 * cs
+        mean = float(e.mean())
+        return {"energy": mean, "stderr_iat": math.sqrt(var * tau / e.numel()), "tau_int": tau, "r_hat": r_hat,
+                "ess": ess, "acceptance": acc, "seconds": seconds}
+
+    plain = MetropolisHastingsExchange(m, chains * spc, num_of_chains=chains, unused_sampels=every - 1,
+                                       discard_ratio=5, seed=7)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    plain_samples = next(plain)
+    torch.cuda.synchronize()
+    out["plain"] = summary(plain_samples, time.perf_counter() - t0, plain.update_acceptance_ratio())
+    q = ConvNetAutoregressive2D((1, L), 4, 16, weights_normalization=True, precision="bf16", seed=8)
+    ind = MetropolisHastingsIndependent(m, q, chains * spc, chains, seed=9, init_chains=plain.sample.clone())
+    t0 = time.perf_counter()
+    ind.fit_proposal(plain_samples, steps=400, lr=3e-3, batch=4096)
+    torch.cuda.synchronize()
+    fit_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    ind_samples = next(ind)
+    torch.cuda.synchronize()
+    out["learned"] = summary(ind_samples, time.perf_counter() - t0, ind.update_acceptance_ratio())
+    out["learned"]["fit_seconds"] = fit_s
+    out["learned"]["mean_log_likelihood"] = ind.mean_log_likelihood(plain_samples)
+    d = abs(out["plain"]["energy"] - out["learned"]["energy"])
+    out["energy_difference_in_sigma"] = d / math.hypot(out["plain"]["stderr_iat"], out["learned"]["stderr_iat"])
+    out["tau_ratio_learned_over_plain"] = out["learned"]["tau_int"] / out["plain"]["tau_int"]
     print(json.dumps(out), flush=True)
 
 
@@ -635,6 +741,10 @@ def main():
         ising12_case(args)
     elif args.case == "matched":
         matched_case(args)
+    elif args.case == "j1j2sr":
+        j1j2sr_case(args)
+    elif args.case == "chain64":
+        chain64_case(args)
     elif args.impl == "reference":
         reference_arm(args, rank, world)
     else:
