@@ -63,17 +63,24 @@ def parse():
                    help="samples of one VMC step per timed CPU step (reference arm and cpu_baseline)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--case", default="vmc", choices=["vmc", "forward", "energy4x4", "vmc16", "ising12", "matched",
-                                                     "j1j2sr", "chain64"],
+                                                     "j1j2sr", "chain64", "kernels"],
                    help="forward: only the batched AR2D forward of the local-energy stage on --configs "
                         "connected configurations (the small case used for ncu captures); energy4x4: train "
                         "the 4x4 Heisenberg model (depth 5, 16 channels) and compare its exact energy "
                         "(enumeration of all 2^16 states) with Lanczos, in --precision")
     p.add_argument("--precision", default="bf16", choices=["bf16", "fp16", "fp32"])
     p.add_argument("--sr-steps", type=int, default=20)
+    p.add_argument("--precisions", nargs="+", default=None, choices=["bf16", "fp16", "fp32"])
+    p.add_argument("--optimizer", default="adam", choices=["adam", "sr"])
+    p.add_argument("--lr", type=float, default=0.02)
+    p.add_argument("--diag-shift", type=float, default=1e-3)
     p.add_argument("--sweeps", type=int, default=2000)
     p.add_argument("--train-steps", type=int, default=24000)
     p.add_argument("--train-batch", type=int, default=2048)
     p.add_argument("--configs", type=int, default=32768)
+    p.add_argument("--lattice", type=int, nargs=2, default=None)
+    p.add_argument("--depth", type=int, default=None)
+    p.add_argument("--channels", type=int, default=None)
     p.add_argument("--batch", type=int, default=8192)
     p.add_argument("--weights", default=None, help="ising12: a Keras weight file of the reference's 12x12 models")
     p.add_argument("--gamma", type=float, default=3.0)
@@ -83,11 +90,14 @@ def parse():
 
 def forward_case(args):
     """The AR2D forward of the local-energy stage alone, on `configs`
-    configurations of the bench workload's network."""
+    configurations of the bench workload's network (or of the network given
+    by --lattice/--depth/--channels), in --precision."""
     from flowket_gb300.machines import ConvNetAutoregressive2D
-    m = ConvNetAutoregressive2D(SHAPE, DEPTH, CHANNELS, weights_normalization=True, precision="bf16", seed=0)
+    shape = tuple(args.lattice) if args.lattice else SHAPE
+    depth, f = args.depth or DEPTH, args.channels or CHANNELS
+    m = ConvNetAutoregressive2D(shape, depth, f, weights_normalization=True, precision=args.precision, seed=0)
     g = torch.Generator(device="cuda").manual_seed(0)
-    spins = (2 * torch.randint(0, 2, (args.configs,) + SHAPE, device="cuda", generator=g) - 1).to(torch.int8)
+    spins = (2 * torch.randint(0, 2, (args.configs,) + shape, device="cuda", generator=g) - 1).to(torch.int8)
     for _ in range(args.warmup):
         m.forward(spins)
     torch.cuda.synchronize()
@@ -98,8 +108,9 @@ def forward_case(args):
     b.record()
     torch.cuda.synchronize()
     ms = a.elapsed_time(b) / args.steps
-    fl = flops_per_sample_forward(SHAPE, DEPTH, CHANNELS) * args.configs
-    print(json.dumps({"case": "forward", "configs": args.configs, "ms_per_forward": ms,
+    fl = flops_per_sample_forward(shape, depth, f) * args.configs
+    print(json.dumps({"case": "forward", "lattice": list(shape), "depth": depth, "channels": f,
+                      "precision": args.precision, "configs": args.configs, "ms_per_forward": ms,
                       "tflops": fl / (ms / 1e3) / 1e12}), flush=True)
 
 
@@ -223,7 +234,8 @@ def j1j2sr_case(args):
     op = J1J2(hilbert_state_shape=shape, j2=0.5, pbc=True)
     out = {"case": "j1j2sr", "workload": "J1-J2 10x10 PBC J2=0.5; ConvNetAutoregressive2D depth 20 F32 (weight "
                                          "norm); 1024 samples/step; SR diag_shift 1e-3 lr 0.05", "steps": args.sr_steps}
-    for prec in ("bf16", "fp16", "fp32"):
+    precisions = args.precisions or ["bf16", "fp16", "fp32"]
+    for prec in precisions:
         m = ConvNetAutoregressive2D(shape, 20, 32, weights_normalization=True, precision=prec, seed=0)
         vmc = VariationalMonteCarlo(m, op, FastAutoregressiveSampler(m, b, seed=1234))
         opt = ComplexValuesStochasticReconfiguration(m, lr=0.05, diag_shift=1e-3)
@@ -247,8 +259,9 @@ def j1j2sr_case(args):
                      "num_params": m.num_params}
         del m, vmc, opt
         torch.cuda.empty_cache()
-    out["bf16_over_fp32"] = out["fp32"]["ms_per_step"] / out["bf16"]["ms_per_step"]
-    out["fp16_over_fp32"] = out["fp32"]["ms_per_step"] / out["fp16"]["ms_per_step"]
+    for prec in ("bf16", "fp16"):
+        if prec in out and "fp32" in out:
+            out[prec + "_over_fp32"] = out["fp32"]["ms_per_step"] / out[prec]["ms_per_step"]
     print(json.dumps(out), flush=True)
 
 
@@ -305,6 +318,137 @@ def chain64_case(args):
     d = abs(out["plain"]["energy"] - out["learned"]["energy"])
     out["energy_difference_in_sigma"] = d / math.hypot(out["plain"]["stderr_iat"], out["learned"]["stderr_iat"])
     out["tau_ratio_learned_over_plain"] = out["learned"]["tau_int"] / out["plain"]["tau_int"]
+    print(json.dumps(out), flush=True)
+
+
+def kernels_case(args):
+    """The memory-bound and FP64 kernels of the path on their own, sized
+    beyond L2 (129 MB) where the kernel streams: CUDA-event time per launch
+    (best of `--steps` after `--warmup`), algorithmic bytes (or FLOPs) per
+    launch and the fraction of the measured HBM copy bandwidth (or of the
+    cuBLAS SGEMM rate for the FP32 Gram). The small case of the per-kernel
+    ncu captures."""
+    from flowket_gb300 import _lib
+    from flowket_gb300.machines import ConvNetAutoregressive2D
+    from flowket_gb300.observables import Observable, energy_stats
+    from flowket_gb300.operators import Heisenberg, Ising
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm = peaks.get("hbm_gbs") or 6800.0
+    g = torch.Generator(device="cuda").manual_seed(0)
+    st = _lib.stream_ptr()
+    out = {"case": "kernels", "hbm_peak_gbs": hbm}
+
+    def timed(fn):
+        for _ in range(max(1, args.warmup)):
+            fn()
+        best = float("inf")
+        for _ in range(max(1, args.steps)):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            torch.cuda.synchronize()
+            best = min(best, a.elapsed_time(b))
+        return best
+
+    def record(name, ms, nbytes=None, flops=None, peak=None, unit=None, **kw):
+        r = {"ms": ms, **kw}
+        if nbytes is not None:
+            r.update(bytes=nbytes, gbs=nbytes / (ms / 1e3) / 1e9, frac_hbm=nbytes / (ms / 1e3) / 1e9 / hbm)
+        if flops is not None:
+            r.update(flops=flops, tflops=flops / (ms / 1e3) / 1e12)
+            if peak:
+                r.update(frac=flops / (ms / 1e3) / 1e12 / peak, peak=peak, peak_unit=unit)
+        out[name] = r
+
+    # enumeration: Ising 10x10 (101 slots) and Heisenberg 16x16 (513 slots)
+    for name, op, shape, b in (("enum_ising_10x10", Ising(h=3.0, hilbert_state_shape=(10, 10), pbc=True), (10, 10),
+                                1 << 18),
+                               ("enum_heisenberg_16x16", Heisenberg(hilbert_state_shape=(16, 16), pbc=True),
+                                (16, 16), 1 << 16)):
+        spins = (2 * torch.randint(0, 2, (b,) + shape, device="cuda", generator=g) - 1).to(torch.int8)
+        flat = spins.view(b, -1)
+        c = op.max_number_of_local_connections
+        flips = torch.empty((c, b, 2), dtype=torch.int16, device="cuda")
+        mel = torch.empty((c, b), dtype=torch.float64, device="cuda")
+        use = torch.empty((c, b), dtype=torch.uint8, device="cuda")
+        ms = timed(lambda: op._launch(flat, b, flips, mel, use, None))
+        record(name, ms, nbytes=b * (flat.shape[1] + c * 13), samples=b, slots=c)
+        if name.startswith("enum_heisenberg"):
+            max_rows = b * (c - 1)
+            bf = {"owner": torch.empty(max_rows, dtype=torch.int32, device="cuda"),
+                  "cmel": torch.empty(max_rows, dtype=torch.float64, device="cuda"),
+                  "cflips": torch.empty((max_rows, 2), dtype=torch.int16, device="cuda"),
+                  "offsets": torch.empty(b + 1, dtype=torch.int64, device="cuda"),
+                  "nrows": torch.empty(1, dtype=torch.int64, device="cuda"),
+                  "ws": torch.empty(_lib.load().fk_compact_workspace_bytes(b), dtype=torch.uint8, device="cuda")}
+
+            def compact():
+                _lib.call("fk_compact_connections", _lib.ptr(flat), b, flat.shape[1], c, _lib.ptr(flips),
+                          _lib.ptr(mel), _lib.ptr(use), 1, None, _lib.ptr(bf["owner"]), _lib.ptr(bf["cmel"]),
+                          _lib.ptr(bf["cflips"]), _lib.ptr(bf["offsets"]), b * (c - 1), _lib.ptr(bf["nrows"]),
+                          _lib.ptr(bf["ws"]), bf["ws"].numel(), st)
+            ms = timed(compact)
+            rows = int(bf["nrows"].item())
+            record("compact_heisenberg_16x16", ms, nbytes=b * c * 13 + rows * (4 + 8 + 4) + (b + 1) * 8, rows=rows)
+    # local-energy reduction: 2^18 samples x 100 rows
+    b, per = 1 << 18, 100
+    rows = b * per
+    lp_self = torch.randn((b, 2), device="cuda", generator=g) * 0.1 - 30.0
+    lp_rows = torch.randn((rows, 2), device="cuda", generator=g) * 0.1 - 30.0
+    mel0 = torch.randn(b, device="cuda", dtype=torch.float64, generator=g)
+    cmel = torch.full((rows,), -3.0, device="cuda", dtype=torch.float64)
+    offsets = torch.arange(0, rows + 1, per, device="cuda", dtype=torch.int64)
+    local = torch.empty((b, 2), device="cuda", dtype=torch.float64)
+    ms = timed(lambda: _lib.call("fk_local_energy_reduce", _lib.ptr(lp_self), _lib.ptr(mel0), b, _lib.ptr(lp_rows),
+                                 _lib.ptr(offsets), _lib.ptr(cmel), _lib.ptr(local), st))
+    record("local_energy_reduce", ms, nbytes=b * (8 + 8 + 8 + 16) + rows * 16, samples=b, rows=rows)
+    ms = timed(lambda: energy_stats(local))
+    record("energy_stats", ms, nbytes=b * (16 + 16 + 8), samples=b)
+    del lp_rows, cmel
+    # SR: sample-space Gram (FP32 products, FP64 reduction), FP64 CG, back-map
+    p, bs = 200_000, 1024
+    n = 2 * bs
+    o_re = torch.randn((p, bs), device="cuda", generator=g)
+    o_im = torch.randn((p, bs), device="cuda", generator=g)
+    gram = torch.empty((n, n), device="cuda", dtype=torch.float64)
+    ms = timed(lambda: _lib.call("fk_sr_gram", _lib.ptr(o_re), _lib.ptr(o_im), p, bs, _lib.ptr(gram), n * n, st))
+    peak32 = fp32_peak_tflops()
+    record("sr_gram", ms, flops=float(n) * (n + 1) * p, peak=peak32, unit="TFLOP/s (cuBLAS SGEMM, measured)",
+           nbytes=2 * p * bs * 4, params=p, samples=bs)
+    rhs = torch.randn(n, device="cuda", dtype=torch.float64, generator=g)
+    alpha = torch.empty(n, device="cuda", dtype=torch.float64)
+    stats = torch.zeros(3, device="cuda", dtype=torch.float64)
+    ws = torch.empty(_lib.load().fk_sr_solve_workspace_bytes(n), dtype=torch.uint8, device="cuda")
+    iters = 50
+    ms = timed(lambda: _lib.call("fk_sr_solve", _lib.ptr(gram), n, 1.0 / bs, 1e3, _lib.ptr(rhs), 1e-30, iters,
+                                 _lib.ptr(alpha), _lib.ptr(stats), _lib.ptr(ws), ws.numel(), st))
+    record("sr_cg_50_iterations", ms, nbytes=iters * n * n * 8, n=n,
+           note="the Gram (33.6 MB) stays in L2 across iterations: bytes are per-iteration reads")
+    x = torch.empty(p, device="cuda")
+    ms = timed(lambda: _lib.call("fk_sr_backmap", _lib.ptr(o_re), _lib.ptr(o_im), p, bs, _lib.ptr(alpha), 1.0 / bs,
+                                 0.0, None, _lib.ptr(x), st))
+    record("sr_backmap", ms, nbytes=2 * p * bs * 4 + p * 4, params=p)
+    del o_re, o_im, gram
+    torch.cuda.empty_cache()
+    # adjoint (tensor cores) and causal-reuse forward of the bench network
+    m = ConvNetAutoregressive2D(SHAPE, DEPTH, CHANNELS, weights_normalization=True, precision=args.precision, seed=0)
+    b = 4096
+    spins = (2 * torch.randint(0, 2, (b,) + SHAPE, device="cuda", generator=g) - 1).to(torch.int8)
+    _, _, saved = m.forward(spins, mode=_lib.FK_AR2D_SAVE)
+    w = torch.randn((b, 2), device="cuda", generator=g) / b
+    ms = timed(lambda: m.backward(spins, w, saved))
+    fps = flops_per_sample_forward(SHAPE, DEPTH, CHANNELS)
+    record("adjoint_10x10_d10_f32", ms, flops=2.0 * fps * b, peak=peaks.get("bf16_tflops_sustained"),
+           unit="TFLOP/s (bf16, measured)", samples=b, note="algorithmic FLOPs: 2x the forward's")
+    obs = Observable(Ising(h=H_FIELD, hilbert_state_shape=SHAPE, pbc=True))
+    lp, _, _ = m.forward(spins)
+    ms = timed(lambda: obs.local_values(m, spins, log_psi=lp, base_saved=saved))
+    record("local_energy_10x10_d10_f32_causal_reuse", ms, samples=b, rows=b * 100)
     print(json.dumps(out), flush=True)
 
 
@@ -392,17 +536,29 @@ def energy4x4_case(args):
 
     m = ConvNetAutoregressive2D(shape, 5, 16, weights_normalization=False, precision=args.precision, seed=0)
     vmc = VariationalMonteCarlo(m, op, FastAutoregressiveSampler(m, args.train_batch, seed=1234))
-    opt = Adam(m, lr=1e-3)
+    if args.optimizer == "sr":
+        # stochastic reconfiguration (the reference's optimizer.py:14-183),
+        # learning rate decayed with the same cosine schedule
+        from flowket_gb300.optimizers import ComplexValuesStochasticReconfiguration
+        opt = ComplexValuesStochasticReconfiguration(m, lr=args.lr, diag_shift=args.diag_shift)
+        lr0, lr1 = args.lr, args.lr * 1e-2
+    else:
+        opt = Adam(m, lr=1e-3)
+        lr0, lr1 = 1e-3, 1e-5
     t0 = time.perf_counter()
+    trace = []
     for k in range(1, args.train_steps + 1):
-        opt.lr = 1e-5 + 0.5 * (1e-3 - 1e-5) * (1 + math.cos(math.pi * k / args.train_steps))
+        opt.lr = lr1 + 0.5 * (lr0 - lr1) * (1 + math.cos(math.pi * k / args.train_steps))
         vmc.step(opt)
+        if k % max(1, args.train_steps // 10) == 0:
+            trace.append((k, exact_energy(m)))
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t0
     e = exact_energy(m)
-    print(json.dumps({"case": "energy4x4", "precision": args.precision, "steps": args.train_steps,
-                      "batch": args.train_batch, "exact_energy": e, "lanczos": e0,
-                      "relative_error": abs(e - e0) / abs(e0), "train_s": train_s}), flush=True)
+    print(json.dumps({"case": "energy4x4", "precision": args.precision, "optimizer": args.optimizer,
+                      "steps": args.train_steps, "batch": args.train_batch, "exact_energy": e, "lanczos": e0,
+                      "relative_error": abs(e - e0) / abs(e0), "train_s": train_s,
+                      "trace_relative_error": [(k, abs(x - e0) / abs(e0)) for k, x in trace]}), flush=True)
 
 
 def dist_init(n):
@@ -745,6 +901,8 @@ def main():
         j1j2sr_case(args)
     elif args.case == "chain64":
         chain64_case(args)
+    elif args.case == "kernels":
+        kernels_case(args)
     elif args.impl == "reference":
         reference_arm(args, rank, world)
     else:

@@ -55,14 +55,32 @@ def load_optimizer_weights(optimizer, filepath):
     return epoch, batch
 
 
+def save_sampler_state(sampler, filepath):
+    """The sampler's draw position (Philox seed and offset, or the chains and
+    their sweep counter) in ``<filepath>_sampler.pt``, so that a resumed run
+    draws what the uninterrupted one would have. The reference keeps no
+    sampler state (numpy's global RNG); this makes the resume exact."""
+    torch.save(_to_host(sampler.state_dict()), filepath + "_sampler.pt")
+
+
+def load_sampler_state(sampler, filepath):
+    filepath += "_sampler.pt"
+    if not os.path.exists(filepath):
+        return False
+    sampler.load_state_dict(torch.load(filepath, map_location="cpu"))
+    return True
+
+
 class CheckpointByTime:
     """Save the machine (and optimiser state) every ``save_frequency_in_minutes``
     and at the end of training; ``filepath`` may hold format fields filled
     from the logs."""
 
-    def __init__(self, machine, optimizer, filepath, save_frequency_in_minutes=30, save_weights_only=True):
+    def __init__(self, machine, optimizer, filepath, save_frequency_in_minutes=30, save_weights_only=True,
+                 sampler=None):
         self.machine = machine
         self.optimizer = optimizer
+        self.sampler = sampler
         self.filepath = filepath
         self.save_weights_only = save_weights_only
         self.save_frequency_in_minutes = save_frequency_in_minutes
@@ -74,6 +92,8 @@ class CheckpointByTime:
         save_weights(self.machine, filepath)
         if self.optimizer is not None:
             save_optimizer_weights(self.optimizer, filepath, self.current_epoch, batch)
+        if self.sampler is not None:
+            save_sampler_state(self.sampler, filepath)
         self.last_save_time = time.time()
 
     def on_batch_end(self, batch, logs=None):

@@ -64,7 +64,12 @@ class Observable(BaseObservable):
                   _lib.ptr(bf["configs"]), _lib.ptr(bf["owner"]), _lib.ptr(bf["cmel"]), _lib.ptr(bf["cflips"]),
                   _lib.ptr(bf["offsets"]), b * (c - 1), _lib.ptr(bf["nrows"]), _lib.ptr(bf["ws"]), bf["ws"].numel(),
                   _lib.stream_ptr())
-        rows = int(bf["nrows"].item())
+        if getattr(self.operator, "all_connections_used", False):
+            # every slot is a connection (Ising): the row count is known on
+            # the host and the step needs no device synchronisation here
+            rows = b * (c - 1)
+        else:
+            rows = int(bf["nrows"].item())
         return spins, mel, bf, rows
 
     def local_values(self, machine, configurations, log_psi=None, base_saved=None):

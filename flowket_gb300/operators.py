@@ -113,7 +113,11 @@ class Heisenberg(OperatorOnGrid):
 
 
 class Ising(OperatorOnGrid):
-    """operators/ising.py:8-46 (transverse field h, coupling j)."""
+    """operators/ising.py:8-46 (transverse field h, coupling j). Every slot
+    is used (ising.py:46), so the local energy knows its row count on the
+    host."""
+
+    all_connections_used = True
 
     def __init__(self, h=1.0, j=1.0, **kwargs):
         super().__init__(**kwargs)

@@ -78,6 +78,14 @@ class FastAutoregressiveSampler(Sampler):
         self.last_workspace = ws
         return spins.view(b, h, w), lp, ws
 
+    def state_dict(self):
+        """The draw position: with these the next draws repeat exactly."""
+        return {"seed": self.seed, "offset": self.offset}
+
+    def load_state_dict(self, state):
+        self.seed = int(state["seed"])
+        self.offset = int(state["offset"])
+
     def sample_with_log_psi(self):
         """(spins, log_psi, activation workspace) of one draw: the driver's
         sampler protocol (the workspace lets the local energy reuse the base
@@ -181,6 +189,16 @@ class MetropolisHastingsSampler(Sampler):
     def calc_r_hat_value(self, estimated_values):
         return r_hat_and_correlations(estimated_values, self.num_of_chains)
 
+    def state_dict(self):
+        """Chains, their log psi and the sweep counter of the Philox stream."""
+        return {"sample": self.sample, "log_psi": self.log_psi, "seed": self.seed, "sweep": self.sweep}
+
+    def load_state_dict(self, state):
+        self.sample.copy_(state["sample"])
+        self.log_psi.copy_(state["log_psi"])
+        self.seed = int(state["seed"])
+        self.sweep = int(state["sweep"])
+
 
 class MetropolisHastingsLocal(MetropolisHastingsSampler):
     """metropolis_hastings.py:119-127: flip one random site."""
@@ -274,6 +292,15 @@ class MetropolisHastingsHamiltonian(Sampler):
 
     def calc_r_hat_value(self, estimated_values):
         return r_hat_and_correlations(estimated_values, self.num_of_chains)
+
+    def state_dict(self):
+        return {"sample": self.sample, "log_psi": self.lp, "seed": self.seed, "sweep": self.sweep}
+
+    def load_state_dict(self, state):
+        self.sample.copy_(state["sample"])
+        self.lp.copy_(state["log_psi"])
+        self.seed = int(state["seed"])
+        self.sweep = int(state["sweep"])
 
 
 class MetropolisHastingsIndependent(Sampler):

@@ -1,8 +1,10 @@
 """Kernels (a) and (b): AR2D forward and exact sampler against the oracle.
 
 Tolerances: FP32 path log psi within 1e-5 relative of the FP64 oracle (the
-reference runs FP32). BF16 path: the stated bound is |d log psi| <= 2e-2 *
-max(1, |log psi|) per sample (bf16 operands, fp32 accumulation).
+reference runs FP32). Tensor-core paths (16-bit operands and stored
+activations, FP32 accumulation): |d log psi| <= bound * max(1, |log psi|)
+per sample, the bound 3x the worst case measured over 5 seeds on these
+cases (BF16 8.4e-4, FP16 1.05e-4, both on the 4x4 depth-5 network).
 """
 import numpy as np
 import pytest
@@ -13,7 +15,7 @@ from oracle import ar2d, exact, philox
 pytestmark = pytest.mark.gpu
 
 FP32_RTOL = 1e-5
-BF16_BOUND = 2e-2
+TC_BOUND = {"bf16": 2.6e-3, "fp16": 3.2e-4}
 
 
 def _machine(shape, depth, f, wn, precision, seed=0):
@@ -49,14 +51,15 @@ def test_forward_fp32_matches_oracle(cuda, shape, depth, f, wn):
     assert err.max() < FP32_RTOL, err.max()
 
 
+@pytest.mark.parametrize("precision", ["bf16", "fp16"])
 @pytest.mark.parametrize("shape,depth,f,wn", CASES)
-def test_forward_bf16_within_bound(cuda, shape, depth, f, wn):
-    m = _machine(shape, depth, f, wn, "bf16")
+def test_forward_tensor_core_within_bound(cuda, shape, depth, f, wn, precision):
+    m = _machine(shape, depth, f, wn, precision)
     s = _spins(300, shape, 2)
     got = m.log_psi(torch.as_tensor(s).cuda()).cpu().numpy()
     want = ar2d.log_psi_numpy(m.params_dict_cpu(), s, depth, wn)
     err = np.abs(got - want) / np.maximum(1.0, np.abs(want))
-    assert err.max() < BF16_BOUND, err.max()
+    assert err.max() < TC_BOUND[precision], err.max()
 
 
 def test_conditionals_fp32(cuda):

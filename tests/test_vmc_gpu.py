@@ -125,3 +125,63 @@ def test_exact_variational_matches_oracle_and_finite_differences(cuda):
     # the generator serves (configurations, coefficients) in batch_size pieces
     x, y = next(iter(ev))
     assert x.shape == (64, 3, 3) and y.shape == (64,)
+
+
+@pytest.mark.parametrize("kind", ["ar_adam", "rbm_sr"])
+def test_checkpoint_resume_continues_a_vmc_run_identically(cuda, tmp_path, kind):
+    """A real VMC run checkpointed after 3 steps (parameters, optimiser state,
+    sampler position; callbacks/checkpoint.py:9-73) and resumed in fresh
+    objects repeats the uninterrupted run's next steps: bit for bit with Adam
+    (every reduction of that step has a fixed order); with SR to rounding,
+    because the Gram's K-split partial sums and CG's dot products are added
+    with atomics in a varying order."""
+    from flowket_gb300 import checkpoint
+    from flowket_gb300.machines import RBM, ConvNetAutoregressive2D
+    from flowket_gb300.operators import Heisenberg
+    from flowket_gb300.optimization import VariationalMonteCarlo
+    from flowket_gb300.optimizers import Adam, ComplexValuesStochasticReconfiguration
+    from flowket_gb300.samplers import FastAutoregressiveSampler, MetropolisHastingsLocal
+
+    def build():
+        if kind == "ar_adam":
+            shape = (4, 4)
+            m = ConvNetAutoregressive2D(shape, 3, 16, weights_normalization=True, precision="bf16", seed=1)
+            smp = FastAutoregressiveSampler(m, 256, seed=5)
+            opt = Adam(m, lr=3e-3)
+        else:
+            shape = (10,)
+            m = RBM(shape, alpha=2, stddev=0.05, seed=1)
+            smp = MetropolisHastingsLocal(m, 256, num_of_chains=32, unused_sampels=4, seed=5)
+            opt = ComplexValuesStochasticReconfiguration(m, lr=0.05, diag_shift=0.1)
+        return m, smp, opt, VariationalMonteCarlo(m, Heisenberg(hilbert_state_shape=shape, pbc=True), smp)
+
+    m, smp, opt, vmc = build()
+    for _ in range(3):
+        vmc.step(opt)
+    path = str(tmp_path / "ckpt")
+    checkpoint.save_weights(m, path)
+    if kind == "ar_adam":
+        checkpoint.save_optimizer_weights(opt, path, 0, 3)
+    checkpoint.save_sampler_state(smp, path)
+    # SR: one resumed step, whose sampling and energy depend only on the
+    # restored state (the update itself is reproduced to rounding)
+    n_more = 3 if kind == "ar_adam" else 1
+    want = []
+    for _ in range(n_more):
+        vmc.step(opt)
+        want.append(vmc.current_energy)
+    want_params = m.params.clone()
+    m2, smp2, opt2, vmc2 = build()
+    checkpoint.load_weights(m2, path)
+    if kind == "ar_adam":
+        assert checkpoint.load_optimizer_weights(opt2, path) == (0, 3)
+    assert checkpoint.load_sampler_state(smp2, path)
+    got = []
+    for _ in range(n_more):
+        vmc2.step(opt2)
+        got.append(vmc2.current_energy)
+    assert got == want
+    if kind == "ar_adam":
+        assert torch.equal(m2.params, want_params)
+    else:
+        assert torch.allclose(m2.params, want_params, rtol=1e-4, atol=1e-6)
