@@ -420,6 +420,11 @@ def kernels_case(args):
     peak32 = fp32_peak_tflops()
     record("sr_gram", ms, flops=float(n) * (n + 1) * p, peak=peak32, unit="TFLOP/s (cuBLAS SGEMM, measured)",
            nbytes=2 * p * bs * 4, params=p, samples=bs)
+    ms = timed(lambda: _lib.call("fk_sr_gram_tc", _lib.ptr(o_re), _lib.ptr(o_im), p, bs, _lib.ptr(gram), n * n,
+                                 st))
+    record("sr_gram_tc", ms, flops=float(n) * (n + 1) * p, peak=peaks.get("bf16_tflops"),
+           unit="TFLOP/s (bf16 burst, measured; each product costs three bf16 MMAs)", nbytes=2 * p * bs * 4,
+           params=p, samples=bs)
     rhs = torch.randn(n, device="cuda", dtype=torch.float64, generator=g)
     alpha = torch.empty(n, device="cuda", dtype=torch.float64)
     stats = torch.zeros(3, device="cuda", dtype=torch.float64)

@@ -60,6 +60,7 @@ _SIGNATURES = {
     "fk_adam_step": (c_i32, [c_p, c_p, c_p, c_p, c_i64, c_i64, c_f32, c_f32, c_f32, c_f32, c_p]),
     "fk_sr_gram_workspace_bytes": (c_i64, [c_i64, c_i64]),
     "fk_sr_gram": (c_i32, [c_p, c_p, c_i64, c_i64, c_p, c_i64, c_p]),
+    "fk_sr_gram_tc": (c_i32, [c_p, c_p, c_i64, c_i64, c_p, c_i64, c_p]),
     "fk_sr_solve_workspace_bytes": (c_i64, [c_i64]),
     "fk_sr_solve": (c_i32, [c_p, c_i64, c_f64, c_f64, c_p, c_f64, c_i32, c_p, c_p, c_p, c_i64, c_p]),
     "fk_sr_solve_noalloc": (c_i32, [c_p, c_i64, c_f64, c_f64, c_p, c_f64, c_i32, c_p, c_p, c_p]),

@@ -277,6 +277,7 @@ struct WgArgs {
   int64_t o_kernel, o_bias;
   int64_t batch;
   int items;            // work items = ntaps * ceil(cin/8) * ceil(N/8)
+  int items_per_cta;
   // Fixed-order mode: each tile writes its sums to part[tile][ntaps*cin*N + N]
   // (kernel then bias) instead of adding them atomically; the tiles are then
   // summed in order (wgrad_part_reduce_kernel).
@@ -294,7 +295,7 @@ __global__ void __launch_bounds__(128) wgrad_kernel(const __grid_constant__ WgAr
   const int64_t b = tile * kTile + m;
   const int kchunks = (a.cin + 7) / 8;
   const int nchunks = (a.N + 7) / 8;
-  for (int it = blockIdx.y * kItemsPerCta; it < a.items && it < (int)(blockIdx.y + 1) * kItemsPerCta; ++it) {
+  for (int it = blockIdx.y * a.items_per_cta; it < a.items && it < (int)(blockIdx.y + 1) * a.items_per_cta; ++it) {
     const int t = it / (kchunks * nchunks);
     const int kc = (it / nchunks) % kchunks;
     const int nc = it % nchunks;
@@ -417,8 +418,10 @@ __global__ void wn_kernel(const __grid_constant__ WnArgs a) {
   int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t cols = a.O ? (int64_t)N * a.batch : N;
   if (idx >= cols) return;
-  int n = (int)(idx % N);
-  int64_t b = idx / N;
+  // per-sample: consecutive threads take consecutive samples of one channel,
+  // so that every access to the parameter-major O rows is coalesced
+  int n = a.O ? (int)(idx / a.batch) : (int)idx;
+  int64_t b = a.O ? idx % a.batch : 0;
   const float* v = a.params + p_kernel;
   float sq = 0.f;
   for (int k = 0; k < K; ++k) sq += v[(int64_t)k * N + n] * v[(int64_t)k * N + n];
@@ -545,7 +548,10 @@ static int launch_wgrad(const NetLayout& L, WgArgs& w, const ConvDesc& cd, float
     w.dW = grad + cd.p_kernel;
     w.dB = grad + cd.p_bias;
   }
-  dim3 grid((unsigned)tiles, (unsigned)((w.items + kItemsPerCta - 1) / kItemsPerCta));
+  // per-sample rows: one item per CTA (the CTA count, not the arithmetic,
+  // bounds that mode); summed: kItemsPerCta
+  w.items_per_cta = O ? 1 : kItemsPerCta;
+  dim3 grid((unsigned)tiles, (unsigned)((w.items + w.items_per_cta - 1) / w.items_per_cta));
   wgrad_kernel<T, TG><<<grid, 128, 0, s>>>(w, L.H, L.W);
   if (!w.part || O) return check_cuda(launched(), "wgrad_kernel");
   FK_CUDA(launched());

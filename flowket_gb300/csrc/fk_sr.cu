@@ -125,6 +125,247 @@ __global__ void mirror_kernel(double* t, int64_t n) {
   if (j < i) t[i * n + j] = t[j * n + i];
 }
 
+// ---------------------------------------------------------------- Gram on tensor cores
+// T = Y^T Y (Y = [o_re | o_im], P x n, parameter-major fp32) with tcgen05:
+// each fp32 value is split into bf16 hi = bf16(y) and lo = bf16(y - hi), and
+// every product is hi*hi + hi*lo + lo*hi (the lo*lo term is below fp32's
+// rounding), accumulated in fp32 in TMEM: fp32-level accuracy at three
+// bf16 MMAs per product. Output tiles of 128 (i) x 256 (j) samples on or
+// above the diagonal, K = parameters split into ranges (work item = tile x
+// range); per range the tile's fp32 sums are added into T with fp64 atomics.
+// Roles (13 warps): 8 converter warps load 64 parameters x (128 + 256)
+// columns per stage from global memory (32-byte sector loads), split them
+// into hi/lo and store them as MN-major operands (8 samples per 16 bytes,
+// LBO 128 B along K, SBO 1 KB along the samples) in one of two stages; one
+// issuer warp (lane 0) issues 12 MMAs (M128 N256 K16) per stage into one of
+// two TMEM accumulators; 4 drain warps read a finished accumulator (the
+// lane quarter of their rank in the warpgroup) and add it into T while the
+// next item accumulates. Every wait is bounded (mbar_wait).
+namespace gram_tc {
+constexpr int kM = 128, kN = 256, kK = 64, kStages = 2;
+constexpr int kAB = kM * kK * 2;                 // one A half (hi or lo): 16 KB
+constexpr int kBB = kN * kK * 2;                 // one B half: 32 KB
+constexpr int kStage = 2 * kAB + 2 * kBB;        // 96 KB
+constexpr int kConvWarps = 8, kIssuerWarp = 8;
+constexpr int kThreads = 32 * 13;
+constexpr int kSmem = kStages * kStage + 256;
+}  // namespace gram_tc
+
+struct GramTcArgs {
+  const float* a;   // o_re [P][bsz]
+  const float* b;   // o_im [P][bsz] (== a when n == bsz)
+  int64_t P, bsz, n;
+  int64_t kper;     // parameters per range (multiple of 64)
+  int64_t splits;
+  int64_t nti, ntj;
+  int64_t items;
+  double* t;        // n x n, j >= i written
+  int* err;
+};
+
+// Work item -> tile origin (i0, j0) and parameter range [k0, k1). Tile rows
+// ti take j-tiles tj >= ti / 2 (the first 256-wide tile reaching row ti*128).
+__device__ __forceinline__ void gram_item(const GramTcArgs& g, int64_t item, int64_t& i0, int64_t& j0, int64_t& k0,
+                                          int64_t& k1) {
+  const int64_t tile = item / g.splits, split = item % g.splits;
+  int64_t ti = 0, rem = tile;
+  while (ti < g.nti && rem >= g.ntj - ti / 2) {
+    rem -= g.ntj - ti / 2;
+    ++ti;
+  }
+  i0 = ti * gram_tc::kM;
+  j0 = (ti / 2 + rem) * gram_tc::kN;
+  k0 = split * g.kper;
+  k1 = min(g.P, k0 + g.kper);
+}
+
+// 8 consecutive columns [c, c+8) of parameter row p: zero outside P x n.
+__device__ __forceinline__ void gram_load8(const GramTcArgs& g, int64_t p, int64_t c, float* v) {
+  if (p < g.P && c < g.n) {
+    const float* src = c < g.bsz ? g.a + p * g.bsz + c : g.b + p * g.bsz + (c - g.bsz);
+    const float4 x0 = reinterpret_cast<const float4*>(src)[0];
+    const float4 x1 = reinterpret_cast<const float4*>(src)[1];
+    v[0] = x0.x; v[1] = x0.y; v[2] = x0.z; v[3] = x0.w;
+    v[4] = x1.x; v[5] = x1.y; v[6] = x1.z; v[7] = x1.w;
+  } else {
+#pragma unroll
+    for (int e = 0; e < 8; ++e) v[e] = 0.f;
+  }
+}
+
+__device__ __forceinline__ void gram_split_store(const float* v, uint8_t* hi, uint8_t* lo, int off) {
+  float h[8], l[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    h[e] = __bfloat162float(__float2bfloat16_rn(v[e]));
+    l[e] = v[e] - h[e];
+  }
+  uint4 uh, ul;
+  uh.x = pack_bf16x2(h[0], h[1]); uh.y = pack_bf16x2(h[2], h[3]);
+  uh.z = pack_bf16x2(h[4], h[5]); uh.w = pack_bf16x2(h[6], h[7]);
+  ul.x = pack_bf16x2(l[0], l[1]); ul.y = pack_bf16x2(l[2], l[3]);
+  ul.z = pack_bf16x2(l[4], l[5]); ul.w = pack_bf16x2(l[6], l[7]);
+  *reinterpret_cast<uint4*>(hi + off) = uh;
+  *reinterpret_cast<uint4*>(lo + off) = ul;
+}
+
+__global__ void __launch_bounds__(gram_tc::kThreads, 1) gram_tc_kernel(const __grid_constant__ GramTcArgs g) {
+  using namespace gram_tc;
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kStages * kStage);
+  uint64_t* full = bars;          // [2] converters -> issuer (8 warp arrivals)
+  uint64_t* empty = bars + 2;     // [2] MMAs done with a stage (commit)
+  uint64_t* accfull = bars + 4;   // [2] accumulator complete (commit)
+  uint64_t* accempty = bars + 6;  // [2] accumulator drained (4 warp arrivals)
+  uint64_t* drain = bars + 8;     // every MMA complete before teardown
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 9);
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&full[i], kConvWarps);
+      mbar_init(&empty[i], 1);
+      mbar_init(&accfull[i], 1);
+      mbar_init(&accempty[i], 4);
+    }
+    mbar_init(drain, 1);
+    fence_mbar_init();
+  }
+  if (warp == kIssuerWarp) {
+    tmem_alloc(tslot, 512);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+  bool abort = false;
+
+  if (warp < kConvWarps) {
+    // ---------------------------------------------------------------- converters
+    uint32_t gc = 0;
+    for (int64_t it = blockIdx.x; it < g.items && !abort; it += gridDim.x) {
+      int64_t i0, j0, k0, k1;
+      gram_item(g, it, i0, j0, k0, k1);
+      for (int64_t kc = k0; kc < k1 && !abort; kc += kK, ++gc) {
+        const uint32_t st = gc % kStages;
+        if (gc >= kStages && !mbar_wait(&empty[st], ((gc / kStages) - 1) & 1, g.err)) {
+          abort = true;
+          break;
+        }
+        uint8_t* base = smem + st * kStage;
+        uint8_t *ahi = base, *alo = base + kAB, *bhi = base + 2 * kAB, *blo = base + 2 * kAB + kBB;
+        // A: 16 groups of 8 samples x 64 parameters; B: 32 groups x 64.
+        // Consecutive threads take consecutive parameters: conflict-free
+        // 16-byte shared stores, one 32-byte sector per global load.
+        for (int q = threadIdx.x; q < (kM / 8 + kN / 8) * kK; q += kConvWarps * 32) {
+          const int pq = q % kK;
+          const int grp = q / kK;
+          float v[8];
+          if (grp < kM / 8) {
+            gram_load8(g, kc + pq, i0 + 8 * grp, v);
+            gram_split_store(v, ahi, alo, (grp * kK + pq) * 16);
+          } else {
+            const int gb = grp - kM / 8;
+            gram_load8(g, kc + pq, j0 + 8 * gb, v);
+            gram_split_store(v, bhi, blo, (gb * kK + pq) * 16);
+          }
+        }
+        fence_proxy_async_smem();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&full[st]);
+      }
+    }
+  } else if (warp == kIssuerWarp) {
+    // ---------------------------------------------------------------- issuer
+    const uint32_t idesc = umma_idesc_bf16_mn(kM, kN);
+    uint32_t gc = 0, li = 0;
+    for (int64_t it = blockIdx.x; it < g.items && !abort; it += gridDim.x, ++li) {
+      int64_t i0, j0, k0, k1;
+      gram_item(g, it, i0, j0, k0, k1);
+      const uint32_t buf = li % 2;
+      if (li >= 2 && !mbar_wait(&accempty[buf], ((li / 2) - 1) & 1, g.err)) {
+        abort = true;
+        break;
+      }
+      tc_fence_after();
+      const uint32_t d = tmem + buf * kN;
+      bool first = true;
+      for (int64_t kc = k0; kc < k1; kc += kK, ++gc) {
+        const uint32_t st = gc % kStages;
+        if (!mbar_wait(&full[st], (gc / kStages) & 1, g.err)) {
+          abort = true;
+          break;
+        }
+        tc_fence_after();
+        if (lane == 0) {
+          const uint32_t base = smem_u32(smem + st * kStage);
+          const uint64_t ahi = umma_sdesc(base, 128, kK * 16), alo = umma_sdesc(base + kAB, 128, kK * 16);
+          const uint64_t bhi = umma_sdesc(base + 2 * kAB, 128, kK * 16);
+          const uint64_t blo = umma_sdesc(base + 2 * kAB + kBB, 128, kK * 16);
+#pragma unroll
+          for (int ks = 0; ks < kK / 16; ++ks) {
+            umma_bf16(d, ahi + ks * 16, bhi + ks * 16, idesc, (first && ks == 0) ? 0u : 1u);
+            umma_bf16(d, ahi + ks * 16, blo + ks * 16, idesc, 1u);
+            umma_bf16(d, alo + ks * 16, bhi + ks * 16, idesc, 1u);
+          }
+          umma_commit(&empty[st]);
+        }
+        __syncwarp();
+        first = false;
+      }
+      if (abort) break;
+      if (lane == 0) umma_commit(&accfull[buf]);
+      __syncwarp();
+    }
+    if (lane == 0) {
+      umma_commit(drain);
+      mbar_wait(drain, 0, g.err);
+    }
+    __syncwarp();
+  } else {
+    // ---------------------------------------------------------------- drain
+    // a warp reads the TMEM lane quarter of its rank in its warpgroup
+    // (warps 9, 10, 11, 12 -> quarters 1, 2, 3, 0)
+    const int q4 = warp % 4;
+    uint32_t li = 0;
+    for (int64_t it = blockIdx.x; it < g.items && !abort; it += gridDim.x, ++li) {
+      int64_t i0, j0, k0, k1;
+      gram_item(g, it, i0, j0, k0, k1);
+      const uint32_t buf = li % 2;
+      bool ok = mbar_wait(&accfull[buf], (li / 2) & 1, g.err);
+      ok = __all_sync(0xffffffffu, ok);
+      if (!ok) {
+        abort = true;
+        break;
+      }
+      tc_fence_after();
+      const int64_t i = i0 + q4 * 32 + lane;
+      const uint32_t tl = tmem + buf * kN + ((uint32_t)(q4 * 32) << 16);
+      for (int c0 = 0; c0 < kN; c0 += 16) {
+        float v[16];
+        tmem_ld16(tl + c0, v);
+        tmem_ld_wait();
+        if (i < g.n) {
+#pragma unroll
+          for (int e = 0; e < 16; ++e) {
+            const int64_t j = j0 + c0 + e;
+            if (j >= i && j < g.n) atomicAdd(&g.t[i * g.n + j], (double)v[e]);
+          }
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&accempty[buf]);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == kIssuerWarp) {
+    tc_fence_after();
+    tmem_dealloc(tmem, 512);
+  }
+}
+
 // ---------------------------------------------------------------- FP64 CG
 // State: x, r, p, q (n each) + scalars s[0]=rr, s[1]=pq, s[2]=rr_new, s[3]=stop
 // (1 when converged), s[4]=tol^2 * ||b||^2, s[5]=iterations.
@@ -212,18 +453,22 @@ __global__ void cg_roll_kernel(double* s) {
 }
 
 // ---------------------------------------------------------------- back-map
-// params[p] -= lr * scale * sum_j Y[p][j] alpha[j]   (a warp per row)
+// params[p] -= lr * scale * sum_j Y[p][j] alpha[j]   (a warp per row). The
+// update is float32, so the products and sums are too (compensated per lane,
+// then a tree over the warp): FP64 stays in the solve, and this part's
+// narrow FP64 pipe does not bound the kernel.
 __global__ void backmap_kernel(const float* __restrict__ a, const float* __restrict__ b, int64_t P, int64_t bsz,
                                int64_t n, const double* __restrict__ alpha, double scale, float lr,
                                float* __restrict__ params, float* __restrict__ x_out) {
   int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   if (row >= P) return;
-  double acc = 0.0;
-  for (int64_t j = lane; j < n; j += 32) acc += (double)ycol(a, b, bsz, row, j) * alpha[j];
+  Kahan k;
+  for (int64_t j = lane; j < n; j += 32) k.add(ycol(a, b, bsz, row, j) * (float)alpha[j]);
+  float acc = k.s - k.c;
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
   if (lane == 0) {
-    float xv = (float)(scale * acc);
+    float xv = (float)(scale * (double)acc);
     if (x_out) x_out[row] = xv;
     if (params) params[row] -= lr * xv;
   }
@@ -256,7 +501,8 @@ __global__ void hermitian_embed_kernel(double* g, int64_t n) {
 
 // x = scale * O_c^H z = scale * [(A zr + C zi) + i (A zi - C zr)] per parameter
 // (A, C parameter-major rows); params (interleaved re, im) -= lr * x when
-// params != NULL, x (interleaved) written to x_out when != NULL. Warp per row.
+// params != NULL, x (interleaved) written to x_out when != NULL. Warp per
+// row, float32 compensated sums as in backmap_kernel.
 __global__ void complex_backmap_kernel(const float* __restrict__ a, const float* __restrict__ c, int64_t P,
                                        int64_t bsz, const double* __restrict__ z, double scale, float lr,
                                        float2* __restrict__ params, float2* __restrict__ x_out) {
@@ -265,18 +511,19 @@ __global__ void complex_backmap_kernel(const float* __restrict__ a, const float*
   if (row >= P) return;
   const float* ar = a + row * bsz;
   const float* cr = c + row * bsz;
-  double xr = 0.0, xi = 0.0;
+  Kahan kr, ki;
   for (int64_t j = lane; j < bsz; j += 32) {
-    double av = ar[j], cv = cr[j], zr = z[j], zi = z[bsz + j];
-    xr += av * zr + cv * zi;
-    xi += av * zi - cv * zr;
+    const float av = ar[j], cv = cr[j], zr = (float)z[j], zi = (float)z[bsz + j];
+    kr.add(av * zr + cv * zi);
+    ki.add(av * zi - cv * zr);
   }
+  float xr = kr.s - kr.c, xi = ki.s - ki.c;
   for (int o = 16; o > 0; o >>= 1) {
     xr += __shfl_xor_sync(0xffffffffu, xr, o);
     xi += __shfl_xor_sync(0xffffffffu, xi, o);
   }
   if (lane == 0) {
-    float2 xv = make_float2((float)(scale * xr), (float)(scale * xi));
+    float2 xv = make_float2((float)(scale * (double)xr), (float)(scale * (double)xi));
     if (x_out) x_out[row] = xv;
     if (params) {
       float2 p = params[row];
@@ -347,6 +594,52 @@ int fk_sr_gram(const float* o_re, const float* o_im, int64_t n_params, int64_t n
   kper = (kper + kGK - 1) / kGK * kGK;
   dim3 grid((unsigned)tiles, 1, (unsigned)splits);
   gram_kernel<<<grid, 256, 0, s>>>(o_re, o_im ? o_im : o_re, n_params, n_samples, n, kper, gram);
+  FK_CUDA(launched());
+  mirror_kernel<<<(unsigned)((n * n + 255) / 256), 256, 0, s>>>(gram, n);
+  FK_CUDA(launched());
+  return FK_OK;
+}
+
+int fk_sr_gram_tc(const float* o_re, const float* o_im, int64_t n_params, int64_t n_samples, double* gram,
+                  int64_t gram_elems, void* stream) {
+  FK_CHECK_ARG(o_re && gram && n_params > 0 && n_samples > 0, "fk_sr_gram_tc: bad arguments");
+  FK_CHECK_ARG(n_samples % 8 == 0, "fk_sr_gram_tc: n_samples must be a multiple of 8 (got %lld)",
+               (long long)n_samples);
+  FK_CHECK_ARG(((uintptr_t)o_re % 16) == 0 && (!o_im || ((uintptr_t)o_im % 16) == 0),
+               "fk_sr_gram_tc: o_re / o_im must be 16-byte aligned");
+  const int64_t n = o_im ? 2 * n_samples : n_samples;
+  FK_CHECK_ARG(n <= 65536, "fk_sr_gram_tc: n = %lld exceeds 65536", (long long)n);
+  FK_CHECK_ARG(gram_elems >= n * n, "fk_sr_gram_tc: gram buffer too small (%lld < %lld)", (long long)gram_elems,
+               (long long)(n * n));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  static bool attr = false;
+  if (!attr) {
+    FK_CUDA(cudaFuncSetAttribute(gram_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, gram_tc::kSmem));
+    attr = true;
+  }
+  FK_CUDA(cudaMemsetAsync(gram, 0, (size_t)(n * n) * sizeof(double), s));
+  GramTcArgs a;
+  a.a = o_re;
+  a.b = o_im ? o_im : o_re;
+  a.P = n_params;
+  a.bsz = n_samples;
+  a.n = n;
+  a.nti = (n + gram_tc::kM - 1) / gram_tc::kM;
+  a.ntj = (n + gram_tc::kN - 1) / gram_tc::kN;
+  int64_t tiles = 0;
+  for (int64_t ti = 0; ti < a.nti; ++ti) tiles += a.ntj - ti / 2;
+  // parameter ranges: about two items per SM, each range at least 4096 parameters
+  int64_t splits = (2 * 152 + tiles - 1) / tiles;
+  const int64_t max_splits = (n_params + 4095) / 4096;
+  if (splits > max_splits) splits = max_splits;
+  if (splits < 1) splits = 1;
+  a.kper = ((n_params + splits - 1) / splits + gram_tc::kK - 1) / gram_tc::kK * gram_tc::kK;
+  a.splits = (n_params + a.kper - 1) / a.kper;
+  a.items = tiles * a.splits;
+  a.t = gram;
+  a.err = device_error_word();
+  const int64_t grid = a.items < 152 ? a.items : 152;
+  gram_tc_kernel<<<(unsigned)grid, gram_tc::kThreads, gram_tc::kSmem, s>>>(a);
   FK_CUDA(launched());
   mirror_kernel<<<(unsigned)((n * n + 255) / 256), 256, 0, s>>>(gram, n);
   FK_CUDA(launched());

@@ -54,11 +54,20 @@ class ComplexValuesStochasticReconfiguration:
 
     The solve is FP64 CG with the reference's tolerance rule
     (linear_equations.py:34-137); ``iterative_solver=False`` runs CG to 1e-10
-    instead of a Cholesky factorisation."""
+    instead of a Cholesky factorisation.
+
+    ``gram``: "tc" builds the Gram on the tensor cores (split-BF16 products,
+    FP32-level accuracy, fk_sr_gram_tc), "fp32" on the CUDA cores
+    (fk_sr_gram); "auto" takes the tensor cores for a machine on the
+    tensor-core path (BF16/FP16) when the batch is a multiple of 8, the CUDA
+    cores otherwise (the plain FP32 path stays on CUDA cores throughout)."""
 
     def __init__(self, machine, predictions_jacobian=None, lr=0.01, diag_shift=0.05, iterative_solver=True,
                  compute_jvp_instead_of_full_jacobian=False, use_cholesky=True, conjugate_gradient_tol=1e-3,
-                 iterative_solver_max_iterations=200, **kwargs):
+                 iterative_solver_max_iterations=200, gram="auto", **kwargs):
+        if gram not in ("auto", "tc", "fp32"):
+            raise ValueError("gram must be 'auto', 'tc' or 'fp32'")
+        self.gram = gram
         self.machine = machine
         self.lr = float(lr)
         self.diag_shift = float(diag_shift)
@@ -90,6 +99,14 @@ class ComplexValuesStochasticReconfiguration:
         self.iterations += 1
         self.last_stats = self._buf[2 * spins.shape[0]]["stats"]
 
+    def _gram_entry(self, b):
+        if self.gram == "tc":
+            return "fk_sr_gram_tc"
+        if self.gram == "fp32":
+            return "fk_sr_gram"
+        tc = getattr(self.machine, "precision", "fp32") in ("bf16", "fp16") and b % 8 == 0
+        return "fk_sr_gram_tc" if tc else "fk_sr_gram"
+
     def _max_iter(self, n, n_complex_params):
         if self.iterative_solver:
             return self.max_iter
@@ -107,7 +124,7 @@ class ComplexValuesStochasticReconfiguration:
         _lib.call("fk_center_columns", _lib.ptr(o_im), p, b, None, st)
         n = 2 * b
         bf = self._buffers(n, m.device)
-        _lib.call("fk_sr_gram", _lib.ptr(o_re), _lib.ptr(o_im), p, b, _lib.ptr(bf["gram"]), n * n, st)
+        _lib.call(self._gram_entry(b), _lib.ptr(o_re), _lib.ptr(o_im), p, b, _lib.ptr(bf["gram"]), n * n, st)
         _lib.call("fk_sr_hermitian_embed", _lib.ptr(bf["gram"]), b, st)
         bf["rhs"][:b] = local[:, 0] - local[:, 0].mean()
         bf["rhs"][b:] = local[:, 1] - local[:, 1].mean()
@@ -138,7 +155,7 @@ class ComplexValuesStochasticReconfiguration:
         _lib.call("fk_center_columns", _lib.ptr(o_im), p, b, None, st)
         n = 2 * b
         bf = self._buffers(n, m.device)
-        _lib.call("fk_sr_gram", _lib.ptr(o_re), _lib.ptr(o_im), p, b, _lib.ptr(bf["gram"]), n * n, st)
+        _lib.call(self._gram_entry(b), _lib.ptr(o_re), _lib.ptr(o_im), p, b, _lib.ptr(bf["gram"]), n * n, st)
         bf["rhs"][:b] = local[:, 0] - local[:, 0].mean()
         bf["rhs"][b:] = local[:, 1] - local[:, 1].mean()
         _lib.call("fk_sr_solve", _lib.ptr(bf["gram"]), n, 1.0 / b, self.diag_shift, _lib.ptr(bf["rhs"]), self.tol,

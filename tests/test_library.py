@@ -53,6 +53,12 @@ def test_descriptor_queries_without_gpu(built):
         assert lib.fk_ar2d_workspace_bytes(ctypes.byref(desc), 4096, 1) > 0
     # 42,756 parameters for depth 5, 16 channels without weight norm (the reference's 4x4 machine)
     assert lib.fk_ar2d_num_params(ctypes.byref(_lib.Ar2dDesc(4, 4, 5, 16, 0, 1))) == 42756
+    # the FP16-operand format has the BF16 layout and workspace sizes
+    d16, d32 = _lib.Ar2dDesc(10, 10, 10, 32, 1, 2), _lib.Ar2dDesc(10, 10, 10, 32, 1, 1)
+    assert lib.fk_ar2d_packed_bytes(ctypes.byref(d16)) == lib.fk_ar2d_packed_bytes(ctypes.byref(d32)) > 0
+    assert (lib.fk_ar2d_workspace_bytes(ctypes.byref(d16), 4096, 1) ==
+            lib.fk_ar2d_workspace_bytes(ctypes.byref(d32), 4096, 1))
+    assert lib.fk_ar2d_num_params(ctypes.byref(_lib.Ar2dDesc(4, 4, 5, 16, 0, 3))) < 0
     bad = _lib.Ar2dDesc(4, 4, 5, 24, 0, 1)
     assert lib.fk_ar2d_num_params(ctypes.byref(bad)) < 0
     assert b"channels" in lib.fk_last_error()

@@ -33,9 +33,46 @@ def test_gram_and_solve_match_numpy(cuda):
     assert 0 < stats[0].item() <= 500
 
 
-def test_sr_direction_matches_parameter_space_solve(cuda):
+@pytest.mark.parametrize("p,b,complex_", [(3000, 96, True), (4133, 200, True), (70_000, 512, True),
+                                         (1000, 40, False), (64, 8, True)])
+def test_tensor_core_gram_matches_fp64(cuda, p, b, complex_):
+    """fk_sr_gram_tc (tcgen05, split-BF16 products, FP32 accumulation) against
+    the FP64 Gram of the same FP32 rows: FP32-level error, like the CUDA-core
+    fk_sr_gram. Sizes not multiples of the 128 x 256 tiles or of the 64
+    parameters per stage, and a single tile."""
+    from flowket_gb300 import _lib
+    rng = np.random.default_rng(p + b)
+    a = rng.normal(size=(p, b)).astype(np.float32)
+    c = rng.normal(size=(p, b)).astype(np.float32) if complex_ else None
+    ta = torch.as_tensor(a).cuda()
+    tc = torch.as_tensor(c).cuda() if complex_ else None
+    n = 2 * b if complex_ else b
+    y = np.concatenate([a, c], axis=1).astype(np.float64) if complex_ else a.astype(np.float64)
+    want = y.T @ y
+    scale = np.sqrt(np.outer(np.diag(want), np.diag(want)))
+    for entry in ("fk_sr_gram_tc", "fk_sr_gram"):
+        gram = torch.full((n, n), float("nan"), dtype=torch.float64, device="cuda")
+        _lib.call(entry, _lib.ptr(ta), _lib.ptr(tc), p, b, _lib.ptr(gram), n * n, _lib.stream_ptr())
+        got = gram.cpu().numpy()
+        err = np.abs(got - want) / scale
+        assert err.max() < 1e-5, (entry, err.max())
+        np.testing.assert_array_equal(got, got.T)
+
+
+def test_tensor_core_gram_rejects_unsupported_shapes(cuda):
+    from flowket_gb300 import _lib
+    lib = _lib.load()
+    buf = torch.zeros(1024, dtype=torch.float32, device="cuda")
+    g = torch.zeros(1024, dtype=torch.float64, device="cuda")
+    assert lib.fk_sr_gram_tc(_lib.ptr(buf), None, 10, 12, _lib.ptr(g), 1024, _lib.stream_ptr()) == -1
+    assert b"multiple of 8" in lib.fk_last_error()
+
+
+@pytest.mark.parametrize("gram", ["fp32", "tc"])
+def test_sr_direction_matches_parameter_space_solve(cuda, gram):
     """(Re<O_c^* O_c> + lambda) x = Re<O_c^* E_c>: the sample-space GPU solve
-    equals the oracle's parameter-space solve on the same O and E_loc."""
+    (Gram on the CUDA cores or on the tensor cores) equals the oracle's
+    parameter-space solve on the same O and E_loc."""
     from flowket_gb300 import _lib
     from flowket_gb300.machines import ConvNetAutoregressive2D
     from flowket_gb300.operators import Heisenberg
@@ -44,10 +81,10 @@ def test_sr_direction_matches_parameter_space_solve(cuda):
     shape, depth, f = (3, 4), 2, 16
     m = ConvNetAutoregressive2D(shape, depth, f, weights_normalization=False, precision="fp32", seed=1)
     rng = np.random.default_rng(2)
-    s = torch.as_tensor(rng.choice([-1, 1], size=(100,) + shape).astype(np.int8)).cuda()
+    s = torch.as_tensor(rng.choice([-1, 1], size=(96,) + shape).astype(np.int8)).cuda()
     _, _, saved = m.forward(s, mode=_lib.FK_AR2D_SAVE)
     local = Observable(Heisenberg(hilbert_state_shape=shape, pbc=True)).local_values(m, s)
-    opt = ComplexValuesStochasticReconfiguration(m, lr=0.05, diag_shift=1e-2, iterative_solver=False)
+    opt = ComplexValuesStochasticReconfiguration(m, lr=0.05, diag_shift=1e-2, iterative_solver=False, gram=gram)
     x = opt.direction(s, local, saved).cpu().numpy().astype(np.float64)
     o = m.log_derivatives(s, saved).cpu().numpy().T.astype(np.complex128)
     e = local[:, 0].cpu().numpy() + 1j * local[:, 1].cpu().numpy()
