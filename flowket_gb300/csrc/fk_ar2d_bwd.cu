@@ -738,9 +738,13 @@ static bool use_tc_adjoint(const NetLayout& L) {
   return v == 1 && L.precision != FK_PRECISION_FP32 && L.F == 32 && pipe_supported(L.F, L.W);
 }
 
+// With O != NULL (per-sample rows) the data gradients still run on the
+// tensor cores and every weight gradient is the CUDA-core per-sample kernel
+// reading the bf16 gradient tensors (the tensor-core weight-gradient GEMM sums
+// over the samples, which per-sample rows must not).
 static int backward_tc(const NetLayout& L, const void* packed, const float* params, const int8_t* spins,
                        int64_t batch, const float* seeds, const Tensors& A, const TcBwdTensors& G, float* grad,
-                       cudaStream_t s) {
+                       float* O, cudaStream_t s) {
   using T = tc16;
   constexpr int F = 32;
   const int64_t tiles = (batch + kTile - 1) / kTile;
@@ -749,7 +753,7 @@ static int backward_tc(const NetLayout& L, const void* packed, const float* para
   int* err = device_error_word();
   int st;
   auto wt = [&](int idx) { return static_cast<const char*>(packed) + L.conv[idx].wt_off; };
-  FK_CUDA(cudaMemsetAsync(grad, 0, (size_t)L.num_params * sizeof(float), s));
+  if (!O) FK_CUDA(cudaMemsetAsync(grad, 0, (size_t)L.num_params * sizeof(float), s));
   {
     HeadBwdArgs h;
     const int io = L.n_convs - 1;
@@ -774,8 +778,31 @@ static int backward_tc(const NetLayout& L, const void* packed, const float* para
     w.N = 4;
     w.spins = spins;
     w.part = G.part;
-    if ((st = launch_wgrad<T, float>(L, w, L.conv[io], grad, nullptr, batch, s)) != FK_OK) return st;
+    if ((st = launch_wgrad<T, float>(L, w, L.conv[io], grad, O, batch, s)) != FK_OK) return st;
   }
+  // per-sample weight gradient of one conv: taps of `kind` (or one tap at
+  // (dr, dc) for the 1x1 convs), input X (cin channels), gradient channels
+  // [g0, g0 + n) of Gt
+  auto wg_rows = [&](int kind, int dr, int dc, const void* X, int cin, const void* Gt, int g0, int n,
+                     const ConvDesc& cd) -> int {
+    WgArgs w;
+    memset(&w, 0, sizeof(w));
+    w.spins = spins;
+    if (kind >= 0) {
+      tap_list(kind, w);
+    } else {
+      w.ntaps = 1;
+      w.dr[0] = dr;
+      w.dc[0] = dc;
+    }
+    w.X = X;
+    w.cin = cin;
+    w.G = Gt;
+    w.gC = F;
+    w.g0 = g0;
+    w.N = n;
+    return launch_wgrad<T, T>(L, w, cd, nullptr, O, batch, s);
+  };
   auto wg = [&](const void* X, int x_rows, int x_row0, const void* Gt, int g0, int n, int ntc, int dc0,
                 const ConvDesc& cd) -> int {
     WgTcArgs a;
@@ -821,12 +848,24 @@ static int backward_tc(const NetLayout& L, const void* packed, const float* para
       if ((st = launch_bwd_op(b, tiles, L.H, L.W, err, s)) != FK_OK) return st;
     }
     // weight and bias gradients of the five convs of causal conv i
-    if ((st = wg(A.cat[i], 3, -2, G.ghp[i], 0, F, 3, -2, cc)) != FK_OK) return st;
-    if ((st = wg(A.t[i], 1, 0, G.gcatm, 0, F / 2, 1, -shift, cx)) != FK_OK) return st;
-    if ((st = wg(A.rv[i], 1, -1, G.gcatm, F / 2, F / 2, 1, 0, cy)) != FK_OK) return st;
+    if (O) {
+      if ((st = wg_rows(kConvC, 0, 0, A.cat[i], F, G.ghp[i], 0, F, cc)) != FK_OK) return st;
+      if ((st = wg_rows(-1, 0, -shift, A.t[i], F, G.gcatm, 0, F / 2, cx)) != FK_OK) return st;
+      if ((st = wg_rows(-1, -1, 0, A.rv[i], F, G.gcatm, F / 2, F / 2, cy)) != FK_OK) return st;
+      if (i > 0) {
+        if ((st = wg_rows(kConvH, 0, 0, A.h[i - 1], F, G.gt, 0, F, ch)) != FK_OK) return st;
+        if ((st = wg_rows(kConvV, 0, 0, A.v[i - 1], F, G.gvp, 0, F, cv)) != FK_OK) return st;
+      }
+    } else {
+      if ((st = wg(A.cat[i], 3, -2, G.ghp[i], 0, F, 3, -2, cc)) != FK_OK) return st;
+      if ((st = wg(A.t[i], 1, 0, G.gcatm, 0, F / 2, 1, -shift, cx)) != FK_OK) return st;
+      if ((st = wg(A.rv[i], 1, -1, G.gcatm, F / 2, F / 2, 1, 0, cy)) != FK_OK) return st;
+      if (i > 0) {
+        if ((st = wg(A.h[i - 1], 1, 0, G.gt, 0, F, 3, -2, ch)) != FK_OK) return st;
+        if ((st = wg(A.v[i - 1], 3, -2, G.gvp, 0, F, 3, -1, cv)) != FK_OK) return st;
+      }
+    }
     if (i > 0) {
-      if ((st = wg(A.h[i - 1], 1, 0, G.gt, 0, F, 3, -2, ch)) != FK_OK) return st;
-      if ((st = wg(A.v[i - 1], 3, -2, G.gvp, 0, F, 3, -1, cv)) != FK_OK) return st;
       // cc i = 2b+1 is the first conv of a block whose second conv (2b+2) adds
       // the block input S_{2b} = S_{i-1} as residual
       const bool block_first = (i % 2 == 1) && (i + 1 < last);
@@ -858,13 +897,13 @@ static int backward_tc(const NetLayout& L, const void* packed, const float* para
       w.gC = F;
       w.N = F;
       w.part = G.part;
-      if ((st = launch_wgrad<T, T>(L, w, ch, grad, nullptr, batch, s)) != FK_OK) return st;
+      if ((st = launch_wgrad<T, T>(L, w, ch, grad, O, batch, s)) != FK_OK) return st;
       tap_list(kConvV, w);
       w.G = G.gvp;
-      if ((st = launch_wgrad<T, T>(L, w, cv, grad, nullptr, batch, s)) != FK_OK) return st;
+      if ((st = launch_wgrad<T, T>(L, w, cv, grad, O, batch, s)) != FK_OK) return st;
     }
   }
-  if (L.wn) return launch_wn(L, params, grad, nullptr, batch, s);
+  if (L.wn) return launch_wn(L, params, grad, O, batch, s);
   return FK_OK;
 }
 
@@ -901,12 +940,12 @@ int FK_AR2D_ENTRY(fk_ar2d_backward)(const fk_ar2d_desc* desc, const void* packed
   FK_CHECK_ARG(saved_bytes >= need, "fk_ar2d_backward: saved workspace %lld < %lld bytes", (long long)saved_bytes,
                (long long)need);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  if (!per_sample && use_tc_adjoint(L)) {
+  if (use_tc_adjoint(L)) {
     TcBwdTensors TG;
     int64_t tneed = tc_bwd_layout(L, batch, static_cast<char*>(workspace), &TG);
     FK_CHECK_ARG(workspace && workspace_bytes >= tneed, "fk_ar2d_backward: workspace %lld < %lld bytes",
                  (long long)workspace_bytes, (long long)tneed);
-    return backward_tc(L, packed, params, spins, batch, w, A, TG, grad, s);
+    return backward_tc(L, packed, params, spins, batch, w, A, TG, per_sample ? nullptr : grad, per_sample, s);
   }
   BwdTensors G;
   int64_t gneed = bwd_layout(L, batch, static_cast<char*>(workspace), &G);

@@ -28,10 +28,13 @@ __global__ void center_kernel(float* __restrict__ y, int64_t rows, int64_t cols,
   int lane = threadIdx.x & 31;
   if (row >= rows) return;
   float* r = y + row * cols;
-  double s = 0.0;
-  for (int64_t j = lane; j < cols; j += 32) s += r[j];
+  // compensated float32 sums per lane, a float32 tree over the warp (the
+  // FP64 pipe of this part is narrow)
+  Kahan k;
+  for (int64_t j = lane; j < cols; j += 32) k.add(r[j]);
+  float s = k.s - k.c;
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  float mu = (float)(s / (double)cols);
+  float mu = s / (float)cols;
   for (int64_t j = lane; j < cols; j += 32) r[j] -= mu;
   if (mean && lane == 0) mean[row] = mu;
 }
@@ -129,8 +132,8 @@ __global__ void mirror_kernel(double* t, int64_t n) {
 // T = Y^T Y (Y = [o_re | o_im], P x n, parameter-major fp32) with tcgen05:
 // each fp32 value is split into bf16 hi = bf16(y) and lo = bf16(y - hi), and
 // every product is hi*hi + hi*lo + lo*hi (the lo*lo term is below fp32's
-// rounding), accumulated in fp32 in TMEM: fp32-level accuracy at three
-// bf16 MMAs per product. Output tiles of 128 (i) x 256 (j) samples on or
+// rounding), accumulated in fp32 in TMEM over ranges of at most 4096
+// parameters and in fp64 across ranges: three bf16 MMAs per product. Output tiles of 128 (i) x 256 (j) samples on or
 // above the diagonal, K = parameters split into ranges (work item = tile x
 // range); per range the tile's fp32 sums are added into T with fp64 atomics.
 // Roles (13 warps): 8 converter warps load 64 parameters x (128 + 256)
@@ -149,6 +152,7 @@ constexpr int kStage = 2 * kAB + 2 * kBB;        // 96 KB
 constexpr int kConvWarps = 8, kIssuerWarp = 8;
 constexpr int kThreads = 32 * 13;
 constexpr int kSmem = kStages * kStage + 256;
+static_assert((kM / 8 + kN / 8) * kK % (kConvWarps * 32) == 0, "whole chunks per converter thread");
 }  // namespace gram_tc
 
 struct GramTcArgs {
@@ -256,19 +260,25 @@ __global__ void __launch_bounds__(gram_tc::kThreads, 1) gram_tc_kernel(const __g
         uint8_t *ahi = base, *alo = base + kAB, *bhi = base + 2 * kAB, *blo = base + 2 * kAB + kBB;
         // A: 16 groups of 8 samples x 64 parameters; B: 32 groups x 64.
         // Consecutive threads take consecutive parameters: conflict-free
-        // 16-byte shared stores, one 32-byte sector per global load.
-        for (int q = threadIdx.x; q < (kM / 8 + kN / 8) * kK; q += kConvWarps * 32) {
-          const int pq = q % kK;
-          const int grp = q / kK;
-          float v[8];
-          if (grp < kM / 8) {
-            gram_load8(g, kc + pq, i0 + 8 * grp, v);
-            gram_split_store(v, ahi, alo, (grp * kK + pq) * 16);
-          } else {
-            const int gb = grp - kM / 8;
-            gram_load8(g, kc + pq, j0 + 8 * gb, v);
-            gram_split_store(v, bhi, blo, (gb * kK + pq) * 16);
-          }
+        // 16-byte shared stores, one 32-byte sector per global load. All of
+        // a thread's loads are issued before the first store, so that their
+        // latencies overlap.
+        constexpr int kPer = (kM / 8 + kN / 8) * kK / (kConvWarps * 32);
+        float v[kPer][8];
+#pragma unroll
+        for (int r = 0; r < kPer; ++r) {
+          const int q = threadIdx.x + r * kConvWarps * 32;
+          const int pq = q % kK, grp = q / kK;
+          gram_load8(g, kc + pq, grp < kM / 8 ? i0 + 8 * grp : j0 + 8 * (grp - kM / 8), v[r]);
+        }
+#pragma unroll
+        for (int r = 0; r < kPer; ++r) {
+          const int q = threadIdx.x + r * kConvWarps * 32;
+          const int pq = q % kK, grp = q / kK;
+          if (grp < kM / 8)
+            gram_split_store(v[r], ahi, alo, (grp * kK + pq) * 16);
+          else
+            gram_split_store(v[r], bhi, blo, ((grp - kM / 8) * kK + pq) * 16);
         }
         fence_proxy_async_smem();
         __syncwarp();
@@ -628,10 +638,13 @@ int fk_sr_gram_tc(const float* o_re, const float* o_im, int64_t n_params, int64_
   a.ntj = (n + gram_tc::kN - 1) / gram_tc::kN;
   int64_t tiles = 0;
   for (int64_t ti = 0; ti < a.nti; ++ti) tiles += a.ntj - ti / 2;
-  // parameter ranges: about two items per SM, each range at least 4096 parameters
+  // parameter ranges of at most 4096 parameters: the tensor core sums a
+  // range in fp32 (relative error of a positive sum, e.g. a diagonal entry,
+  // about 2e-5 at this length), the ranges are added in fp64; and at least
+  // two items per SM
   int64_t splits = (2 * 152 + tiles - 1) / tiles;
-  const int64_t max_splits = (n_params + 4095) / 4096;
-  if (splits > max_splits) splits = max_splits;
+  const int64_t min_splits = (n_params + 4095) / 4096;
+  if (splits < min_splits) splits = min_splits;
   if (splits < 1) splits = 1;
   a.kper = ((n_params + splits - 1) / splits + gram_tc::kK - 1) / gram_tc::kK * gram_tc::kK;
   a.splits = (n_params + a.kper - 1) / a.kper;

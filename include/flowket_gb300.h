@@ -260,9 +260,10 @@ int fk_sr_gram(const float* o_re, const float* o_im, int64_t n_params, int64_t n
                int64_t gram_elems, void* stream);
 /* The same Gram on the tensor cores (tcgen05, kind::f16): every float32 value
  * is split into bf16 hi + lo and each product taken as hi*hi + hi*lo + lo*hi
- * with float32 accumulation in TMEM, float64 sums across parameter ranges:
- * the float32 Gram's accuracy from bf16 MMAs. n_samples a multiple of 8,
- * o_re / o_im 16-byte aligned, n <= 65536. */
+ * with float32 accumulation in TMEM over ranges of at most 4096 parameters,
+ * float64 sums across ranges (relative error of an entry against
+ * sqrt(T_ii T_jj): ~2e-7 off the diagonal, up to ~2e-5 on it). n_samples a
+ * multiple of 8, o_re / o_im 16-byte aligned, n <= 65536. */
 int fk_sr_gram_tc(const float* o_re, const float* o_im, int64_t n_params, int64_t n_samples, double* gram,
                   int64_t gram_elems, void* stream);
 /* FP64 conjugate gradients on (scale * gram + shift I) x = rhs, stopping at

@@ -162,3 +162,46 @@ def test_backward_recompute_equals_saved_adjoint(cuda):
     want = m.backward(sc, w, saved).cpu().numpy().astype(np.float64)
     got = m.backward_recompute(sc, w, chunk=128).cpu().numpy().astype(np.float64)
     assert np.linalg.norm(got - want) / np.linalg.norm(want) < 1e-5
+
+
+@pytest.mark.parametrize("precision", ["bf16", "fp16"])
+def test_tensor_core_per_sample_rows_match_cuda_core(cuda, tmp_path, precision):
+    """Per-sample O on the tensor-core path (data gradients on tcgen05 with
+    16-bit gradients between ops, per-sample weight gradients on CUDA cores)
+    against the CUDA-core adjoint's rows on the same saved activations
+    (FK_AR2D_ENGINE=rowwise): the same bound as the summed gradients
+    (relative < 3e-2, cosine > 0.999), per sample and overall."""
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    shape, depth, b = (5, 7), 4, 160
+    code = (
+        "import sys; sys.path.insert(0, %r);"
+        "import numpy as np, torch;"
+        "from flowket_gb300 import _lib;"
+        "from flowket_gb300.machines import ConvNetAutoregressive2D;"
+        "m = ConvNetAutoregressive2D(%r, %d, 32, weights_normalization=True, precision=%r, seed=5);"
+        "rng = np.random.default_rng(6);"
+        "s = torch.as_tensor(rng.choice([-1, 1], size=(%d,) + %r).astype(np.int8)).cuda();"
+        "_, _, saved = m.forward(s, mode=_lib.FK_AR2D_SAVE);"
+        "np.save(%r, m.log_derivatives(s, saved).cpu().numpy())"
+    ) % (root, shape, depth, precision, b, shape, str(tmp_path / "o.npy"))
+    env = dict(os.environ, FK_AR2D_ENGINE="rowwise")
+    subprocess.run([sys.executable, "-c", code], check=True, env=env)
+    ref = np.load(tmp_path / "o.npy").astype(np.complex128)
+    from flowket_gb300 import _lib
+    from flowket_gb300.machines import ConvNetAutoregressive2D
+    m = ConvNetAutoregressive2D(shape, depth, 32, weights_normalization=True, precision=precision, seed=5)
+    rng = np.random.default_rng(6)
+    s = torch.as_tensor(rng.choice([-1, 1], size=(b,) + shape).astype(np.int8)).cuda()
+    _, _, saved = m.forward(s, mode=_lib.FK_AR2D_SAVE)
+    got = m.log_derivatives(s, saved).cpu().numpy().astype(np.complex128)
+    rel = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+    assert rel < 3e-2, rel
+    for part in (np.real, np.imag):
+        g, r = part(got), part(ref)
+        cos = (g * r).sum(0) / (np.linalg.norm(g, axis=0) * np.linalg.norm(r, axis=0))
+        assert cos.min() > 0.999, cos.min()
+    # the rows weighted by the seeds sum to the summed tensor-core gradient
+    w = rng.normal(size=(b, 2)).astype(np.float32)
+    summed = m.backward(s, torch.as_tensor(w).cuda(), saved).cpu().numpy().astype(np.float64)
+    from_rows = got.real @ w[:, 0] + got.imag @ w[:, 1]
+    assert np.linalg.norm(from_rows - summed) / np.linalg.norm(summed) < 3e-2

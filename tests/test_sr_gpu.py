@@ -37,9 +37,11 @@ def test_gram_and_solve_match_numpy(cuda):
                                          (1000, 40, False), (64, 8, True)])
 def test_tensor_core_gram_matches_fp64(cuda, p, b, complex_):
     """fk_sr_gram_tc (tcgen05, split-BF16 products, FP32 accumulation) against
-    the FP64 Gram of the same FP32 rows: FP32-level error, like the CUDA-core
-    fk_sr_gram. Sizes not multiples of the 128 x 256 tiles or of the 64
-    parameters per stage, and a single tile."""
+    the FP64 Gram of the same FP32 rows, relative to sqrt(T_ii T_jj): 5e-5
+    (the tensor core sums a 4096-parameter range in FP32: 2e-5 measured on
+    the diagonal, where every term is positive; 2e-7 off it), and the
+    CUDA-core fk_sr_gram at 1e-5. Sizes not multiples of the 128 x 256 tiles
+    or of the 64 parameters per stage, and a single tile."""
     from flowket_gb300 import _lib
     rng = np.random.default_rng(p + b)
     a = rng.normal(size=(p, b)).astype(np.float32)
@@ -55,7 +57,9 @@ def test_tensor_core_gram_matches_fp64(cuda, p, b, complex_):
         _lib.call(entry, _lib.ptr(ta), _lib.ptr(tc), p, b, _lib.ptr(gram), n * n, _lib.stream_ptr())
         got = gram.cpu().numpy()
         err = np.abs(got - want) / scale
-        assert err.max() < 1e-5, (entry, err.max())
+        assert err.max() < (5e-5 if entry == "fk_sr_gram_tc" else 1e-5), (entry, err.max())
+        off = err[~np.eye(n, dtype=bool)]
+        assert off.max() < 2e-6, (entry, off.max())
         np.testing.assert_array_equal(got, got.T)
 
 
