@@ -70,6 +70,8 @@ def parse():
                         "(enumeration of all 2^16 states) with Lanczos, in --precision")
     p.add_argument("--precision", default="bf16", choices=["bf16", "fp16", "fp32"])
     p.add_argument("--sr-steps", type=int, default=20)
+    p.add_argument("--sr-leg-steps", type=int, default=3,
+                   help="timed steps per precision of the bench line's J1-J2 SR leg (0: skip)")
     p.add_argument("--precisions", nargs="+", default=None, choices=["bf16", "fp16", "fp32"])
     p.add_argument("--optimizer", default="adam", choices=["adam", "sr"])
     p.add_argument("--lr", type=float, default=0.02)
@@ -216,14 +218,15 @@ def matched_case(args):
     print(json.dumps(out), flush=True)
 
 
-def j1j2sr_case(args):
+def j1j2sr_summary(steps, precisions):
     """J1-J2 10x10 periodic, J2/J1 = 0.5 (operators/j1j2.py edge list);
     ConvNetAutoregressive2D depth 20, 32 channels (weight norm), Re and Im
     heads; 1024 exact samples per step; stochastic reconfiguration
-    (diag_shift 1e-3, lr 0.05, FP32 Gram reduced in FP64, FP64 CG). Runs
-    `--sr-steps` full steps (sampling, local energy over the used
-    connections, per-sample log-derivatives, Gram, solve, update) on each
-    precision from the same seeded parameters: ms per step, stage split,
+    (diag_shift 1e-3, lr 0.05; Gram on the tensor cores for BF16/FP16, on the
+    CUDA cores for the plain FP32 path; FP64 CG). Runs `steps` full steps
+    (sampling, local energy over the used connections, per-sample
+    log-derivatives, Gram, solve, update) on each precision from the same
+    seeded parameters after one untimed step: ms per step, stage split,
     energy and variance per step."""
     from flowket_gb300.machines import ConvNetAutoregressive2D
     from flowket_gb300.operators import J1J2
@@ -232,16 +235,15 @@ def j1j2sr_case(args):
     from flowket_gb300.samplers import FastAutoregressiveSampler
     shape, b = (10, 10), 1024
     op = J1J2(hilbert_state_shape=shape, j2=0.5, pbc=True)
-    out = {"case": "j1j2sr", "workload": "J1-J2 10x10 PBC J2=0.5; ConvNetAutoregressive2D depth 20 F32 (weight "
-                                         "norm); 1024 samples/step; SR diag_shift 1e-3 lr 0.05", "steps": args.sr_steps}
-    precisions = args.precisions or ["bf16", "fp16", "fp32"]
+    out = {"workload": "J1-J2 10x10 PBC J2=0.5; ConvNetAutoregressive2D depth 20 F32 (weight norm); 1024 "
+                       "samples/step; full VMC step with SR diag_shift 1e-3 lr 0.05", "steps": steps}
     for prec in precisions:
         m = ConvNetAutoregressive2D(shape, 20, 32, weights_normalization=True, precision=prec, seed=0)
         vmc = VariationalMonteCarlo(m, op, FastAutoregressiveSampler(m, b, seed=1234))
         opt = ComplexValuesStochasticReconfiguration(m, lr=0.05, diag_shift=1e-3)
         vmc.step(opt)
         energies, variances, ms, stages = [], [], [], []
-        for _ in range(args.sr_steps):
+        for _ in range(steps):
             a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record()
             vmc.step(opt)
@@ -262,6 +264,12 @@ def j1j2sr_case(args):
     for prec in ("bf16", "fp16"):
         if prec in out and "fp32" in out:
             out[prec + "_over_fp32"] = out["fp32"]["ms_per_step"] / out[prec]["ms_per_step"]
+    return out
+
+
+def j1j2sr_case(args):
+    out = {"case": "j1j2sr"}
+    out.update(j1j2sr_summary(args.sr_steps, args.precisions or ["bf16", "fp16", "fp32"]))
     print(json.dumps(out), flush=True)
 
 
@@ -434,6 +442,9 @@ def kernels_case(args):
                                  _lib.ptr(alpha), _lib.ptr(stats), _lib.ptr(ws), ws.numel(), st))
     record("sr_cg_50_iterations", ms, nbytes=iters * n * n * 8, n=n,
            note="the Gram (33.6 MB) stays in L2 across iterations: bytes are per-iteration reads")
+    ms = timed(lambda: _lib.call("fk_center_columns", _lib.ptr(o_re), p, bs, None, st))
+    record("sr_center_columns", ms, nbytes=2 * p * bs * 4, params=p, samples=bs,
+           note="one read for the mean, one read-modify-write pass (the second read hits L2 per row)")
     x = torch.empty(p, device="cuda")
     ms = timed(lambda: _lib.call("fk_sr_backmap", _lib.ptr(o_re), _lib.ptr(o_im), p, bs, _lib.ptr(alpha), 1.0 / bs,
                                  0.0, None, _lib.ptr(x), st))
@@ -834,6 +845,9 @@ def ours_arm(args, rank, world):
     matched = None
     if args.matched_steps > 0 and rank == 0:
         matched = matched_summary(args.matched_steps, args.matched_batch, args.matched_samples)
+    sr_leg = None
+    if args.sr_leg_steps > 0 and rank == 0:
+        sr_leg = j1j2sr_summary(args.sr_leg_steps, ["bf16", "fp32"])
 
     peaks = {}
     try:
@@ -868,6 +882,7 @@ def ours_arm(args, rank, world):
                 "energy_bf16": energy_bf16, "fp32_path": fp32,
                 "bf16_over_fp32": (samples_per_s / world) / fp32["samples_per_s"] if fp32 else None,
                 "matched": matched,
+                "sr_step_j1j2_10x10_d20": sr_leg,
                 "stage_ms": vmc.times,
                 "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                              "frac": achieved / peak if achieved else None,
