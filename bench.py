@@ -556,7 +556,8 @@ def energy4x4_case(args):
         # stochastic reconfiguration (the reference's optimizer.py:14-183),
         # learning rate decayed with the same cosine schedule
         from flowket_gb300.optimizers import ComplexValuesStochasticReconfiguration
-        opt = ComplexValuesStochasticReconfiguration(m, lr=args.lr, diag_shift=args.diag_shift)
+        opt = ComplexValuesStochasticReconfiguration(m, lr=args.lr, diag_shift=args.diag_shift,
+                                                     gram="tc" if args.train_batch % 8 == 0 else "fp32")
         lr0, lr1 = args.lr, args.lr * 1e-2
     else:
         opt = Adam(m, lr=1e-3)

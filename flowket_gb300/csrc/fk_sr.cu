@@ -171,7 +171,10 @@ struct GramTcArgs {
 // ti take j-tiles tj >= ti / 2 (the first 256-wide tile reaching row ti*128).
 __device__ __forceinline__ void gram_item(const GramTcArgs& g, int64_t item, int64_t& i0, int64_t& j0, int64_t& k0,
                                           int64_t& k1) {
-  const int64_t tile = item / g.splits, split = item % g.splits;
+  // consecutive items (the CTAs running at the same time) share a parameter
+  // range, so its rows are read from DRAM once and from L2 by every tile
+  const int64_t tiles = g.items / g.splits;
+  const int64_t split = item / tiles, tile = item % tiles;
   int64_t ti = 0, rem = tile;
   while (ti < g.nti && rem >= g.ntj - ti / 2) {
     rem -= g.ntj - ti / 2;
@@ -467,14 +470,24 @@ __global__ void cg_roll_kernel(double* s) {
 // update is float32, so the products and sums are too (compensated per lane,
 // then a tree over the warp): FP64 stays in the solve, and this part's
 // narrow FP64 pipe does not bound the kernel.
-__global__ void backmap_kernel(const float* __restrict__ a, const float* __restrict__ b, int64_t P, int64_t bsz,
-                               int64_t n, const double* __restrict__ alpha, double scale, float lr,
-                               float* __restrict__ params, float* __restrict__ x_out) {
+// alpha is converted to float once per block into shared memory (a
+// double-to-float conversion runs on the FP64 pipe).
+constexpr int kBackmapThreads = 1024;
+constexpr int64_t kBackmapMaxN = 16384;  // float alpha in shared memory: 64 KB
+
+__global__ void __launch_bounds__(kBackmapThreads) backmap_kernel(const float* __restrict__ a,
+                                                                  const float* __restrict__ b, int64_t P, int64_t bsz,
+                                                                  int64_t n, const double* __restrict__ alpha,
+                                                                  double scale, float lr, float* __restrict__ params,
+                                                                  float* __restrict__ x_out) {
+  extern __shared__ float alpha_f[];
+  for (int64_t j = threadIdx.x; j < n; j += blockDim.x) alpha_f[j] = (float)alpha[j];
+  __syncthreads();
   int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   if (row >= P) return;
   Kahan k;
-  for (int64_t j = lane; j < n; j += 32) k.add(ycol(a, b, bsz, row, j) * (float)alpha[j]);
+  for (int64_t j = lane; j < n; j += 32) k.add(ycol(a, b, bsz, row, j) * alpha_f[j]);
   float acc = k.s - k.c;
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
   if (lane == 0) {
@@ -513,9 +526,15 @@ __global__ void hermitian_embed_kernel(double* g, int64_t n) {
 // (A, C parameter-major rows); params (interleaved re, im) -= lr * x when
 // params != NULL, x (interleaved) written to x_out when != NULL. Warp per
 // row, float32 compensated sums as in backmap_kernel.
-__global__ void complex_backmap_kernel(const float* __restrict__ a, const float* __restrict__ c, int64_t P,
-                                       int64_t bsz, const double* __restrict__ z, double scale, float lr,
-                                       float2* __restrict__ params, float2* __restrict__ x_out) {
+__global__ void __launch_bounds__(kBackmapThreads) complex_backmap_kernel(const float* __restrict__ a,
+                                                                          const float* __restrict__ c, int64_t P,
+                                                                          int64_t bsz, const double* __restrict__ z,
+                                                                          double scale, float lr,
+                                                                          float2* __restrict__ params,
+                                                                          float2* __restrict__ x_out) {
+  extern __shared__ float z_f[];
+  for (int64_t j = threadIdx.x; j < 2 * bsz; j += blockDim.x) z_f[j] = (float)z[j];
+  __syncthreads();
   int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   if (row >= P) return;
@@ -523,7 +542,7 @@ __global__ void complex_backmap_kernel(const float* __restrict__ a, const float*
   const float* cr = c + row * bsz;
   Kahan kr, ki;
   for (int64_t j = lane; j < bsz; j += 32) {
-    const float av = ar[j], cv = cr[j], zr = (float)z[j], zi = (float)z[bsz + j];
+    const float av = ar[j], cv = cr[j], zr = z_f[j], zi = z_f[bsz + j];
     kr.add(av * zr + cv * zi);
     ki.add(av * zi - cv * zr);
   }
@@ -540,6 +559,19 @@ __global__ void complex_backmap_kernel(const float* __restrict__ a, const float*
       params[row] = make_float2(p.x - lr * xv.x, p.y - lr * xv.y);
     }
   }
+}
+
+// Both back-maps stage up to 64 KB of float coefficients in shared memory.
+static cudaError_t backmap_smem_attr() {
+  static bool done = false;
+  if (done) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(backmap_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)(kBackmapMaxN * sizeof(float)));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(complex_backmap_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(kBackmapMaxN * sizeof(float)));
+  done = e == cudaSuccess;
+  return e;
 }
 
 }  // namespace fk
@@ -561,8 +593,12 @@ int fk_sr_complex_backmap(const float* o_re, const float* o_im, int64_t n_params
                           const double* z, double scale, float lr, float* params, float* x_out, void* stream) {
   FK_CHECK_ARG(o_re && o_im && z && n_params > 0 && n_samples > 0 && (params || x_out),
                "fk_sr_complex_backmap: bad arguments");
+  FK_CHECK_ARG(2 * n_samples <= kBackmapMaxN, "fk_sr_complex_backmap: 2 n_samples = %lld exceeds %lld",
+               (long long)(2 * n_samples), (long long)kBackmapMaxN);
+  FK_CUDA(backmap_smem_attr());
   int64_t threads = n_params * 32;
-  complex_backmap_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+  complex_backmap_kernel<<<(unsigned)((threads + kBackmapThreads - 1) / kBackmapThreads), kBackmapThreads,
+                           (size_t)(2 * n_samples) * sizeof(float), static_cast<cudaStream_t>(stream)>>>(
       o_re, o_im, n_params, n_samples, z, scale, lr, reinterpret_cast<float2*>(params),
       reinterpret_cast<float2*>(x_out));
   FK_CUDA(launched());
@@ -697,8 +733,11 @@ int fk_sr_backmap(const float* o_re, const float* o_im, int64_t n_params, int64_
                   double scale, float lr, float* params, float* x_out, void* stream) {
   FK_CHECK_ARG(o_re && alpha && n_params > 0 && n_samples > 0 && (params || x_out), "fk_sr_backmap: bad arguments");
   int64_t n = o_im ? 2 * n_samples : n_samples;
+  FK_CHECK_ARG(n <= kBackmapMaxN, "fk_sr_backmap: n = %lld exceeds %lld", (long long)n, (long long)kBackmapMaxN);
+  FK_CUDA(backmap_smem_attr());
   int64_t threads = n_params * 32;
-  backmap_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+  backmap_kernel<<<(unsigned)((threads + kBackmapThreads - 1) / kBackmapThreads), kBackmapThreads,
+                   (size_t)n * sizeof(float), static_cast<cudaStream_t>(stream)>>>(
       o_re, o_im ? o_im : o_re, n_params, n_samples, n, alpha, scale, lr, params, x_out);
   FK_CUDA(launched());
   return FK_OK;
