@@ -150,6 +150,12 @@ __device__ void pipe_producer(const PipeGeom& g, const PipeItems& items, const v
   }
 }
 
+// Input columns released to the issuer per rendezvous: the issuer issues
+// their MMAs back to back (same MMAs, same order, so results are unchanged),
+// and the rendezvous cost is shared. The ring (>= 6 slots) and the TMEM
+// accumulator slots (>= 8) hold the columns and outputs of a step.
+constexpr int kColsPerStep = 2;
+
 // Waiter (whole warp).
 template <int F>
 __device__ void pipe_waiter(const PipeGeom& g, const PipeItems& items, uint64_t* full, uint64_t* wbar,
@@ -157,18 +163,22 @@ __device__ void pipe_waiter(const PipeGeom& g, const PipeItems& items, uint64_t*
   using C = PipeCfg<F>;
   constexpr int NR = C::kNcol;
   constexpr int NS = C::kNS;
+  static_assert(NR >= 2 * kColsPerStep && NS >= 3 + kColsPerStep + 1, "ring or TMEM slots too few for a step");
   pwait(wbar, 0, err, abort);
   uint32_t gx = 0, gbase = 0;
   bool stop = false;
   for (int64_t it = blockIdx.x; it < items.n && !stop; it += gridDim.x) {
-    for (int x = 0; x < g.W; ++x, ++gx) {
-      pwait(&full[gx % NR], (gx / NR) & 1, err, abort);
-      const int c_lo = x + g.o0 < 0 ? 0 : x + g.o0;
-      const int c_hi = x + g.o0 + 2 < g.W - 1 ? x + g.o0 + 2 : g.W - 1;
-      const int c_f = x == 0 ? c_lo : (x + g.o0 + 2 < c_hi + 1 ? x + g.o0 + 2 : c_hi + 1);
-      for (int c = c_f; c <= c_hi; ++c) {
-        const uint32_t p = gbase + (uint32_t)c;
-        if (p >= (uint32_t)NS) pwait(&acce[p % NS], ((p / NS) - 1) & 1, err, abort);
+    for (int x0 = 0; x0 < g.W; x0 += kColsPerStep) {
+      const int x1 = x0 + kColsPerStep < g.W ? x0 + kColsPerStep : g.W;
+      for (int x = x0; x < x1; ++x, ++gx) {
+        pwait(&full[gx % NR], (gx / NR) & 1, err, abort);
+        const int c_lo = x + g.o0 < 0 ? 0 : x + g.o0;
+        const int c_hi = x + g.o0 + 2 < g.W - 1 ? x + g.o0 + 2 : g.W - 1;
+        const int c_f = x == 0 ? c_lo : (x + g.o0 + 2 < c_hi + 1 ? x + g.o0 + 2 : c_hi + 1);
+        for (int c = c_f; c <= c_hi; ++c) {
+          const uint32_t p = gbase + (uint32_t)c;
+          if (p >= (uint32_t)NS) pwait(&acce[p % NS], ((p / NS) - 1) & 1, err, abort);
+        }
       }
       stop = step_rendezvous(abort);
       if (stop) break;
@@ -260,9 +270,11 @@ __device__ void pipe_issuer(const PipeGeom& g, const PipeItems& items, uint8_t* 
     int k_lo, k_hi;
     ring_rows(g, r, k_lo, k_hi);
     for (int x = 0; x < W; ++x) {
-      abort = step_rendezvous(false);
-      if (abort) break;
-      tc_fence_after();
+      if (x % kColsPerStep == 0) {
+        abort = step_rendezvous(false);
+        if (abort) break;
+        tc_fence_after();
+      }
       const int c_lo = x + o0 < 0 ? 0 : x + o0;
       const int c_hi = x + o0 + 2 < W - 1 ? x + o0 + 2 : W - 1;
       // outputs first reached by this column, [c_f, c_hi]: all of them at
