@@ -550,6 +550,23 @@ def energy4x4_case(args):
         p = p / p.sum()
         return float((p * obs.local_values(m, states, log_psi=lp)[:, 0]).sum())
 
+    # connected states of every state as indices into the table of all
+    # states (state bit k = 1 <-> spin +1 at site k; a used slot exchanges
+    # two opposite spins, i.e. toggles two bits)
+    flips, mel_all, use_all, _ = op.enumerate(states)
+    f64 = flips.to(torch.int64)
+    toggles = torch.where(f64 >= 0, torch.ones_like(f64) << f64.clamp(min=0), torch.zeros_like(f64)).sum(-1)
+    conn_idx = idx[None, :] ^ toggles
+
+    def exact_energy_table(lp):
+        """Exact energy of a wave function given on every state (FP64)."""
+        lpc = torch.complex(lp[:, 0].double(), lp[:, 1].double())
+        p = torch.exp(2 * lpc.real)
+        p = p / p.sum()
+        ratio = torch.exp(lpc[conn_idx] - lpc[None, :])
+        eloc = (mel_all * use_all.double() * ratio).sum(0)
+        return float((p * eloc.real).sum())
+
     m = ConvNetAutoregressive2D(shape, 5, 16, weights_normalization=False, precision=args.precision, seed=0)
     vmc = VariationalMonteCarlo(m, op, FastAutoregressiveSampler(m, args.train_batch, seed=1234))
     if args.optimizer == "sr":
@@ -572,10 +589,23 @@ def energy4x4_case(args):
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t0
     e = exact_energy(m)
-    print(json.dumps({"case": "energy4x4", "precision": args.precision, "optimizer": args.optimizer,
-                      "steps": args.train_steps, "batch": args.train_batch, "exact_energy": e, "lanczos": e0,
-                      "relative_error": abs(e - e0) / abs(e0), "train_s": train_s,
-                      "trace_relative_error": [(k, abs(x - e0) / abs(e0)) for k, x in trace]}), flush=True)
+    out = {"case": "energy4x4", "precision": args.precision, "optimizer": args.optimizer,
+           "steps": args.train_steps, "batch": args.train_batch, "exact_energy": e, "lanczos": e0,
+           "relative_error": abs(e - e0) / abs(e0), "train_s": train_s,
+           "trace_relative_error": [(k, abs(x - e0) / abs(e0)) for k, x in trace]}
+    # the trained network evaluated through the reference's symmetrised
+    # ensembles (machines/ensemble.py:41-66), as its published numbers are
+    # (experiments/run_evaluation.py:12-24): exact energies over all states
+    from flowket_gb300.ensemble import make_pbc_invariants, make_up_down_invariant
+    ens = {"plain": m, "up_down": make_up_down_invariant(m),
+           "translations_d4": make_pbc_invariants(m),
+           "translations_d4_up_down": make_up_down_invariant(make_pbc_invariants(m))}
+    out["ensembles"] = {}
+    for name, mach in ens.items():
+        lp, _, _ = mach.forward(states)
+        en = exact_energy_table(lp)
+        out["ensembles"][name] = {"exact_energy": en, "relative_error": abs(en - e0) / abs(e0)}
+    print(json.dumps(out), flush=True)
 
 
 def dist_init(n):
