@@ -120,25 +120,38 @@ def vmc16_case(args):
     """Heisenberg 16x16 PBC (Marshall sign), ConvNetAutoregressive2D depth 20,
     64 channels (weight norm), `--batch` samples per step: full VMC steps
     (exact sampling, local energy over the connected configurations with
-    causal reuse, adjoint gradient, Adam) of the BF16 path and of the plain
-    FP32 path of the same code, each after one warm-up step, CUDA-event
-    timed. Both start from the same seeded parameters."""
+    causal reuse, adjoint gradient) of the BF16 path and of the plain FP32
+    path of the same code, each after one warm-up step, CUDA-event timed.
+    Both start from the same seeded parameters. `--optimizer adam` (lr 1e-3)
+    or `sr`: stochastic reconfiguration (diag shift 1e-3, lr 0.05, CG) with
+    the per-sample rows streamed into the Gram conv by conv (their
+    num_params x 2B array, 222 GB at 8192 samples, is never stored); with SR
+    both paths run the same `--steps` timed steps and the peak device memory
+    of each path is reported."""
     from flowket_gb300.machines import ConvNetAutoregressive2D
     from flowket_gb300.operators import Heisenberg
     from flowket_gb300.optimization import VariationalMonteCarlo
-    from flowket_gb300.optimizers import Adam
+    from flowket_gb300.optimizers import Adam, ComplexValuesStochasticReconfiguration
     from flowket_gb300.samplers import FastAutoregressiveSampler
     shape = (16, 16)
+    sr = args.optimizer == "sr"
     out = {"case": "vmc16", "workload": "Heisenberg 16x16 PBC, Marshall sign; ConvNetAutoregressive2D depth 20 F64 "
-                                        "(weight norm); full VMC step with Adam", "batch": args.batch}
+                                        "(weight norm); full VMC step with " +
+                                        ("SR (diag shift 1e-3, lr 0.05, streamed Gram)" if sr else "Adam"),
+           "batch": args.batch}
     for prec in ("bf16", "fp32"):
         m = ConvNetAutoregressive2D(shape, 20, 64, weights_normalization=True, precision=prec, seed=0)
         vmc = VariationalMonteCarlo(m, Heisenberg(hilbert_state_shape=shape, pbc=True),
                                     FastAutoregressiveSampler(m, args.batch, seed=1234))
-        opt = Adam(m, lr=1e-3)
+        if sr:
+            opt = ComplexValuesStochasticReconfiguration(m, lr=0.05, diag_shift=1e-3)
+        else:
+            opt = Adam(m, lr=1e-3)
+        torch.cuda.synchronize()
+        torch.cuda.reset_peak_memory_stats()
         vmc.step(opt)
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        steps = max(1, args.steps if prec == "bf16" else args.fp32_steps)
+        steps = max(1, args.steps if (prec == "bf16" or sr) else args.fp32_steps)
         torch.cuda.synchronize()
         a.record()
         for _ in range(steps):
@@ -147,7 +160,14 @@ def vmc16_case(args):
         torch.cuda.synchronize()
         ms = a.elapsed_time(b) / steps
         out[prec] = {"ms_per_step": ms, "samples_per_s": args.batch / (ms / 1e3), "steps": steps,
-                     "stage_ms": vmc.times, "energy": vmc.current_energy.real}
+                     "stage_ms": vmc.times, "energy": vmc.current_energy.real,
+                     "peak_memory_gb": torch.cuda.max_memory_allocated() / 1e9}
+        if sr:
+            out[prec].update({"num_params": m.num_params, "streamed": opt.streamed,
+                              "cg_iterations_last": float(opt.last_stats[0]),
+                              "per_sample_rows_gb_if_stored": 2 * m.num_params * args.batch * 4 / 1e9})
+        del vmc, opt, m
+        torch.cuda.empty_cache()
     out["bf16_over_fp32"] = out["fp32"]["ms_per_step"] / out["bf16"]["ms_per_step"]
     print(json.dumps(out), flush=True)
 

@@ -306,6 +306,10 @@ int fk_ar2d_forward_connections_tc_fp16(const fk_ar2d_desc* desc, const void* pa
 int fk_ar2d_backward_tc_fp16(const fk_ar2d_desc* desc, const void* packed, const float* params, const int8_t* spins,
                              int64_t batch, const float* w, const void* saved, int64_t saved_bytes, void* workspace,
                              int64_t workspace_bytes, float* grad, float* per_sample, void* stream);
+int fk_ar2d_sr_gram_tc_fp16(const fk_ar2d_desc* desc, const void* packed, const float* params, const int8_t* spins,
+                            int64_t batch, const void* saved, int64_t saved_bytes, void* workspace,
+                            int64_t workspace_bytes, float* rows, int64_t rows_floats, double* gram,
+                            int32_t tensor_cores, void* stream);
 }
 #define FK_DISPATCH_FP16(desc, call) \
   do {                                \

@@ -273,8 +273,9 @@ struct WgArgs {
   int gC, g0, N;
   float* dW;            // summed raw kernel gradient [ntaps*cin][N]
   float* dB;            // summed bias gradient [N]
-  float* O;             // per-sample: O[(k_off + k*N + n) * batch + b]
+  float* O;             // per-sample: O[(o_kernel + k*N + n) * o_ld + o_col + b]
   int64_t o_kernel, o_bias;
+  int64_t o_ld, o_col;
   int64_t batch;
   int items;            // work items = ntaps * ceil(cin/8) * ceil(N/8)
   int items_per_cta;
@@ -339,10 +340,10 @@ __global__ void __launch_bounds__(128) wgrad_kernel(const __grid_constant__ WgAr
       if (b < a.batch) {
         for (int i = 0; i < kmax; ++i) {
           int64_t row = (int64_t)(t * a.cin + kc * 8 + i) * a.N + nc * 8;
-          for (int j = 0; j < nmax; ++j) a.O[(a.o_kernel + row + j) * a.batch + b] = acc[i][j];
+          for (int j = 0; j < nmax; ++j) a.O[(a.o_kernel + row + j) * a.o_ld + a.o_col + b] = acc[i][j];
         }
         if (with_bias)
-          for (int j = 0; j < nmax; ++j) a.O[(a.o_bias + nc * 8 + j) * a.batch + b] = gb[j];
+          for (int j = 0; j < nmax; ++j) a.O[(a.o_bias + nc * 8 + j) * a.o_ld + a.o_col + b] = gb[j];
       }
     } else {
       // block reduction over the 128 samples, then one atomic per element
@@ -409,6 +410,7 @@ struct WnArgs {
   float* O;        // per-sample rows (kernel slots hold dW on entry)
   int64_t batch;
   ConvDesc conv[kMaxConvs];
+  int64_t o_row[kMaxConvs];  // per-sample: row of O holding the conv's first kernel element
 };
 
 __global__ void wn_kernel(const __grid_constant__ WnArgs a) {
@@ -427,8 +429,9 @@ __global__ void wn_kernel(const __grid_constant__ WnArgs a) {
   for (int k = 0; k < K; ++k) sq += v[(int64_t)k * N + n] * v[(int64_t)k * N + n];
   float inv = rsqrtf(fmaxf(sq, 1e-12f));
   float eg = expf(a.params[p_g + n]);
+  const int64_t o_row = a.o_row[blockIdx.y];
   auto at = [&](int k) -> float& {
-    return a.O ? a.O[(p_kernel + (int64_t)k * N + n) * a.batch + b] : a.grad[p_kernel + (int64_t)k * N + n];
+    return a.O ? a.O[(o_row + (int64_t)k * N + n) * a.batch + b] : a.grad[p_kernel + (int64_t)k * N + n];
   };
   float dot = 0.f;
   for (int k = 0; k < K; ++k) dot += at(k) * v[(int64_t)k * N + n] * inv;
@@ -437,7 +440,7 @@ __global__ void wn_kernel(const __grid_constant__ WnArgs a) {
     at(k) = eg * inv * (at(k) - u * dot);
   }
   if (a.O)
-    a.O[(p_g + n) * a.batch + b] = eg * dot;
+    a.O[(o_row + (p_g - p_kernel) + n) * a.batch + b] = eg * dot;
   else
     a.grad[p_g + n] = eg * dot;
 }
@@ -452,6 +455,7 @@ static int launch_wn(const NetLayout& L, const float* params, float* grad, float
   int maxc = 0;
   for (int k = 0; k < L.n_convs - 1; ++k) {
     a->conv[k] = L.conv[k];
+    a->o_row[k] = L.conv[k].p_kernel;
     maxc = maxc > L.conv[k].cout ? maxc : L.conv[k].cout;
   }
   const int64_t cols = O ? (int64_t)maxc * batch : maxc;
@@ -461,7 +465,159 @@ static int launch_wn(const NetLayout& L, const float* params, float* grad, float
   return check_cuda(launched(), "wn_kernel");
 }
 
+// ---------------------------------------------------------------- SR Gram sink
+// Per-sample rows one conv at a time, for the SR Gram without the whole
+// [num_params][B] arrays: each conv's rows (kernel, bias, weight-norm gain: a
+// contiguous parameter range) go to the next free rows of a buffer whose rows
+// hold the columns of every pass ([0, B): seeds (1, 0), [B, 2B): seeds
+// (0, 1)). When the next step's convs do not fit, and after the last step,
+// the buffered convs get the weight-norm chain rule, every row is centred
+// within each pass's columns, and Y^T Y of the buffer is added into the Gram.
+struct RowSink {
+  const NetLayout* L;
+  const float* params;
+  float* buf;
+  int64_t cap;   // buffer rows
+  int64_t used;
+  int64_t ld;    // row length: passes x B
+  int64_t col;   // first column of the pass being written
+  int groups;    // passes
+  int tensor_cores;
+  double* gram;
+  int n;         // buffered convs
+  int conv[kMaxConvs];
+  int64_t row[kMaxConvs];
+  int64_t at[kMaxConvs];  // buffer row of each conv, -1: not buffered
+};
+
+static int64_t conv_rows(const ConvDesc& cd) {
+  return (cd.p_g >= 0 ? cd.p_g : cd.p_bias) + cd.cout - cd.p_kernel;
+}
+
+static int sink_flush(RowSink& k, cudaStream_t s) {
+  if (k.used == 0) return FK_OK;
+  const NetLayout& L = *k.L;
+  if (L.wn) {
+    WnArgs* a = new WnArgs;
+    a->params = k.params;
+    a->grad = nullptr;
+    a->O = k.buf;
+    a->batch = k.ld;
+    int nw = 0, maxc = 0;
+    for (int i = 0; i < k.n; ++i) {
+      const ConvDesc& cd = L.conv[k.conv[i]];
+      if (cd.p_g < 0) continue;
+      a->conv[nw] = cd;
+      a->o_row[nw++] = k.row[i];
+      maxc = maxc > cd.cout ? maxc : cd.cout;
+    }
+    if (nw > 0) {
+      dim3 grid((unsigned)(((int64_t)maxc * k.ld + 127) / 128), (unsigned)nw);
+      wn_kernel<<<grid, 128, 0, s>>>(*a);
+    }
+    delete a;
+    if (nw > 0) FK_CUDA(launched());
+  }
+  int st = fk_center_columns(k.buf, k.used * k.groups, k.ld / k.groups, nullptr, s);
+  if (st == FK_OK) st = fk_sr_gram_accumulate(k.buf, k.used, k.ld, k.gram, k.tensor_cores, s);
+  for (int i = 0; i < k.n; ++i) k.at[k.conv[i]] = -1;
+  k.used = 0;
+  k.n = 0;
+  return st;
+}
+
+// Buffer rows for the convs cs[0..n) not yet buffered, flushing first when
+// they do not all fit.
+static int sink_reserve(RowSink& k, const int* cs, int n, cudaStream_t s) {
+  int64_t need = 0;
+  for (int i = 0; i < n; ++i)
+    if (k.at[cs[i]] < 0) need += conv_rows(k.L->conv[cs[i]]);
+  FK_CHECK_ARG(need <= k.cap, "fk_ar2d_sr_gram: row buffer of %lld rows < %lld rows of one step", (long long)k.cap,
+               (long long)need);
+  if (k.used + need > k.cap) {
+    int st = sink_flush(k, s);
+    if (st != FK_OK) return st;
+  }
+  for (int i = 0; i < n; ++i) {
+    if (k.at[cs[i]] >= 0) continue;
+    k.at[cs[i]] = k.used;
+    k.conv[k.n] = cs[i];
+    k.row[k.n++] = k.used;
+    k.used += conv_rows(k.L->conv[cs[i]]);
+  }
+  return FK_OK;
+}
+
+// Buffer row of conv `ci`.
+static int sink_place(RowSink& k, int ci, int64_t* r0, cudaStream_t s) {
+  if (k.at[ci] < 0) {
+    int st = sink_reserve(k, &ci, 1, s);
+    if (st != FK_OK) return st;
+  }
+  *r0 = k.at[ci];
+  return FK_OK;
+}
+
+// The convs whose per-sample rows step i of the backward writes (all five
+// convs of causal conv i); the head's are written before step n_cc - 1.
+static void step_convs(int i, int cs[5]) {
+  cs[0] = conv_index(i, kConvC);
+  cs[1] = conv_index(i, kConvX);
+  cs[2] = conv_index(i, kConvY);
+  cs[3] = conv_index(i, kConvH);
+  cs[4] = conv_index(i, kConvV);
+}
+
+// Rows the buffer needs at least: the largest step (or the head).
+static int64_t sink_min_rows(const NetLayout& L) {
+  int64_t m = conv_rows(L.conv[L.n_convs - 1]);
+  for (int i = 0; i < L.n_cc; ++i) {
+    int cs[5];
+    step_convs(i, cs);
+    int64_t r = 0;
+    for (int k = 0; k < 5; ++k) r += conv_rows(L.conv[cs[k]]);
+    m = r > m ? r : m;
+  }
+  return m;
+}
+
+// The head and the steps n_cc - 1 .. 0 of one pass, or of two passes over the
+// same activations (seeds0 / G0 and seeds1 / G1, their per-sample rows in
+// columns [0, B) and [B, 2B) of the sink's buffer). With a sink, the convs of
+// a step get their buffer rows before either pass writes them, so that no
+// flush falls between the passes.
+template <typename GT, typename HeadFn, typename StepFn>
+static int run_passes(const NetLayout& L, int64_t batch, RowSink* sink, const float* seeds0, const GT& G0,
+                      const float* seeds1, const GT* G1, HeadFn& head, StepFn& step, cudaStream_t s) {
+  const int np = G1 ? 2 : 1;
+  const float* sd[2] = {seeds0, seeds1};
+  const GT* gs[2] = {&G0, G1};
+  int st;
+  if (sink) {
+    const int io = L.n_convs - 1;
+    if ((st = sink_reserve(*sink, &io, 1, s)) != FK_OK) return st;
+  }
+  for (int p = 0; p < np; ++p) {
+    if (sink) sink->col = p * batch;
+    if ((st = head(sd[p], *gs[p])) != FK_OK) return st;
+  }
+  for (int i = L.n_cc - 1; i >= 0; --i) {
+    if (sink) {
+      int cs[5];
+      step_convs(i, cs);
+      if ((st = sink_reserve(*sink, cs, 5, s)) != FK_OK) return st;
+    }
+    for (int p = 0; p < np; ++p) {
+      if (sink) sink->col = p * batch;
+      if ((st = step(i, *gs[p])) != FK_OK) return st;
+    }
+  }
+  return FK_OK;
+}
+
 // ---------------------------------------------------------------- driver
+constexpr int kGradRing = 3;
+
 struct BwdTensors {
   float* gvpd[40];
   float* ghp[40];
@@ -484,9 +640,11 @@ static int64_t bwd_layout(const NetLayout& L, int64_t batch, char* base, BwdTens
   BwdTensors tmp;
   BwdTensors* t = T ? T : &tmp;
   memset(t, 0, sizeof(*t));
+  // Step i of the backward reads the gradients of causal convs i and i + 1
+  // and writes those of i - 1: three buffers per stream, indexed i mod 3.
   for (int i = 0; i < L.n_cc; ++i) {
-    t->gvpd[i] = take(tb);
-    t->ghp[i] = take(tb);
+    t->gvpd[i] = i < kGradRing ? take(tb) : t->gvpd[i % kGradRing];
+    t->ghp[i] = i < kGradRing ? take(tb) : t->ghp[i % kGradRing];
   }
   t->gcatm = take(tb);
   t->gt = take(tb);
@@ -536,14 +694,25 @@ __global__ void wgrad_part_reduce_kernel(const float* part, int64_t tiles, int k
 
 template <typename T, typename TG = float>
 static int launch_wgrad(const NetLayout& L, WgArgs& w, const ConvDesc& cd, float* grad, float* O, int64_t batch,
-                        cudaStream_t s) {
+                        cudaStream_t s, RowSink* sink = nullptr) {
   int64_t tiles = (batch + kTile - 1) / kTile;
   w.batch = batch;
   w.items = w.ntaps * ((w.cin + 7) / 8) * ((w.N + 7) / 8);
-  if (O) {
+  if (O && sink) {
+    int64_t r0 = 0;
+    const int st = sink_place(*sink, (int)(&cd - L.conv), &r0, s);
+    if (st != FK_OK) return st;
+    w.O = sink->buf;
+    w.o_kernel = r0;
+    w.o_bias = r0 + (cd.p_bias - cd.p_kernel);
+    w.o_ld = sink->ld;
+    w.o_col = sink->col;
+  } else if (O) {
     w.O = O;
     w.o_kernel = cd.p_kernel;
     w.o_bias = cd.p_bias;
+    w.o_ld = batch;
+    w.o_col = 0;
   } else {
     w.dW = grad + cd.p_kernel;
     w.dB = grad + cd.p_bias;
@@ -562,16 +731,17 @@ static int launch_wgrad(const NetLayout& L, WgArgs& w, const ConvDesc& cd, float
 
 template <int F, typename T>
 static int backward_impl(const NetLayout& L, const void* packed, const float* params, const int8_t* spins,
-                         int64_t batch, const float* seeds, const Tensors& A, const BwdTensors& G, float* grad,
-                         float* O, cudaStream_t s) {
+                         int64_t batch, const float* seeds, const Tensors& A, const BwdTensors& G0, float* grad,
+                         float* O, cudaStream_t s, RowSink* sink = nullptr, const float* seeds1 = nullptr,
+                         const BwdTensors* G1 = nullptr) {
   const int64_t tiles = (batch + kTile - 1) / kTile;
   const unsigned rows = (unsigned)(tiles * L.H);
   const int last = L.n_cc - 1;
-  int st;
   // Per-sample rows are written exactly once per (parameter, sample); the
   // summed gradient accumulates with atomics and starts from zero.
   if (!O) FK_CUDA(cudaMemsetAsync(grad, 0, (size_t)L.num_params * sizeof(float), s));
-  {
+  // head and step i of one pass (seeds, gradient tensors)
+  auto head = [&](const float* seeds, const BwdTensors& G) -> int {
     HeadBwdArgs h;
     const int io = L.n_convs - 1;
     h.hlast = A.h[last];
@@ -595,9 +765,10 @@ static int backward_impl(const NetLayout& L, const void* packed, const float* pa
     w.g0 = 0;
     w.N = 4;
     w.spins = spins;
-    if ((st = launch_wgrad<T>(L, w, L.conv[io], grad, O, batch, s)) != FK_OK) return st;
-  }
-  for (int i = last; i >= 0; --i) {
+    return launch_wgrad<T>(L, w, L.conv[io], grad, O, batch, s, sink);
+  };
+  auto step = [&](int i, const BwdTensors& G) -> int {
+    int st;
     const ConvDesc& cv = L.conv[conv_index(i, kConvV)];
     const ConvDesc& ch = L.conv[conv_index(i, kConvH)];
     const ConvDesc& cx = L.conv[conv_index(i, kConvX)];
@@ -628,7 +799,7 @@ static int backward_impl(const NetLayout& L, const void* packed, const float* pa
     w.G = G.ghp[i];
     w.gC = F;
     w.N = F;
-    if ((st = launch_wgrad<T>(L, w, cc, grad, O, batch, s)) != FK_OK) return st;
+    if ((st = launch_wgrad<T>(L, w, cc, grad, O, batch, s, sink)) != FK_OK) return st;
     memset(&w, 0, sizeof(w));
     w.spins = spins;
     w.ntaps = 1;
@@ -640,12 +811,12 @@ static int backward_impl(const NetLayout& L, const void* packed, const float* pa
     w.gC = F;
     w.g0 = 0;
     w.N = F / 2;
-    if ((st = launch_wgrad<T>(L, w, cx, grad, O, batch, s)) != FK_OK) return st;
+    if ((st = launch_wgrad<T>(L, w, cx, grad, O, batch, s, sink)) != FK_OK) return st;
     w.dr[0] = -1;
     w.dc[0] = 0;
     w.X = A.rv[i];
     w.g0 = F / 2;
-    if ((st = launch_wgrad<T>(L, w, cy, grad, O, batch, s)) != FK_OK) return st;
+    if ((st = launch_wgrad<T>(L, w, cy, grad, O, batch, s, sink)) != FK_OK) return st;
     memset(&w, 0, sizeof(w));
     w.spins = spins;
     tap_list(kConvH, w);
@@ -654,11 +825,11 @@ static int backward_impl(const NetLayout& L, const void* packed, const float* pa
     w.G = G.gt;
     w.gC = F;
     w.N = F;
-    if ((st = launch_wgrad<T>(L, w, ch, grad, O, batch, s)) != FK_OK) return st;
+    if ((st = launch_wgrad<T>(L, w, ch, grad, O, batch, s, sink)) != FK_OK) return st;
     tap_list(kConvV, w);
     w.X = i == 0 ? nullptr : A.v[i - 1];
     w.G = G.gvp;
-    if ((st = launch_wgrad<T>(L, w, cv, grad, O, batch, s)) != FK_OK) return st;
+    if ((st = launch_wgrad<T>(L, w, cv, grad, O, batch, s, sink)) != FK_OK) return st;
     if (i > 0) {
       VHBwdArgs v;
       v.gvp = G.gvp;
@@ -677,7 +848,11 @@ static int backward_impl(const NetLayout& L, const void* packed, const float* pa
       vh_bwd_kernel<F, T><<<rows, 128, 0, s>>>(v, L.H, L.W);
       FK_CUDA(launched());
     }
-  }
+    return FK_OK;
+  };
+  int st = run_passes(L, batch, sink, seeds, G0, seeds1, G1, head, step, s);
+  if (st != FK_OK) return st;
+  if (sink) return sink_flush(*sink, s);
   if (L.wn) return launch_wn(L, params, grad, O, batch, s);
   return FK_OK;
 }
@@ -710,9 +885,9 @@ static int64_t tc_bwd_layout(const NetLayout& L, int64_t batch, char* base, TcBw
   TcBwdTensors tmp;
   TcBwdTensors* t = T ? T : &tmp;
   memset(t, 0, sizeof(*t));
-  for (int i = 0; i < L.n_cc; ++i) {
-    t->gvs[i] = take(tb);
-    t->ghp[i] = take(tb);
+  for (int i = 0; i < L.n_cc; ++i) {  // ring of three, as in bwd_layout
+    t->gvs[i] = i < kGradRing ? take(tb) : t->gvs[i % kGradRing];
+    t->ghp[i] = i < kGradRing ? take(tb) : t->ghp[i % kGradRing];
   }
   t->gcatm = take(tb);
   t->gt = take(tb);
@@ -743,18 +918,19 @@ static bool use_tc_adjoint(const NetLayout& L) {
 // reading the bf16 gradient tensors (the tensor-core weight-gradient GEMM sums
 // over the samples, which per-sample rows must not).
 static int backward_tc(const NetLayout& L, const void* packed, const float* params, const int8_t* spins,
-                       int64_t batch, const float* seeds, const Tensors& A, const TcBwdTensors& G, float* grad,
-                       float* O, cudaStream_t s) {
+                       int64_t batch, const float* seeds, const Tensors& A, const TcBwdTensors& G0, float* grad,
+                       float* O, cudaStream_t s, RowSink* sink = nullptr, const float* seeds1 = nullptr,
+                       const TcBwdTensors* G1 = nullptr) {
   using T = tc16;
   constexpr int F = 32;
   const int64_t tiles = (batch + kTile - 1) / kTile;
   const unsigned rows = (unsigned)(tiles * L.H);
   const int last = L.n_cc - 1;
   int* err = device_error_word();
-  int st;
   auto wt = [&](int idx) { return static_cast<const char*>(packed) + L.conv[idx].wt_off; };
   if (!O) FK_CUDA(cudaMemsetAsync(grad, 0, (size_t)L.num_params * sizeof(float), s));
-  {
+  // head and step i of one pass (seeds, gradient tensors)
+  auto head = [&](const float* seeds, const TcBwdTensors& G) -> int {
     HeadBwdArgs h;
     const int io = L.n_convs - 1;
     h.hlast = A.h[last];
@@ -778,8 +954,8 @@ static int backward_tc(const NetLayout& L, const void* packed, const float* para
     w.N = 4;
     w.spins = spins;
     w.part = G.part;
-    if ((st = launch_wgrad<T, float>(L, w, L.conv[io], grad, O, batch, s)) != FK_OK) return st;
-  }
+    return launch_wgrad<T, float>(L, w, L.conv[io], grad, O, batch, s, sink);
+  };
   // per-sample weight gradient of one conv: taps of `kind` (or one tap at
   // (dr, dc) for the 1x1 convs), input X (cin channels), gradient channels
   // [g0, g0 + n) of Gt
@@ -801,10 +977,12 @@ static int backward_tc(const NetLayout& L, const void* packed, const float* para
     w.gC = F;
     w.g0 = g0;
     w.N = n;
-    return launch_wgrad<T, T>(L, w, cd, nullptr, O, batch, s);
+    return launch_wgrad<T, T>(L, w, cd, nullptr, O, batch, s, sink);
   };
+  // summed weight gradients on the tensor cores (single pass)
   auto wg = [&](const void* X, int x_rows, int x_row0, const void* Gt, int g0, int n, int ntc, int dc0,
                 const ConvDesc& cd) -> int {
+    const TcBwdTensors& G = G0;
     WgTcArgs a;
     a.X = X;
     a.x_rows = x_rows;
@@ -822,7 +1000,8 @@ static int backward_tc(const NetLayout& L, const void* packed, const float* para
     if (r != FK_OK || a.bias_jpos >= 0) return r;
     return launch_bias_sum(Gt, tiles, L.H, L.W, g0, n, batch, G.bpart, grad + cd.p_bias, s);
   };
-  for (int i = last; i >= 0; --i) {
+  auto step = [&](int i, const TcBwdTensors& G) -> int {
+    int st;
     const ConvDesc& cv = L.conv[conv_index(i, kConvV)];
     const ConvDesc& ch = L.conv[conv_index(i, kConvH)];
     const ConvDesc& cx = L.conv[conv_index(i, kConvX)];
@@ -897,14 +1076,41 @@ static int backward_tc(const NetLayout& L, const void* packed, const float* para
       w.gC = F;
       w.N = F;
       w.part = G.part;
-      if ((st = launch_wgrad<T, T>(L, w, ch, grad, O, batch, s)) != FK_OK) return st;
+      if ((st = launch_wgrad<T, T>(L, w, ch, grad, O, batch, s, sink)) != FK_OK) return st;
       tap_list(kConvV, w);
       w.G = G.gvp;
-      if ((st = launch_wgrad<T, T>(L, w, cv, grad, O, batch, s)) != FK_OK) return st;
+      if ((st = launch_wgrad<T, T>(L, w, cv, grad, O, batch, s, sink)) != FK_OK) return st;
     }
-  }
+    return FK_OK;
+  };
+  int st = run_passes(L, batch, sink, seeds, G0, seeds1, G1, head, step, s);
+  if (st != FK_OK) return st;
+  if (sink) return sink_flush(*sink, s);
   if (L.wn) return launch_wn(L, params, grad, O, batch, s);
   return FK_OK;
+}
+
+// Seeds of the two passes of the SR rows: (1, 0) and (0, 1) for every sample.
+__global__ void sr_seeds_kernel(float* s0, float* s1, int64_t batch) {
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= batch) return;
+  s0[2 * b] = 1.f;
+  s0[2 * b + 1] = 0.f;
+  s1[2 * b] = 0.f;
+  s1[2 * b + 1] = 1.f;
+}
+
+// Workspace of fk_ar2d_sr_gram: the gradient tensors of two passes and their
+// seeds. Returns its size; with base != NULL also the pieces.
+static int64_t sr_gram_ws(const NetLayout& L, int64_t batch, char* base, char** g0, char** g1, float** seeds) {
+  const int64_t g = use_tc_adjoint(L) ? tc_bwd_layout(L, batch, nullptr, nullptr) : bwd_layout(L, batch, nullptr, nullptr);
+  const int64_t ga = (g + 255) / 256 * 256;
+  if (base) {
+    *g0 = base;
+    *g1 = base + ga;
+    *seeds = reinterpret_cast<float*>(base + 2 * ga);
+  }
+  return 2 * ga + 4 * batch * (int64_t)sizeof(float);
 }
 
 }  // namespace FK_NS
@@ -963,5 +1169,85 @@ int FK_AR2D_ENTRY(fk_ar2d_backward)(const fk_ar2d_desc* desc, const void* packed
                        : backward_impl<64, float>(L, packed, params, spins, batch, w, A, G, g, O, s);
   }
 }
+
+int FK_AR2D_ENTRY(fk_ar2d_sr_gram)(const fk_ar2d_desc* desc, const void* packed, const float* params,
+                                   const int8_t* spins, int64_t batch, const void* saved, int64_t saved_bytes,
+                                   void* workspace, int64_t workspace_bytes, float* rows, int64_t rows_floats,
+                                   double* gram, int32_t tensor_cores, void* stream) {
+  FK_DISPATCH_FP16(desc, fk_ar2d_sr_gram_tc_fp16(desc, packed, params, spins, batch, saved, saved_bytes, workspace,
+                                                 workspace_bytes, rows, rows_floats, gram, tensor_cores, stream));
+  NetLayout L;
+  int st = build_layout(desc, &L);
+  if (st != FK_OK) return st;
+  FK_CHECK_ARG(packed && params && spins && saved && rows && gram && workspace, "fk_ar2d_sr_gram: NULL buffer");
+  FK_CHECK_ARG(batch > 0, "fk_ar2d_sr_gram: batch must be positive");
+  const int64_t n = 2 * batch;
+  FK_CHECK_ARG(rows_floats / n >= sink_min_rows(L), "fk_ar2d_sr_gram: row buffer of %lld floats < %lld",
+               (long long)rows_floats, (long long)(sink_min_rows(L) * n));
+  FK_CHECK_ARG(workspace_bytes >= sr_gram_ws(L, batch, nullptr, nullptr, nullptr, nullptr),
+               "fk_ar2d_sr_gram: workspace %lld < %lld bytes", (long long)workspace_bytes,
+               (long long)sr_gram_ws(L, batch, nullptr, nullptr, nullptr, nullptr));
+  Tensors A;
+  int64_t need = workspace_layout(L, batch, FK_AR2D_SAVE, static_cast<char*>(const_cast<void*>(saved)), &A);
+  FK_CHECK_ARG(saved_bytes >= need, "fk_ar2d_sr_gram: saved workspace %lld < %lld bytes", (long long)saved_bytes,
+               (long long)need);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  char* g0 = nullptr;
+  char* g1 = nullptr;
+  float* seeds0 = nullptr;
+  float* seeds1 = nullptr;
+  sr_gram_ws(L, batch, static_cast<char*>(workspace), &g0, &g1, &seeds0);
+  seeds1 = seeds0 + 2 * batch;
+  sr_seeds_kernel<<<(unsigned)((batch + 255) / 256), 256, 0, s>>>(seeds0, seeds1, batch);
+  FK_CUDA(launched());
+  FK_CUDA(cudaMemsetAsync(gram, 0, (size_t)(n * n) * sizeof(double), s));
+  RowSink k;
+  k.L = &L;
+  k.params = params;
+  k.buf = rows;
+  k.cap = rows_floats / n;
+  k.used = 0;
+  k.ld = n;
+  k.col = 0;
+  k.groups = 2;
+  k.tensor_cores = tensor_cores;
+  k.gram = gram;
+  k.n = 0;
+  for (int i = 0; i < kMaxConvs; ++i) k.at[i] = -1;
+  if (use_tc_adjoint(L)) {
+    TcBwdTensors T0, T1;
+    tc_bwd_layout(L, batch, g0, &T0);
+    tc_bwd_layout(L, batch, g1, &T1);
+    st = backward_tc(L, packed, params, spins, batch, seeds0, A, T0, nullptr, rows, s, &k, seeds1, &T1);
+  } else {
+    BwdTensors G0, G1;
+    bwd_layout(L, batch, g0, &G0);
+    bwd_layout(L, batch, g1, &G1);
+    const bool bf = L.precision != FK_PRECISION_FP32;
+#define FK_SR_ROWS(FF, TT) backward_impl<FF, TT>(L, packed, params, spins, batch, seeds0, A, G0, nullptr, rows, s, &k, \
+                                                 seeds1, &G1)
+    switch (L.F) {
+      case 16: st = bf ? FK_SR_ROWS(16, tc16) : FK_SR_ROWS(16, float); break;
+      case 32: st = bf ? FK_SR_ROWS(32, tc16) : FK_SR_ROWS(32, float); break;
+      default: st = bf ? FK_SR_ROWS(64, tc16) : FK_SR_ROWS(64, float);
+    }
+#undef FK_SR_ROWS
+  }
+  return st != FK_OK ? st : fk_sr_gram_mirror(gram, n, stream);
+}
+
+#ifndef FK_TC_FP16
+int64_t fk_ar2d_sr_gram_workspace_bytes(const fk_ar2d_desc* desc, int64_t batch) {
+  NetLayout L;
+  if (build_layout(desc, &L) != FK_OK || batch <= 0) return -1;
+  return sr_gram_ws(L, batch, nullptr, nullptr, nullptr, nullptr);
+}
+
+int64_t fk_ar2d_sr_gram_min_rows(const fk_ar2d_desc* desc, int64_t batch) {
+  NetLayout L;
+  if (build_layout(desc, &L) != FK_OK || batch <= 0) return -1;
+  return sink_min_rows(L) * 2 * batch;
+}
+#endif
 
 }  // extern "C"

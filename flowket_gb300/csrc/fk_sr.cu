@@ -621,54 +621,45 @@ int64_t fk_sr_gram_workspace_bytes(int64_t n_params, int64_t n_samples) {
   return 0;
 }
 
-int fk_sr_gram(const float* o_re, const float* o_im, int64_t n_params, int64_t n_samples, double* gram,
-               int64_t gram_elems, void* stream) {
-  FK_CHECK_ARG(o_re && gram && n_params > 0 && n_samples > 0, "fk_sr_gram: bad arguments");
-  int64_t n = o_im ? 2 * n_samples : n_samples;
-  FK_CHECK_ARG(gram_elems >= n * n, "fk_sr_gram: gram buffer too small (%lld < %lld)", (long long)gram_elems,
-               (long long)(n * n));
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  FK_CUDA(cudaMemsetAsync(gram, 0, (size_t)(n * n) * sizeof(double), s));
+}  // extern "C"
+
+// Adds the upper triangle (j >= i) of Y^T Y into gram (CUDA cores), Y =
+// [a | b] (b == a when n == bsz), P parameter rows.
+static int gram_cc_add(const float* a, const float* b, int64_t P, int64_t bsz, int64_t n, double* gram,
+                       cudaStream_t s) {
   int64_t ntile = (n + kGT - 1) / kGT;
   int64_t tiles = ntile * (ntile + 1) / 2;
   // enough K splits to fill the GPU ~4 times over
   int64_t splits = (4 * 152 + tiles - 1) / tiles;
-  int64_t kmax = (n_params + kGK - 1) / kGK;
+  int64_t kmax = (P + kGK - 1) / kGK;
   if (splits > kmax) splits = kmax;
   if (splits < 1) splits = 1;
-  int64_t kper = (n_params + splits - 1) / splits;
+  int64_t kper = (P + splits - 1) / splits;
   kper = (kper + kGK - 1) / kGK * kGK;
   dim3 grid((unsigned)tiles, 1, (unsigned)splits);
-  gram_kernel<<<grid, 256, 0, s>>>(o_re, o_im ? o_im : o_re, n_params, n_samples, n, kper, gram);
-  FK_CUDA(launched());
-  mirror_kernel<<<(unsigned)((n * n + 255) / 256), 256, 0, s>>>(gram, n);
-  FK_CUDA(launched());
-  return FK_OK;
+  gram_kernel<<<grid, 256, 0, s>>>(a, b, P, bsz, n, kper, gram);
+  return check_cuda(launched(), "gram_kernel");
 }
 
-int fk_sr_gram_tc(const float* o_re, const float* o_im, int64_t n_params, int64_t n_samples, double* gram,
-                  int64_t gram_elems, void* stream) {
-  FK_CHECK_ARG(o_re && gram && n_params > 0 && n_samples > 0, "fk_sr_gram_tc: bad arguments");
-  FK_CHECK_ARG(n_samples % 8 == 0, "fk_sr_gram_tc: n_samples must be a multiple of 8 (got %lld)",
-               (long long)n_samples);
-  FK_CHECK_ARG(((uintptr_t)o_re % 16) == 0 && (!o_im || ((uintptr_t)o_im % 16) == 0),
-               "fk_sr_gram_tc: o_re / o_im must be 16-byte aligned");
-  const int64_t n = o_im ? 2 * n_samples : n_samples;
-  FK_CHECK_ARG(n <= 65536, "fk_sr_gram_tc: n = %lld exceeds 65536", (long long)n);
-  FK_CHECK_ARG(gram_elems >= n * n, "fk_sr_gram_tc: gram buffer too small (%lld < %lld)", (long long)gram_elems,
-               (long long)(n * n));
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  static bool attr = false;
-  if (!attr) {
-    FK_CUDA(cudaFuncSetAttribute(gram_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, gram_tc::kSmem));
-    attr = true;
-  }
-  FK_CUDA(cudaMemsetAsync(gram, 0, (size_t)(n * n) * sizeof(double), s));
+static int mirror(double* gram, int64_t n, cudaStream_t s) {
+  mirror_kernel<<<(unsigned)((n * n + 255) / 256), 256, 0, s>>>(gram, n);
+  return check_cuda(launched(), "mirror_kernel");
+}
+
+// The same on the tensor cores (n a multiple of 8, a and b 16-byte aligned).
+static int gram_tc_add(const float* a_re, const float* a_im, int64_t n_params, int64_t bsz, int64_t n, double* gram,
+                       cudaStream_t s) {
+  static std::once_flag attr_once;
+  static cudaError_t attr_err = cudaSuccess;
+  std::call_once(attr_once, [] {
+    attr_err = cudaFuncSetAttribute(gram_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, gram_tc::kSmem);
+  });
+  FK_CUDA(attr_err);
   GramTcArgs a;
-  a.a = o_re;
-  a.b = o_im ? o_im : o_re;
+  a.a = a_re;
+  a.b = a_im;
   a.P = n_params;
-  a.bsz = n_samples;
+  a.bsz = bsz;
   a.n = n;
   a.nti = (n + gram_tc::kM - 1) / gram_tc::kM;
   a.ntj = (n + gram_tc::kN - 1) / gram_tc::kN;
@@ -689,10 +680,56 @@ int fk_sr_gram_tc(const float* o_re, const float* o_im, int64_t n_params, int64_
   a.err = device_error_word();
   const int64_t grid = a.items < 152 ? a.items : 152;
   gram_tc_kernel<<<(unsigned)grid, gram_tc::kThreads, gram_tc::kSmem, s>>>(a);
-  FK_CUDA(launched());
-  mirror_kernel<<<(unsigned)((n * n + 255) / 256), 256, 0, s>>>(gram, n);
-  FK_CUDA(launched());
-  return FK_OK;
+  return check_cuda(launched(), "gram_tc_kernel");
+}
+
+extern "C" {
+
+int fk_sr_gram(const float* o_re, const float* o_im, int64_t n_params, int64_t n_samples, double* gram,
+               int64_t gram_elems, void* stream) {
+  FK_CHECK_ARG(o_re && gram && n_params > 0 && n_samples > 0, "fk_sr_gram: bad arguments");
+  int64_t n = o_im ? 2 * n_samples : n_samples;
+  FK_CHECK_ARG(gram_elems >= n * n, "fk_sr_gram: gram buffer too small (%lld < %lld)", (long long)gram_elems,
+               (long long)(n * n));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  FK_CUDA(cudaMemsetAsync(gram, 0, (size_t)(n * n) * sizeof(double), s));
+  int st = gram_cc_add(o_re, o_im ? o_im : o_re, n_params, n_samples, n, gram, s);
+  return st != FK_OK ? st : mirror(gram, n, s);
+}
+
+int fk_sr_gram_tc(const float* o_re, const float* o_im, int64_t n_params, int64_t n_samples, double* gram,
+                  int64_t gram_elems, void* stream) {
+  FK_CHECK_ARG(o_re && gram && n_params > 0 && n_samples > 0, "fk_sr_gram_tc: bad arguments");
+  FK_CHECK_ARG(n_samples % 8 == 0, "fk_sr_gram_tc: n_samples must be a multiple of 8 (got %lld)",
+               (long long)n_samples);
+  FK_CHECK_ARG(((uintptr_t)o_re % 16) == 0 && (!o_im || ((uintptr_t)o_im % 16) == 0),
+               "fk_sr_gram_tc: o_re / o_im must be 16-byte aligned");
+  const int64_t n = o_im ? 2 * n_samples : n_samples;
+  FK_CHECK_ARG(n <= 65536, "fk_sr_gram_tc: n = %lld exceeds 65536", (long long)n);
+  FK_CHECK_ARG(gram_elems >= n * n, "fk_sr_gram_tc: gram buffer too small (%lld < %lld)", (long long)gram_elems,
+               (long long)(n * n));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  FK_CUDA(cudaMemsetAsync(gram, 0, (size_t)(n * n) * sizeof(double), s));
+  int st = gram_tc_add(o_re, o_im ? o_im : o_re, n_params, n_samples, n, gram, s);
+  return st != FK_OK ? st : mirror(gram, n, s);
+}
+
+int fk_sr_gram_accumulate(const float* y, int64_t rows, int64_t n, double* gram, int32_t tensor_cores,
+                          void* stream) {
+  FK_CHECK_ARG(y && gram && rows >= 0 && n > 0, "fk_sr_gram_accumulate: bad arguments");
+  if (rows == 0) return FK_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!tensor_cores) return gram_cc_add(y, y, rows, n, n, gram, s);
+  FK_CHECK_ARG(n % 8 == 0 && ((uintptr_t)y % 16) == 0 && n <= 65536,
+               "fk_sr_gram_accumulate: the tensor cores need n a multiple of 8 and <= 65536 (got %lld) and y "
+               "16-byte aligned",
+               (long long)n);
+  return gram_tc_add(y, y, rows, n, n, gram, s);
+}
+
+int fk_sr_gram_mirror(double* gram, int64_t n, void* stream) {
+  FK_CHECK_ARG(gram && n > 0, "fk_sr_gram_mirror: bad arguments");
+  return mirror(gram, n, static_cast<cudaStream_t>(stream));
 }
 
 int64_t fk_sr_solve_workspace_bytes(int64_t n) { return (3 * n + 8) * (int64_t)sizeof(double); }

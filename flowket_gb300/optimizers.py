@@ -5,7 +5,7 @@ flat parameter vector on the GPU.
   epsilon = K.epsilon() = 1e-7), the optimiser of experiments/train.py:52
   and the examples.
 * ``ComplexValuesStochasticReconfiguration``: optimizers/stochastic_reconfiguration/optimizer.py:14-183,
-  solved in sample space (see flowket_gb300.sr).
+  solved in sample space on the GPU.
 """
 import torch
 
@@ -60,14 +60,32 @@ class ComplexValuesStochasticReconfiguration:
     FP32-level accuracy, fk_sr_gram_tc), "fp32" on the CUDA cores
     (fk_sr_gram); "auto" takes the tensor cores for a machine on the
     tensor-core path (BF16/FP16) when the batch is a multiple of 8, the CUDA
-    cores otherwise (the plain FP32 path stays on CUDA cores throughout)."""
+    cores otherwise (the plain FP32 path stays on CUDA cores throughout).
+
+    ``rows_bytes``: for the AR network, the per-sample rows Y (num_params x
+    2B float32) are stored whole when they take at most
+    ``STORED_ROWS_LIMIT`` bytes; otherwise (or whenever ``rows_bytes`` is
+    given) they are streamed: fk_ar2d_sr_gram builds the Gram conv by conv
+    through a row buffer of ``rows_bytes`` (default ``STREAM_BUFFER_BYTES``)
+    from the two per-sample adjoints (seeds (1, 0) and (0, 1)) run together
+    over the step's activations, and the update x = Y alpha / B is the summed
+    adjoint with the centred seeds (alpha_b - mean, alpha_{B+b} - mean) / B,
+    so that Y is never held: the memory on top of the step's is two adjoint
+    workspaces, the buffer and the Gram."""
+
+    STORED_ROWS_LIMIT = 32 << 30
+    STREAM_BUFFER_BYTES = 16 << 30
 
     def __init__(self, machine, predictions_jacobian=None, lr=0.01, diag_shift=0.05, iterative_solver=True,
                  compute_jvp_instead_of_full_jacobian=False, use_cholesky=True, conjugate_gradient_tol=1e-3,
-                 iterative_solver_max_iterations=200, gram="auto", **kwargs):
+                 iterative_solver_max_iterations=200, gram="auto", rows_bytes=None, **kwargs):
         if gram not in ("auto", "tc", "fp32"):
             raise ValueError("gram must be 'auto', 'tc' or 'fp32'")
+        if rows_bytes is not None and int(rows_bytes) <= 0:
+            raise ValueError("rows_bytes must be positive")
         self.gram = gram
+        self.rows_bytes = None if rows_bytes is None else int(rows_bytes)
+        self.streamed = False
         self.machine = machine
         self.lr = float(lr)
         self.diag_shift = float(diag_shift)
@@ -143,6 +161,10 @@ class ComplexValuesStochasticReconfiguration:
             self._complex_solve(spins, local, 0.0, None, x)
             return x
         b = spins.shape[0]
+        p = m.num_params
+        self.streamed = self.rows_bytes is not None or 2 * p * b * 4 > self.STORED_ROWS_LIMIT
+        if self.streamed:
+            return self._streamed_direction(spins, local, saved)
         ones = torch.zeros((b, 2), dtype=torch.float32, device=m.device)
         ones[:, 0] = 1
         o_re = m.backward(spins, ones, saved, per_sample=True)
@@ -165,6 +187,39 @@ class ComplexValuesStochasticReconfiguration:
         _lib.call("fk_sr_backmap", _lib.ptr(o_re), _lib.ptr(o_im), p, b, _lib.ptr(bf["alpha"]), 1.0 / b, 0.0, None,
                   _lib.ptr(x), st)
         return x
+
+    def _streamed_direction(self, spins, local, saved):
+        from .machines import ctypes_ref
+        m = self.machine
+        lib = _lib.load()
+        s = m._spins(spins)
+        b = s.shape[0]
+        n = 2 * b
+        st = _lib.stream_ptr()
+        if saved is None:
+            _, _, saved = m.forward(s, mode=_lib.FK_AR2D_SAVE)
+        ws = torch.empty(lib.fk_ar2d_sr_gram_workspace_bytes(ctypes_ref(m.desc), b), dtype=torch.uint8,
+                         device=m.device)
+        budget = self.rows_bytes if self.rows_bytes is not None else self.STREAM_BUFFER_BYTES
+        floats = min(budget // 4, m.num_params * n)
+        floats = max(floats, lib.fk_ar2d_sr_gram_min_rows(ctypes_ref(m.desc), b))
+        rows = torch.empty(floats, dtype=torch.float32, device=m.device)
+        bf = self._buffers(n, m.device)
+        tc = 1 if self._gram_entry(b) == "fk_sr_gram_tc" else 0
+        _lib.call("fk_ar2d_sr_gram", ctypes_ref(m.desc), _lib.ptr(m.packed()), _lib.ptr(m.params), _lib.ptr(s), b,
+                  _lib.ptr(saved), saved.numel(), _lib.ptr(ws), ws.numel(), _lib.ptr(rows), rows.numel(),
+                  _lib.ptr(bf["gram"]), tc, st)
+        del rows, ws
+        bf["rhs"][:b] = local[:, 0] - local[:, 0].mean()
+        bf["rhs"][b:] = local[:, 1] - local[:, 1].mean()
+        _lib.call("fk_sr_solve", _lib.ptr(bf["gram"]), n, 1.0 / b, self.diag_shift, _lib.ptr(bf["rhs"]), self.tol,
+                  self.max_iter, _lib.ptr(bf["alpha"]), _lib.ptr(bf["stats"]), _lib.ptr(bf["ws"]), bf["ws"].numel(),
+                  st)
+        # x = Y alpha / B = sum_b (alpha_b - mean) Re O_b + (alpha_{B+b} - mean) Im O_b, all / B: the
+        # summed adjoint with these seeds
+        a = bf["alpha"]
+        w = torch.stack([a[:b] - a[:b].mean(), a[b:] - a[b:].mean()], dim=1).div_(b).to(torch.float32).contiguous()
+        return m.backward(s, w, saved)
 
 
 class AccumulateGradientOptimizer:

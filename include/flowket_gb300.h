@@ -161,13 +161,32 @@ int fk_ar2d_forward_connections(const fk_ar2d_desc* desc, const void* packed, co
  * Re and Im log psi of each sample. grad [num_params] = d/dtheta sum_b
  * (w_re Re log psi_b + w_im Im log psi_b) (the Keras loss gradient of
  * optimization/loss.py:4-5; utils/jacobian.py:114-127 per example). When
- * per_sample != NULL it receives per_sample[b][num_params] instead of the sum.
+ * per_sample != NULL it receives the per-sample rows instead of the sum,
+ * parameter-major: per_sample[p * B + b].
  * `saved` is the FK_AR2D_SAVE workspace of the forward/sample that produced
  * the activations of these spins. */
 int64_t fk_ar2d_backward_workspace_bytes(const fk_ar2d_desc* desc, int64_t batch);
 int fk_ar2d_backward(const fk_ar2d_desc* desc, const void* packed, const float* params, const int8_t* spins,
                      int64_t batch, const float* w, const void* saved, int64_t saved_bytes, void* workspace,
                      int64_t workspace_bytes, float* grad, float* per_sample, void* stream);
+/* The SR Gram of the per-sample rows without storing them (the S matrix of
+ * optimizers/stochastic_reconfiguration/optimizer.py:94-114 in sample space,
+ * for networks whose [num_params][B] rows do not fit in memory): gram
+ * [2B][2B] = Y^T Y with Y = [Re O_c | Im O_c] (num_params x 2B, each half
+ * centred over its samples), the matrix fk_sr_gram builds from the stored
+ * rows of fk_ar2d_backward with seeds (1, 0) and (0, 1). Both per-sample
+ * adjoints run together over the one set of activations in `saved`; each
+ * conv's rows go, as they are produced, to a row buffer of rows_floats
+ * floats (at least fk_ar2d_sr_gram_min_rows); when the next step's convs do
+ * not fit, and at the end, the buffered rows get the weight-norm chain rule,
+ * are centred (fk_center_columns) and Y^T Y of the buffer is added into gram
+ * (fk_sr_gram_accumulate; tensor_cores selects the split-BF16 tensor-core
+ * Gram, which needs B a multiple of 4). */
+int64_t fk_ar2d_sr_gram_workspace_bytes(const fk_ar2d_desc* desc, int64_t batch);
+int64_t fk_ar2d_sr_gram_min_rows(const fk_ar2d_desc* desc, int64_t batch);
+int fk_ar2d_sr_gram(const fk_ar2d_desc* desc, const void* packed, const float* params, const int8_t* spins,
+                    int64_t batch, const void* saved, int64_t saved_bytes, void* workspace, int64_t workspace_bytes,
+                    float* rows, int64_t rows_floats, double* gram, int32_t tensor_cores, void* stream);
 
 /* ------------------------------------------------------------------ optimisers */
 /* tf.keras Adam (TF 1.x): lr_t = lr sqrt(1-b2^t)/(1-b1^t), epsilon 1e-7.
@@ -266,6 +285,15 @@ int fk_sr_gram(const float* o_re, const float* o_im, int64_t n_params, int64_t n
  * multiple of 8, o_re / o_im 16-byte aligned, n <= 65536. */
 int fk_sr_gram_tc(const float* o_re, const float* o_im, int64_t n_params, int64_t n_samples, double* gram,
                   int64_t gram_elems, void* stream);
+/* Adds the upper triangle (j >= i) of Y^T Y into gram (n x n float64), Y
+ * [rows][n] float32 row-major: the Gram of a block of parameter rows, for
+ * Grams accumulated block by block (fk_sr_gram's arithmetic with
+ * tensor_cores = 0, fk_sr_gram_tc's with 1, which needs n a multiple of 8 and
+ * y 16-byte aligned). The lower triangle is left as it is. */
+int fk_sr_gram_accumulate(const float* y, int64_t rows, int64_t n, double* gram, int32_t tensor_cores,
+                          void* stream);
+/* Copies the upper triangle of gram (n x n) into the lower one. */
+int fk_sr_gram_mirror(double* gram, int64_t n, void* stream);
 /* FP64 conjugate gradients on (scale * gram + shift I) x = rhs, stopping at
  * ||r|| <= tol ||rhs|| or max_iter (linear_equations.py:34-137); stats (device,
  * optional) = {iterations, ||r||^2, tol^2 ||rhs||^2}. No host synchronisation. */

@@ -112,3 +112,123 @@ def test_vmc_with_sr_lowers_energy(cuda):
         vmc.step(opt)
         energies.append(vmc.current_energy.real)
     assert np.mean(energies[-5:]) < np.mean(energies[:3]) - 1.0
+
+
+@pytest.mark.parametrize("tensor_cores", [0, 1])
+def test_gram_accumulated_by_row_blocks(cuda, tensor_cores):
+    """fk_sr_gram_accumulate over row blocks of Y, then fk_sr_gram_mirror,
+    against the FP64 Gram of the same rows: the block-by-block Gram of the
+    streamed SR path (same bounds as the whole-array kernels)."""
+    from flowket_gb300 import _lib
+    rng = np.random.default_rng(11)
+    p, n = 9000, 264
+    y = rng.normal(size=(p, n)).astype(np.float32)
+    ty = torch.as_tensor(y).cuda()
+    gram = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+    for r0, r1 in ((0, 1000), (1000, 1008), (1008, 6100), (6100, p)):
+        _lib.call("fk_sr_gram_accumulate", _lib.ptr(ty[r0:]), r1 - r0, n, _lib.ptr(gram), tensor_cores,
+                  _lib.stream_ptr())
+    _lib.call("fk_sr_gram_mirror", _lib.ptr(gram), n, _lib.stream_ptr())
+    want = y.astype(np.float64).T @ y.astype(np.float64)
+    err = np.abs(gram.cpu().numpy() - want) / np.sqrt(np.outer(np.diag(want), np.diag(want)))
+    assert err.max() < (5e-5 if tensor_cores else 1e-5), err.max()
+    assert err[~np.eye(n, dtype=bool)].max() < 2e-6
+
+
+# (shape, depth, channels, weight norm, precision): CUDA-core adjoint (F = 16,
+# FP32), the tensor-core adjoint's per-sample rows (F = 32, BF16 and FP16)
+STREAMED_NETS = [((4, 4), 3, 16, True, "fp32"), ((6, 6), 3, 32, True, "bf16"), ((5, 6), 2, 32, True, "fp16"),
+                 ((4, 4), 2, 16, False, "bf16")]
+
+
+def _stored_rows(m, s, saved):
+    """Y = [Re O_c | Im O_c] (num_params x 2B) from the stored per-sample rows."""
+    b = s.shape[0]
+    ones = torch.zeros((b, 2), dtype=torch.float32, device="cuda")
+    ones[:, 0] = 1
+    o_re = m.backward(s, ones, saved, per_sample=True).double()
+    ones[:, 0], ones[:, 1] = 0, 1
+    o_im = m.backward(s, ones, saved, per_sample=True).double()
+    y = torch.cat([o_re - o_re.mean(1, keepdim=True), o_im - o_im.mean(1, keepdim=True)], dim=1)
+    return y.cpu().numpy()
+
+
+@pytest.mark.parametrize("tensor_cores", [0, 1])
+@pytest.mark.parametrize("net", range(len(STREAMED_NETS)))
+def test_streamed_sr_gram_equals_gram_of_stored_rows(cuda, net, tensor_cores):
+    """fk_ar2d_sr_gram (both per-sample adjoints over one set of activations,
+    rows streamed conv by conv through the smallest row buffer allowed: a
+    flush at almost every step, weight-norm chain rule and centring per
+    buffer) against the FP64 Gram of the stored, centred per-sample rows of
+    fk_ar2d_backward: the streamed rows are the same numbers, so the bounds
+    are the Gram kernels' own."""
+    from flowket_gb300 import _lib
+    from flowket_gb300.machines import ConvNetAutoregressive2D, ctypes_ref
+    shape, depth, f, wn, prec = STREAMED_NETS[net]
+    m = ConvNetAutoregressive2D(shape, depth, f, weights_normalization=wn, precision=prec, seed=3 + net)
+    b = 64
+    s = m._spins(torch.as_tensor(np.random.default_rng(net).choice([-1, 1], size=(b,) + shape).astype(np.int8)))
+    _, _, saved = m.forward(s, mode=_lib.FK_AR2D_SAVE)
+    y = _stored_rows(m, s, saved)
+    want = y.T @ y
+    n = 2 * b
+    lib = _lib.load()
+    d = ctypes_ref(m.desc)
+    ws = torch.empty(lib.fk_ar2d_sr_gram_workspace_bytes(d, b), dtype=torch.uint8, device="cuda")
+    min_rows = lib.fk_ar2d_sr_gram_min_rows(d, b)
+    rows = torch.empty(min_rows + 7, dtype=torch.float32, device="cuda")
+    gram = torch.full((n, n), float("nan"), dtype=torch.float64, device="cuda")
+    _lib.call("fk_ar2d_sr_gram", d, _lib.ptr(m.packed()), _lib.ptr(m.params), _lib.ptr(s), b, _lib.ptr(saved),
+              saved.numel(), _lib.ptr(ws), ws.numel(), _lib.ptr(rows), rows.numel(), _lib.ptr(gram), tensor_cores,
+              _lib.stream_ptr())
+    got = gram.cpu().numpy()
+    np.testing.assert_array_equal(got, got.T)
+    err = np.abs(got - want) / np.sqrt(np.outer(np.diag(want), np.diag(want)))
+    assert err.max() < (5e-5 if tensor_cores else 1e-5), err.max()
+    # off the diagonal the split-BF16 products (lo*lo dropped, lo rounded:
+    # <= 3 * 2^-18 of sum |y_pi y_pj| <= sqrt(T_ii T_jj)) reach 5.7e-6 on
+    # these rows, whose entries share signs (2e-7 on random rows)
+    assert err[~np.eye(n, dtype=bool)].max() < (1.5e-5 if tensor_cores else 2e-6)
+    # a buffer below the minimum, or a short workspace, is an argument error
+    args = [d, _lib.ptr(m.packed()), _lib.ptr(m.params), _lib.ptr(s), b, _lib.ptr(saved), saved.numel(),
+            _lib.ptr(ws), ws.numel(), _lib.ptr(rows), min_rows - 1, _lib.ptr(gram), tensor_cores, _lib.stream_ptr()]
+    assert lib.fk_ar2d_sr_gram(*args) == -1 and b"row buffer" in lib.fk_last_error()
+    args[10], args[8] = min_rows, ws.numel() - 1
+    assert lib.fk_ar2d_sr_gram(*args) == -1 and b"workspace" in lib.fk_last_error()
+
+
+# ||x_streamed - x_stored|| / ||x_stored||, 3x the worst of 5 seeds per
+# network (6.2e-6, 8.0e-3, 1.0e-3, 6.5e-6): the CUDA-core adjoints keep FP32
+# gradient tensors (rounding only); on the tensor-core adjoint (F = 32, BF16
+# and FP16) the update's seeds pass through its 16-bit gradient tensors
+STREAMED_X = [2e-5, 2.5e-2, 3e-3, 2e-5]
+
+
+@pytest.mark.parametrize("with_saved", [True, False])
+@pytest.mark.parametrize("net", range(len(STREAMED_NETS)))
+def test_streamed_sr_direction_equals_stored(cuda, net, with_saved):
+    """ComplexValuesStochasticReconfiguration with ``rows_bytes`` (the
+    streamed route: Gram through fk_ar2d_sr_gram, update as the summed
+    adjoint with the centred solution as seeds) against the stored route on
+    the same samples and local energies."""
+    from flowket_gb300 import _lib
+    from flowket_gb300.machines import ConvNetAutoregressive2D
+    from flowket_gb300.observables import Observable
+    from flowket_gb300.operators import Heisenberg
+    from flowket_gb300.optimizers import ComplexValuesStochasticReconfiguration
+    shape, depth, f, wn, prec = STREAMED_NETS[net]
+    m = ConvNetAutoregressive2D(shape, depth, f, weights_normalization=wn, precision=prec, seed=7 + net)
+    b = 128
+    s = m._spins(torch.as_tensor(np.random.default_rng(20 + net).choice([-1, 1], size=(b,) + shape)
+                                 .astype(np.int8)))
+    _, _, saved = m.forward(s, mode=_lib.FK_AR2D_SAVE)
+    local = Observable(Heisenberg(hilbert_state_shape=shape, pbc=True)).local_values(m, s)
+    ref = ComplexValuesStochasticReconfiguration(m, lr=0.05, diag_shift=1e-2, iterative_solver=False)
+    x_ref = ref.direction(s, local, saved).double()
+    assert not ref.streamed
+    opt = ComplexValuesStochasticReconfiguration(m, lr=0.05, diag_shift=1e-2, iterative_solver=False,
+                                                 rows_bytes=4)  # the smallest buffer allowed
+    x = opt.direction(s, local, saved if with_saved else None).double()
+    assert opt.streamed
+    rel = (torch.linalg.norm(x - x_ref) / torch.linalg.norm(x_ref)).item()
+    assert rel < STREAMED_X[net], rel
