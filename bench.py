@@ -63,13 +63,15 @@ def parse():
                    help="samples of one VMC step per timed CPU step (reference arm and cpu_baseline)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--case", default="vmc", choices=["vmc", "forward", "energy4x4", "vmc16", "ising12", "matched",
-                                                     "j1j2sr", "chain64", "kernels"],
+                                                     "j1j2sr", "chain64", "kernels", "sampler"],
                    help="forward: only the batched AR2D forward of the local-energy stage on --configs "
                         "connected configurations (the small case used for ncu captures); energy4x4: train "
                         "the 4x4 Heisenberg model (depth 5, 16 channels) and compare its exact energy "
                         "(enumeration of all 2^16 states) with Lanczos, in --precision")
     p.add_argument("--precision", default="bf16", choices=["bf16", "fp16", "fp32"])
     p.add_argument("--sr-steps", type=int, default=20)
+    p.add_argument("--sr-rows-bytes", type=int, default=None,
+                   help="j1j2sr: stream the per-sample rows into the SR Gram through a buffer of this many bytes")
     p.add_argument("--sr-leg-steps", type=int, default=3,
                    help="timed steps per precision of the bench line's J1-J2 SR leg (0: skip)")
     p.add_argument("--precisions", nargs="+", default=None, choices=["bf16", "fp16", "fp32"])
@@ -139,7 +141,7 @@ def vmc16_case(args):
                                         "(weight norm); full VMC step with " +
                                         ("SR (diag shift 1e-3, lr 0.05, streamed Gram)" if sr else "Adam"),
            "batch": args.batch}
-    for prec in ("bf16", "fp32"):
+    for prec in args.precisions or ["bf16", "fp32"]:
         m = ConvNetAutoregressive2D(shape, 20, 64, weights_normalization=True, precision=prec, seed=0)
         vmc = VariationalMonteCarlo(m, Heisenberg(hilbert_state_shape=shape, pbc=True),
                                     FastAutoregressiveSampler(m, args.batch, seed=1234))
@@ -168,7 +170,8 @@ def vmc16_case(args):
                               "per_sample_rows_gb_if_stored": 2 * m.num_params * args.batch * 4 / 1e9})
         del vmc, opt, m
         torch.cuda.empty_cache()
-    out["bf16_over_fp32"] = out["fp32"]["ms_per_step"] / out["bf16"]["ms_per_step"]
+    if "bf16" in out and "fp32" in out:
+        out["bf16_over_fp32"] = out["fp32"]["ms_per_step"] / out["bf16"]["ms_per_step"]
     print(json.dumps(out), flush=True)
 
 
@@ -238,7 +241,7 @@ def matched_case(args):
     print(json.dumps(out), flush=True)
 
 
-def j1j2sr_summary(steps, precisions):
+def j1j2sr_summary(steps, precisions, rows_bytes=None):
     """J1-J2 10x10 periodic, J2/J1 = 0.5 (operators/j1j2.py edge list);
     ConvNetAutoregressive2D depth 20, 32 channels (weight norm), Re and Im
     heads; 1024 exact samples per step; stochastic reconfiguration
@@ -247,7 +250,8 @@ def j1j2sr_summary(steps, precisions):
     (sampling, local energy over the used connections, per-sample
     log-derivatives, Gram, solve, update) on each precision from the same
     seeded parameters after one untimed step: ms per step, stage split,
-    energy and variance per step."""
+    energy and variance per step. With `rows_bytes` the per-sample rows are
+    streamed into the Gram through a buffer of that size instead of stored."""
     from flowket_gb300.machines import ConvNetAutoregressive2D
     from flowket_gb300.operators import J1J2
     from flowket_gb300.optimization import VariationalMonteCarlo
@@ -260,7 +264,7 @@ def j1j2sr_summary(steps, precisions):
     for prec in precisions:
         m = ConvNetAutoregressive2D(shape, 20, 32, weights_normalization=True, precision=prec, seed=0)
         vmc = VariationalMonteCarlo(m, op, FastAutoregressiveSampler(m, b, seed=1234))
-        opt = ComplexValuesStochasticReconfiguration(m, lr=0.05, diag_shift=1e-3)
+        opt = ComplexValuesStochasticReconfiguration(m, lr=0.05, diag_shift=1e-3, rows_bytes=rows_bytes)
         vmc.step(opt)
         energies, variances, ms, stages = [], [], [], []
         for _ in range(steps):
@@ -278,7 +282,7 @@ def j1j2sr_summary(steps, precisions):
                      "stage_ms": {k: float(np.mean([st[k] for st in stages])) for k in stages[0]},
                      "energy_first": energies[0], "energy_last": energies[-1], "energies": energies,
                      "variance_last": variances[-1], "cg_iterations_last": float(opt.last_stats[0].item()),
-                     "num_params": m.num_params}
+                     "num_params": m.num_params, "rows_streamed": opt.streamed}
         del m, vmc, opt
         torch.cuda.empty_cache()
     for prec in ("bf16", "fp16"):
@@ -289,7 +293,7 @@ def j1j2sr_summary(steps, precisions):
 
 def j1j2sr_case(args):
     out = {"case": "j1j2sr"}
-    out.update(j1j2sr_summary(args.sr_steps, args.precisions or ["bf16", "fp16", "fp32"]))
+    out.update(j1j2sr_summary(args.sr_steps, args.precisions or ["bf16", "fp16", "fp32"], args.sr_rows_bytes))
     print(json.dumps(out), flush=True)
 
 
@@ -346,6 +350,40 @@ def chain64_case(args):
     d = abs(out["plain"]["energy"] - out["learned"]["energy"])
     out["energy_difference_in_sigma"] = d / math.hypot(out["plain"]["stderr_iat"], out["learned"]["stderr_iat"])
     out["tau_ratio_learned_over_plain"] = out["learned"]["tau_int"] / out["plain"]["tau_int"]
+    print(json.dumps(out), flush=True)
+
+
+def sampler_case(args):
+    """The exact sampler of the bench network (10x10, depth 10, 32 channels,
+    weight norm) at batch sizes from 1,024 to 19,456 samples (one persistent
+    CTA per 128 samples: 8 to 152 CTAs on the 152 SMs), and of the 16x16
+    depth-20 F64 network at 8,192: CUDA-event time per draw (best of
+    `--steps` after `--warmup`) in BF16, FP16 and FP32. A draw's time that
+    does not grow with the CTA count while CTAs < SMs is set by the length of
+    one CTA's chain of dependent site ops, not by how many SMs work."""
+    from flowket_gb300.machines import ConvNetAutoregressive2D
+    from flowket_gb300.samplers import FastAutoregressiveSampler
+    out = {"case": "sampler", "network": "10x10 depth 10 F32 (weight norm)", "ms_per_draw": {}}
+
+    def time_draw(m, b):
+        smp = FastAutoregressiveSampler(m, b, seed=5)
+        for _ in range(max(1, args.warmup)):
+            smp.sample()
+        best = float("inf")
+        for _ in range(max(1, args.steps)):
+            a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            smp.sample()
+            e.record()
+            torch.cuda.synchronize()
+            best = min(best, a.elapsed_time(e))
+        return best
+
+    for prec in ("bf16", "fp16", "fp32"):
+        m = ConvNetAutoregressive2D((10, 10), 10, 32, weights_normalization=True, precision=prec, seed=0)
+        out["ms_per_draw"][prec] = {str(b): time_draw(m, b) for b in (1024, 2048, 4096, 8192, 16384, 19456)}
+    m = ConvNetAutoregressive2D((16, 16), 20, 64, weights_normalization=True, precision="bf16", seed=0)
+    out["ms_per_draw_16x16_d20_f64_bf16"] = {"8192": time_draw(m, 8192)}
     print(json.dumps(out), flush=True)
 
 
@@ -453,6 +491,17 @@ def kernels_case(args):
     record("sr_gram_tc", ms, flops=float(n) * (n + 1) * p, peak=peaks.get("bf16_tflops"),
            unit="TFLOP/s (bf16 burst, measured; each product costs three bf16 MMAs)", nbytes=2 * p * bs * 4,
            params=p, samples=bs)
+    sbytes = _lib.load().fk_sr_gram_split_bytes(p, n)
+    split = torch.empty(sbytes, dtype=torch.uint8, device="cuda")
+    ms = timed(lambda: _lib.call("fk_sr_gram_split", _lib.ptr(o_re), _lib.ptr(o_im), bs, bs, p, n, _lib.ptr(split),
+                                 sbytes, st))
+    record("sr_gram_split", ms, nbytes=2 * p * bs * 4 + sbytes, params=p, samples=bs,
+           note="read the FP32 rows once, write bf16 hi + lo in the blocked operand layout")
+    ms = timed(lambda: _lib.call("fk_sr_gram_split_accumulate", _lib.ptr(split), p, n, _lib.ptr(gram), st))
+    record("sr_gram_split_accumulate", ms, flops=float(n) * (n + 1) * p, peak=peaks.get("bf16_tflops"),
+           unit="TFLOP/s (bf16 burst, measured; each product costs three bf16 MMAs)", nbytes=sbytes, params=p,
+           samples=bs)
+    del split
     rhs = torch.randn(n, device="cuda", dtype=torch.float64, generator=g)
     alpha = torch.empty(n, device="cuda", dtype=torch.float64)
     stats = torch.zeros(3, device="cuda", dtype=torch.float64)
@@ -974,6 +1023,8 @@ def main():
         chain64_case(args)
     elif args.case == "kernels":
         kernels_case(args)
+    elif args.case == "sampler":
+        sampler_case(args)
     elif args.impl == "reference":
         reference_arm(args, rank, world)
     else:

@@ -57,7 +57,7 @@ _SIGNATURES = {
     "fk_ar2d_backward_workspace_bytes": (c_i64, [c_p, c_i64]),
     "fk_ar2d_backward": (c_i32, [c_p, c_p, c_p, c_p, c_i64, c_p, c_p, c_i64, c_p, c_i64, c_p, c_p, c_p]),
     "fk_ar2d_sr_gram_workspace_bytes": (c_i64, [c_p, c_i64]),
-    "fk_ar2d_sr_gram_min_rows": (c_i64, [c_p, c_i64]),
+    "fk_ar2d_sr_gram_min_rows": (c_i64, [c_p, c_i64, c_i32]),
     "fk_ar2d_sr_gram": (c_i32, [c_p, c_p, c_p, c_p, c_i64, c_p, c_i64, c_p, c_i64, c_p, c_i64, c_p, c_i32, c_p]),
     "fk_axpy": (c_i32, [c_i64, c_f32, c_p, c_p, c_p]),
     "fk_adam_step": (c_i32, [c_p, c_p, c_p, c_p, c_i64, c_i64, c_f32, c_f32, c_f32, c_f32, c_p]),
@@ -66,6 +66,9 @@ _SIGNATURES = {
     "fk_sr_gram_tc": (c_i32, [c_p, c_p, c_i64, c_i64, c_p, c_i64, c_p]),
     "fk_sr_gram_accumulate": (c_i32, [c_p, c_i64, c_i64, c_p, c_i32, c_p]),
     "fk_sr_gram_mirror": (c_i32, [c_p, c_i64, c_p]),
+    "fk_sr_gram_split_bytes": (c_i64, [c_i64, c_i64]),
+    "fk_sr_gram_split": (c_i32, [c_p, c_p, c_i64, c_i64, c_i64, c_i64, c_p, c_i64, c_p]),
+    "fk_sr_gram_split_accumulate": (c_i32, [c_p, c_i64, c_i64, c_p, c_p]),
     "fk_sr_solve_workspace_bytes": (c_i64, [c_i64]),
     "fk_sr_solve": (c_i32, [c_p, c_i64, c_f64, c_f64, c_p, c_f64, c_i32, c_p, c_p, c_p, c_i64, c_p]),
     "fk_sr_solve_noalloc": (c_i32, [c_p, c_i64, c_f64, c_f64, c_p, c_f64, c_i32, c_p, c_p, c_p]),

@@ -483,6 +483,8 @@ struct RowSink {
   int64_t col;   // first column of the pass being written
   int groups;    // passes
   int tensor_cores;
+  void* split;   // tensor cores: the buffer's rows as split operands (fk_sr_gram_split)
+  int64_t split_bytes;
   double* gram;
   int n;         // buffered convs
   int conv[kMaxConvs];
@@ -519,7 +521,12 @@ static int sink_flush(RowSink& k, cudaStream_t s) {
     if (nw > 0) FK_CUDA(launched());
   }
   int st = fk_center_columns(k.buf, k.used * k.groups, k.ld / k.groups, nullptr, s);
-  if (st == FK_OK) st = fk_sr_gram_accumulate(k.buf, k.used, k.ld, k.gram, k.tensor_cores, s);
+  if (st == FK_OK && k.tensor_cores) {
+    st = fk_sr_gram_split(k.buf, nullptr, k.ld, k.ld, k.used, k.ld, k.split, k.split_bytes, s);
+    if (st == FK_OK) st = fk_sr_gram_split_accumulate(k.split, k.used, k.ld, k.gram, s);
+  } else if (st == FK_OK) {
+    st = fk_sr_gram_accumulate(k.buf, k.used, k.ld, k.gram, 0, s);
+  }
   for (int i = 0; i < k.n; ++i) k.at[k.conv[i]] = -1;
   k.used = 0;
   k.n = 0;
@@ -556,6 +563,13 @@ static int sink_place(RowSink& k, int ci, int64_t* r0, cudaStream_t s) {
   }
   *r0 = k.at[ci];
   return FK_OK;
+}
+
+// Floats of a row buffer holding `rows` rows of n floats, and with the
+// tensor cores also their split operands (after the rows, 256-byte aligned).
+static int64_t sink_floats(int64_t rows, int64_t n, bool tc) {
+  const int64_t f = (rows * n + 63) / 64 * 64;
+  return tc ? f + fk_sr_gram_split_bytes(rows, n) / 4 : f;
 }
 
 // The convs whose per-sample rows step i of the backward writes (all five
@@ -1182,8 +1196,9 @@ int FK_AR2D_ENTRY(fk_ar2d_sr_gram)(const fk_ar2d_desc* desc, const void* packed,
   FK_CHECK_ARG(packed && params && spins && saved && rows && gram && workspace, "fk_ar2d_sr_gram: NULL buffer");
   FK_CHECK_ARG(batch > 0, "fk_ar2d_sr_gram: batch must be positive");
   const int64_t n = 2 * batch;
-  FK_CHECK_ARG(rows_floats / n >= sink_min_rows(L), "fk_ar2d_sr_gram: row buffer of %lld floats < %lld",
-               (long long)rows_floats, (long long)(sink_min_rows(L) * n));
+  const int64_t need_floats = sink_floats(sink_min_rows(L), n, tensor_cores != 0);
+  FK_CHECK_ARG(rows_floats >= need_floats, "fk_ar2d_sr_gram: row buffer of %lld floats < %lld",
+               (long long)rows_floats, (long long)need_floats);
   FK_CHECK_ARG(workspace_bytes >= sr_gram_ws(L, batch, nullptr, nullptr, nullptr, nullptr),
                "fk_ar2d_sr_gram: workspace %lld < %lld bytes", (long long)workspace_bytes,
                (long long)sr_gram_ws(L, batch, nullptr, nullptr, nullptr, nullptr));
@@ -1205,7 +1220,19 @@ int FK_AR2D_ENTRY(fk_ar2d_sr_gram)(const fk_ar2d_desc* desc, const void* packed,
   k.L = &L;
   k.params = params;
   k.buf = rows;
-  k.cap = rows_floats / n;
+  // the most rows whose floats (and split operands) fit in the buffer
+  int64_t lo = 0, hi = rows_floats / n;  // sink_floats(lo) fits; sink_floats grows with the rows
+  while (lo < hi) {
+    const int64_t mid = lo + (hi - lo + 1) / 2;
+    if (sink_floats(mid, n, tensor_cores != 0) <= rows_floats)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  const int64_t cap = lo;
+  k.cap = cap;
+  k.split = tensor_cores ? static_cast<void*>(rows + (cap * n + 63) / 64 * 64) : nullptr;
+  k.split_bytes = tensor_cores ? fk_sr_gram_split_bytes(cap, n) : 0;
   k.used = 0;
   k.ld = n;
   k.col = 0;
@@ -1243,10 +1270,10 @@ int64_t fk_ar2d_sr_gram_workspace_bytes(const fk_ar2d_desc* desc, int64_t batch)
   return sr_gram_ws(L, batch, nullptr, nullptr, nullptr, nullptr);
 }
 
-int64_t fk_ar2d_sr_gram_min_rows(const fk_ar2d_desc* desc, int64_t batch) {
+int64_t fk_ar2d_sr_gram_min_rows(const fk_ar2d_desc* desc, int64_t batch, int32_t tensor_cores) {
   NetLayout L;
   if (build_layout(desc, &L) != FK_OK || batch <= 0) return -1;
-  return sink_min_rows(L) * 2 * batch;
+  return sink_floats(sink_min_rows(L), 2 * batch, tensor_cores != 0);
 }
 #endif
 

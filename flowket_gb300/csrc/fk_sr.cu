@@ -379,6 +379,248 @@ __global__ void __launch_bounds__(gram_tc::kThreads, 1) gram_tc_kernel(const __g
   }
 }
 
+// ---------------------------------------------------------------- pre-split Gram on tensor cores
+// The tensor-core Gram's split operands written once (split_kernel): every
+// float32 value of Y (rows x n) as bf16 hi = bf16(y) and lo = bf16(y - hi)
+// in a blocked layout in which each operand of a pipeline stage is one
+// contiguous run, so that gram_split_kernel streams them with bulk copies
+// instead of converting every value again for each tile that reads it
+// (n / 128 + n / 256 times). Block (kc, g) holds rows [32 kc, 32 kc + 32) x
+// columns [8 g, 8 g + 8), one row per 16 bytes (a row of an MN-major core
+// matrix); blocks ordered by kc, then g; rows padded to a multiple of 32 and
+// columns to a multiple of 256 with zeros; lo follows hi.
+namespace gram_split {
+constexpr int kK = 32;                   // parameter rows per stage
+constexpr int kBlock = kK * 8 * 2;       // one (kc, g) block: 512 B
+constexpr int kStages = 4;
+constexpr int kA = (gram_tc::kM / 8) * kBlock;  // 128 samples: 8 KB (hi or lo)
+constexpr int kB = (gram_tc::kN / 8) * kBlock;  // 256 samples: 16 KB
+constexpr int kStage = 2 * kA + 2 * kB;         // 48 KB
+constexpr int kThreads = 32 * 8;                // producer, issuer, 2 idle, 4 drain warps
+constexpr int kSmem = kStages * kStage + 256;
+}  // namespace gram_split
+
+static int64_t split_rows_pad(int64_t rows) { return (rows + 31) / 32 * 32; }
+static int64_t split_cols_pad(int64_t n) { return (n + 255) / 256 * 256; }
+static int64_t split_bytes(int64_t rows, int64_t n) { return 2 * split_rows_pad(rows) * split_cols_pad(n) * 2; }
+
+// One thread per (row, group of 8 columns); the 32 threads of a warp write
+// the 32 rows of one block (512 contiguous bytes of hi and of lo). Column c
+// of Y comes from a[p * ld + c] when c < bsz, from b[p * ld + c - bsz] after.
+__global__ void split_kernel(const float* __restrict__ a, const float* __restrict__ b, int64_t ld, int64_t bsz,
+                             int64_t rows, int64_t n, int64_t groups, int64_t total, uint4* __restrict__ hi,
+                             uint4* __restrict__ lo) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= total) return;
+  const int64_t blk = idx / 32;
+  const int r = (int)(idx % 32);
+  const int64_t kc = blk / groups, g = blk % groups;
+  const int64_t p = kc * 32 + r;
+  float v[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const int64_t c = g * 8 + e;
+    v[e] = (p < rows && c < n) ? (c < bsz ? a[p * ld + c] : b[p * ld + (c - bsz)]) : 0.f;
+  }
+  float h[8], l[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    h[e] = __bfloat162float(__float2bfloat16_rn(v[e]));
+    l[e] = v[e] - h[e];
+  }
+  uint4 uh, ul;
+  uh.x = pack_bf16x2(h[0], h[1]); uh.y = pack_bf16x2(h[2], h[3]);
+  uh.z = pack_bf16x2(h[4], h[5]); uh.w = pack_bf16x2(h[6], h[7]);
+  ul.x = pack_bf16x2(l[0], l[1]); ul.y = pack_bf16x2(l[2], l[3]);
+  ul.z = pack_bf16x2(l[4], l[5]); ul.w = pack_bf16x2(l[6], l[7]);
+  hi[idx] = uh;
+  lo[idx] = ul;
+}
+
+struct GramSplitArgs {
+  const uint8_t* hi;
+  const uint8_t* lo;
+  int64_t groups;   // padded columns / 8
+  int64_t n;        // columns of Y (T is n x n)
+  int64_t kchunks;  // padded rows / 32
+  int64_t kper;     // chunks per range
+  int64_t splits;
+  int64_t nti, ntj;
+  int64_t items;
+  double* t;
+  int* err;
+};
+
+__device__ __forceinline__ void gram_split_item(const GramSplitArgs& g, int64_t item, int64_t& i0, int64_t& j0,
+                                                int64_t& c0, int64_t& c1) {
+  // range-major, as gram_item: the CTAs running together share a range
+  const int64_t tiles = g.items / g.splits;
+  const int64_t split = item / tiles, tile = item % tiles;
+  int64_t ti = 0, rem = tile;
+  while (ti < g.nti && rem >= g.ntj - ti / 2) {
+    rem -= g.ntj - ti / 2;
+    ++ti;
+  }
+  i0 = ti * gram_tc::kM;
+  j0 = (ti / 2 + rem) * gram_tc::kN;
+  c0 = split * g.kper;
+  c1 = min(g.kchunks, c0 + g.kper);
+}
+
+// T += upper triangle of Y^T Y from the split operands: a producer thread
+// streams the four operand runs of a stage (A hi, A lo: 128 samples; B hi,
+// B lo: 256 samples; 32 parameters) into one of four 48 KB stages with bulk
+// copies; the issuer (lane 0) issues hi*hi + hi*lo + lo*hi as M128 N256 K16
+// MMAs into one of two TMEM accumulators (FP32 over a range of at most 4096
+// parameters); 4 drain warps add finished tiles into T with FP64 atomics.
+// Every wait is bounded.
+__global__ void __launch_bounds__(gram_split::kThreads, 1) gram_split_kernel(const __grid_constant__ GramSplitArgs g) {
+  using namespace gram_split;
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kStages * kStage);
+  uint64_t* full = bars;                 // [4] bytes of a stage landed
+  uint64_t* empty = bars + kStages;      // [4] MMAs done with a stage (commit)
+  uint64_t* accfull = bars + 2 * kStages;
+  uint64_t* accempty = accfull + 2;      // [2] drained (4 warp arrivals)
+  uint64_t* drain = accempty + 2;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(drain + 1);
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < kStages; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&accfull[i], 1);
+      mbar_init(&accempty[i], 4);
+    }
+    mbar_init(drain, 1);
+    fence_mbar_init();
+  }
+  if (warp == 1) {
+    tmem_alloc(tslot, 512);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+  bool abort = false;
+
+  if (warp == 0) {
+    // ---------------------------------------------------------------- producer
+    if (lane == 0) {
+      uint32_t gc = 0;
+      for (int64_t it = blockIdx.x; it < g.items && !abort; it += gridDim.x) {
+        int64_t i0, j0, c0, c1;
+        gram_split_item(g, it, i0, j0, c0, c1);
+        for (int64_t kc = c0; kc < c1; ++kc, ++gc) {
+          const uint32_t st = gc % kStages;
+          if (gc >= kStages && !mbar_wait(&empty[st], ((gc / kStages) - 1) & 1, g.err)) {
+            abort = true;
+            break;
+          }
+          uint8_t* base = smem + st * kStage;
+          const int64_t oa = (kc * g.groups + i0 / 8) * kBlock;
+          const int64_t ob = (kc * g.groups + j0 / 8) * kBlock;
+          mbar_arrive_expect_tx(&full[st], kStage);
+          bulk_g2s(base, g.hi + oa, kA, &full[st]);
+          bulk_g2s(base + kA, g.lo + oa, kA, &full[st]);
+          bulk_g2s(base + 2 * kA, g.hi + ob, kB, &full[st]);
+          bulk_g2s(base + 2 * kA + kB, g.lo + ob, kB, &full[st]);
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ---------------------------------------------------------------- issuer
+    const uint32_t idesc = umma_idesc_bf16_mn(gram_tc::kM, gram_tc::kN);
+    uint32_t gc = 0, li = 0;
+    for (int64_t it = blockIdx.x; it < g.items && !abort; it += gridDim.x, ++li) {
+      int64_t i0, j0, c0, c1;
+      gram_split_item(g, it, i0, j0, c0, c1);
+      const uint32_t buf = li % 2;
+      if (li >= 2 && !mbar_wait(&accempty[buf], ((li / 2) - 1) & 1, g.err)) {
+        abort = true;
+        break;
+      }
+      tc_fence_after();
+      const uint32_t d = tmem + buf * gram_tc::kN;
+      bool first = true;
+      for (int64_t kc = c0; kc < c1; ++kc, ++gc) {
+        const uint32_t st = gc % kStages;
+        if (!mbar_wait(&full[st], (gc / kStages) & 1, g.err)) {
+          abort = true;
+          break;
+        }
+        tc_fence_after();
+        if (lane == 0) {
+          const uint32_t base = smem_u32(smem + st * kStage);
+          const uint64_t ahi = umma_sdesc(base, 128, kK * 16), alo = umma_sdesc(base + kA, 128, kK * 16);
+          const uint64_t bhi = umma_sdesc(base + 2 * kA, 128, kK * 16);
+          const uint64_t blo = umma_sdesc(base + 2 * kA + kB, 128, kK * 16);
+#pragma unroll
+          for (int ks = 0; ks < kK / 16; ++ks) {
+            umma_bf16(d, ahi + ks * 16, bhi + ks * 16, idesc, (first && ks == 0) ? 0u : 1u);
+            umma_bf16(d, ahi + ks * 16, blo + ks * 16, idesc, 1u);
+            umma_bf16(d, alo + ks * 16, bhi + ks * 16, idesc, 1u);
+          }
+          umma_commit(&empty[st]);
+        }
+        __syncwarp();
+        first = false;
+      }
+      if (abort) break;
+      if (lane == 0) umma_commit(&accfull[buf]);
+      __syncwarp();
+    }
+    if (lane == 0) {
+      umma_commit(drain);
+      mbar_wait(drain, 0, g.err);
+    }
+    __syncwarp();
+  } else if (warp >= 4) {
+    // ---------------------------------------------------------------- drain
+    // warps 4..7 read TMEM lane quarters 0..3
+    const int q4 = warp % 4;
+    uint32_t li = 0;
+    for (int64_t it = blockIdx.x; it < g.items && !abort; it += gridDim.x, ++li) {
+      int64_t i0, j0, c0, c1;
+      gram_split_item(g, it, i0, j0, c0, c1);
+      const uint32_t buf = li % 2;
+      bool ok = mbar_wait(&accfull[buf], (li / 2) & 1, g.err);
+      ok = __all_sync(0xffffffffu, ok);
+      if (!ok) {
+        abort = true;
+        break;
+      }
+      tc_fence_after();
+      const int64_t i = i0 + q4 * 32 + lane;
+      const uint32_t tl = tmem + buf * gram_tc::kN + ((uint32_t)(q4 * 32) << 16);
+      for (int cq = 0; cq < gram_tc::kN; cq += 16) {
+        float v[16];
+        tmem_ld16(tl + cq, v);
+        tmem_ld_wait();
+        if (i < g.n) {
+#pragma unroll
+          for (int e = 0; e < 16; ++e) {
+            const int64_t j = j0 + cq + e;
+            if (j >= i && j < g.n) atomicAdd(&g.t[i * g.n + j], (double)v[e]);
+          }
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&accempty[buf]);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    tmem_dealloc(tmem, 512);
+  }
+}
+
 // ---------------------------------------------------------------- FP64 CG
 // State: x, r, p, q (n each) + scalars s[0]=rr, s[1]=pq, s[2]=rr_new, s[3]=stop
 // (1 when converged), s[4]=tol^2 * ||b||^2, s[5]=iterations.
@@ -683,7 +925,74 @@ static int gram_tc_add(const float* a_re, const float* a_im, int64_t n_params, i
   return check_cuda(launched(), "gram_tc_kernel");
 }
 
+static int split_run(const float* a, const float* b, int64_t ld, int64_t bsz, int64_t rows, int64_t n, void* split,
+                     cudaStream_t s) {
+  const int64_t groups = split_cols_pad(n) / 8;
+  const int64_t total = split_rows_pad(rows) * groups;
+  uint4* hi = static_cast<uint4*>(split);
+  uint4* lo = hi + total;
+  split_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(a, b, ld, bsz, rows, n, groups, total, hi, lo);
+  return check_cuda(launched(), "split_kernel");
+}
+
+static int gram_split_add(const void* split, int64_t rows, int64_t n, double* gram, cudaStream_t s) {
+  static std::once_flag attr_once;
+  static cudaError_t attr_err = cudaSuccess;
+  std::call_once(attr_once, [] {
+    attr_err = cudaFuncSetAttribute(gram_split_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    gram_split::kSmem);
+  });
+  FK_CUDA(attr_err);
+  GramSplitArgs a;
+  a.groups = split_cols_pad(n) / 8;
+  a.kchunks = split_rows_pad(rows) / 32;
+  a.hi = static_cast<const uint8_t*>(split);
+  a.lo = a.hi + a.kchunks * a.groups * gram_split::kBlock;
+  a.n = n;
+  a.nti = (n + gram_tc::kM - 1) / gram_tc::kM;
+  a.ntj = (n + gram_tc::kN - 1) / gram_tc::kN;
+  int64_t tiles = 0;
+  for (int64_t ti = 0; ti < a.nti; ++ti) tiles += a.ntj - ti / 2;
+  // ranges of at most 4096 parameters (128 chunks: the FP32 sums in TMEM, as
+  // in fk_sr_gram_tc), at least two items per SM
+  int64_t splits = (2 * 152 + tiles - 1) / tiles;
+  const int64_t min_splits = (a.kchunks + 127) / 128;
+  if (splits < min_splits) splits = min_splits;
+  if (splits > a.kchunks) splits = a.kchunks;
+  a.kper = (a.kchunks + splits - 1) / splits;
+  a.splits = (a.kchunks + a.kper - 1) / a.kper;
+  a.items = tiles * a.splits;
+  a.t = gram;
+  a.err = device_error_word();
+  const int64_t grid = a.items < 152 ? a.items : 152;
+  gram_split_kernel<<<(unsigned)grid, gram_split::kThreads, gram_split::kSmem, s>>>(a);
+  return check_cuda(launched(), "gram_split_kernel");
+}
+
 extern "C" {
+
+int64_t fk_sr_gram_split_bytes(int64_t rows, int64_t n) {
+  if (rows < 0 || n <= 0) return -1;
+  return split_bytes(rows, n);
+}
+
+int fk_sr_gram_split(const float* a, const float* b, int64_t ld, int64_t bsz, int64_t rows, int64_t n, void* split,
+                     int64_t split_bytes_given, void* stream) {
+  FK_CHECK_ARG(a && split && rows >= 0 && n > 0 && bsz > 0 && ld >= (b ? bsz : n) && (b || bsz >= n),
+               "fk_sr_gram_split: bad arguments");
+  FK_CHECK_ARG(((uintptr_t)split % 16) == 0, "fk_sr_gram_split: split must be 16-byte aligned");
+  FK_CHECK_ARG(split_bytes_given >= split_bytes(rows, n), "fk_sr_gram_split: split buffer %lld < %lld bytes",
+               (long long)split_bytes_given, (long long)split_bytes(rows, n));
+  if (rows == 0) return FK_OK;
+  return split_run(a, b ? b : a, ld, bsz, rows, n, split, static_cast<cudaStream_t>(stream));
+}
+
+int fk_sr_gram_split_accumulate(const void* split, int64_t rows, int64_t n, double* gram, void* stream) {
+  FK_CHECK_ARG(split && gram && rows >= 0 && n > 0 && n <= 65536, "fk_sr_gram_split_accumulate: bad arguments");
+  FK_CHECK_ARG(((uintptr_t)split % 16) == 0, "fk_sr_gram_split_accumulate: split must be 16-byte aligned");
+  if (rows == 0) return FK_OK;
+  return gram_split_add(split, rows, n, gram, static_cast<cudaStream_t>(stream));
+}
 
 int fk_sr_gram(const float* o_re, const float* o_im, int64_t n_params, int64_t n_samples, double* gram,
                int64_t gram_elems, void* stream) {

@@ -57,10 +57,10 @@ class ComplexValuesStochasticReconfiguration:
     instead of a Cholesky factorisation.
 
     ``gram``: "tc" builds the Gram on the tensor cores (split-BF16 products,
-    FP32-level accuracy, fk_sr_gram_tc), "fp32" on the CUDA cores
-    (fk_sr_gram); "auto" takes the tensor cores for a machine on the
-    tensor-core path (BF16/FP16) when the batch is a multiple of 8, the CUDA
-    cores otherwise (the plain FP32 path stays on CUDA cores throughout).
+    FP32-level accuracy: fk_sr_gram_split + fk_sr_gram_split_accumulate),
+    "fp32" on the CUDA cores (fk_sr_gram); "auto" takes the tensor cores for
+    a machine on the tensor-core path (BF16/FP16), the CUDA cores otherwise
+    (the plain FP32 path stays on CUDA cores throughout).
 
     ``rows_bytes``: for the AR network, the per-sample rows Y (num_params x
     2B float32) are stored whole when they take at most
@@ -122,8 +122,23 @@ class ComplexValuesStochasticReconfiguration:
             return "fk_sr_gram_tc"
         if self.gram == "fp32":
             return "fk_sr_gram"
-        tc = getattr(self.machine, "precision", "fp32") in ("bf16", "fp16") and b % 8 == 0
+        tc = getattr(self.machine, "precision", "fp32") in ("bf16", "fp16")
         return "fk_sr_gram_tc" if tc else "fk_sr_gram"
+
+    def _gram(self, o_re, o_im, p, b, gram, st):
+        """gram = Y^T Y, Y = [o_re | o_im] (p x 2b): on the tensor cores from
+        operands split into bf16 hi + lo once (fk_sr_gram_split, then
+        fk_sr_gram_split_accumulate), or on the CUDA cores (fk_sr_gram)."""
+        n = 2 * b
+        if self._gram_entry(b) == "fk_sr_gram":
+            _lib.call("fk_sr_gram", _lib.ptr(o_re), _lib.ptr(o_im), p, b, _lib.ptr(gram), n * n, st)
+            return
+        nbytes = _lib.load().fk_sr_gram_split_bytes(p, n)
+        split = torch.empty(nbytes, dtype=torch.uint8, device=gram.device)
+        _lib.call("fk_sr_gram_split", _lib.ptr(o_re), _lib.ptr(o_im), b, b, p, n, _lib.ptr(split), nbytes, st)
+        gram.zero_()
+        _lib.call("fk_sr_gram_split_accumulate", _lib.ptr(split), p, n, _lib.ptr(gram), st)
+        _lib.call("fk_sr_gram_mirror", _lib.ptr(gram), n, st)
 
     def _max_iter(self, n, n_complex_params):
         if self.iterative_solver:
@@ -142,7 +157,7 @@ class ComplexValuesStochasticReconfiguration:
         _lib.call("fk_center_columns", _lib.ptr(o_im), p, b, None, st)
         n = 2 * b
         bf = self._buffers(n, m.device)
-        _lib.call(self._gram_entry(b), _lib.ptr(o_re), _lib.ptr(o_im), p, b, _lib.ptr(bf["gram"]), n * n, st)
+        self._gram(o_re, o_im, p, b, bf["gram"], st)
         _lib.call("fk_sr_hermitian_embed", _lib.ptr(bf["gram"]), b, st)
         bf["rhs"][:b] = local[:, 0] - local[:, 0].mean()
         bf["rhs"][b:] = local[:, 1] - local[:, 1].mean()
@@ -177,7 +192,7 @@ class ComplexValuesStochasticReconfiguration:
         _lib.call("fk_center_columns", _lib.ptr(o_im), p, b, None, st)
         n = 2 * b
         bf = self._buffers(n, m.device)
-        _lib.call(self._gram_entry(b), _lib.ptr(o_re), _lib.ptr(o_im), p, b, _lib.ptr(bf["gram"]), n * n, st)
+        self._gram(o_re, o_im, p, b, bf["gram"], st)
         bf["rhs"][:b] = local[:, 0] - local[:, 0].mean()
         bf["rhs"][b:] = local[:, 1] - local[:, 1].mean()
         _lib.call("fk_sr_solve", _lib.ptr(bf["gram"]), n, 1.0 / b, self.diag_shift, _lib.ptr(bf["rhs"]), self.tol,
@@ -200,12 +215,12 @@ class ComplexValuesStochasticReconfiguration:
             _, _, saved = m.forward(s, mode=_lib.FK_AR2D_SAVE)
         ws = torch.empty(lib.fk_ar2d_sr_gram_workspace_bytes(ctypes_ref(m.desc), b), dtype=torch.uint8,
                          device=m.device)
+        tc = 1 if self._gram_entry(b) == "fk_sr_gram_tc" else 0
         budget = self.rows_bytes if self.rows_bytes is not None else self.STREAM_BUFFER_BYTES
-        floats = min(budget // 4, m.num_params * n)
-        floats = max(floats, lib.fk_ar2d_sr_gram_min_rows(ctypes_ref(m.desc), b))
+        floats = min(budget // 4, m.num_params * n * (2 if tc else 1))
+        floats = max(floats, lib.fk_ar2d_sr_gram_min_rows(ctypes_ref(m.desc), b, tc))
         rows = torch.empty(floats, dtype=torch.float32, device=m.device)
         bf = self._buffers(n, m.device)
-        tc = 1 if self._gram_entry(b) == "fk_sr_gram_tc" else 0
         _lib.call("fk_ar2d_sr_gram", ctypes_ref(m.desc), _lib.ptr(m.packed()), _lib.ptr(m.params), _lib.ptr(s), b,
                   _lib.ptr(saved), saved.numel(), _lib.ptr(ws), ws.numel(), _lib.ptr(rows), rows.numel(),
                   _lib.ptr(bf["gram"]), tc, st)

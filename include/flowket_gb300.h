@@ -177,13 +177,15 @@ int fk_ar2d_backward(const fk_ar2d_desc* desc, const void* packed, const float* 
  * rows of fk_ar2d_backward with seeds (1, 0) and (0, 1). Both per-sample
  * adjoints run together over the one set of activations in `saved`; each
  * conv's rows go, as they are produced, to a row buffer of rows_floats
- * floats (at least fk_ar2d_sr_gram_min_rows); when the next step's convs do
+ * floats (at least fk_ar2d_sr_gram_min_rows with the same tensor_cores);
+ * when the next step's convs do
  * not fit, and at the end, the buffered rows get the weight-norm chain rule,
  * are centred (fk_center_columns) and Y^T Y of the buffer is added into gram
- * (fk_sr_gram_accumulate; tensor_cores selects the split-BF16 tensor-core
- * Gram, which needs B a multiple of 4). */
+ * (tensor_cores = 0: fk_sr_gram_accumulate on the CUDA cores; 1: the split
+ * BF16 tensor-core Gram, fk_sr_gram_split + fk_sr_gram_split_accumulate, its
+ * split operands kept in the same buffer after the rows). */
 int64_t fk_ar2d_sr_gram_workspace_bytes(const fk_ar2d_desc* desc, int64_t batch);
-int64_t fk_ar2d_sr_gram_min_rows(const fk_ar2d_desc* desc, int64_t batch);
+int64_t fk_ar2d_sr_gram_min_rows(const fk_ar2d_desc* desc, int64_t batch, int32_t tensor_cores);
 int fk_ar2d_sr_gram(const fk_ar2d_desc* desc, const void* packed, const float* params, const int8_t* spins,
                     int64_t batch, const void* saved, int64_t saved_bytes, void* workspace, int64_t workspace_bytes,
                     float* rows, int64_t rows_floats, double* gram, int32_t tensor_cores, void* stream);
@@ -294,6 +296,18 @@ int fk_sr_gram_accumulate(const float* y, int64_t rows, int64_t n, double* gram,
                           void* stream);
 /* Copies the upper triangle of gram (n x n) into the lower one. */
 int fk_sr_gram_mirror(double* gram, int64_t n, void* stream);
+/* The tensor-core Gram in two stages, for Grams that read each value many
+ * times (n / 128 + n / 256 tiles per value): fk_sr_gram_split writes Y (rows
+ * x n, column c from a[p * ld + c] when c < bsz, else b[p * ld + c - bsz];
+ * b = NULL: all from a) once as bf16 hi + lo in the blocked operand layout
+ * (fk_sr_gram_split_bytes(rows, n) bytes, 16-byte aligned), and
+ * fk_sr_gram_split_accumulate adds the upper triangle of Y^T Y into gram
+ * (n x n float64, n <= 65536) from it, streaming the operands with bulk
+ * copies: the products and accuracy of fk_sr_gram_tc, any n. */
+int64_t fk_sr_gram_split_bytes(int64_t rows, int64_t n);
+int fk_sr_gram_split(const float* a, const float* b, int64_t ld, int64_t bsz, int64_t rows, int64_t n, void* split,
+                     int64_t split_bytes, void* stream);
+int fk_sr_gram_split_accumulate(const void* split, int64_t rows, int64_t n, double* gram, void* stream);
 /* FP64 conjugate gradients on (scale * gram + shift I) x = rhs, stopping at
  * ||r|| <= tol ||rhs|| or max_iter (linear_equations.py:34-137); stats (device,
  * optional) = {iterations, ||r||^2, tol^2 ||rhs||^2}. No host synchronisation. */

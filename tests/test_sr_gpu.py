@@ -63,6 +63,50 @@ def test_tensor_core_gram_matches_fp64(cuda, p, b, complex_):
         np.testing.assert_array_equal(got, got.T)
 
 
+@pytest.mark.parametrize("p,b,complex_", [(3000, 96, True), (4133, 200, True), (70_000, 512, True),
+                                         (1000, 45, True), (64, 8, True), (33, 300, False), (9000, 1030, False)])
+def test_split_tensor_core_gram_matches_fp64(cuda, p, b, complex_):
+    """fk_sr_gram_split (bf16 hi + lo written once in the blocked operand
+    layout) + fk_sr_gram_split_accumulate (bulk-copied operands, the same
+    split-BF16 products) + fk_sr_gram_mirror against the FP64 Gram of the
+    same FP32 rows, with fk_sr_gram_tc's bounds; column counts that are not
+    multiples of 8, 128 or 256 and row counts that are not multiples of 32.
+    Each call adds into the Gram: a second call doubles it."""
+    from flowket_gb300 import _lib
+    rng = np.random.default_rng(p + 3 * b)
+    a = rng.normal(size=(p, b)).astype(np.float32)
+    c = rng.normal(size=(p, b)).astype(np.float32) if complex_ else None
+    ta = torch.as_tensor(a).cuda()
+    tc = torch.as_tensor(c).cuda() if complex_ else None
+    n = 2 * b if complex_ else b
+    y = np.concatenate([a, c], axis=1).astype(np.float64) if complex_ else a.astype(np.float64)
+    want = y.T @ y
+    scale = np.sqrt(np.outer(np.diag(want), np.diag(want)))
+    lib = _lib.load()
+    nbytes = lib.fk_sr_gram_split_bytes(p, n)
+    split = torch.full((nbytes,), 255, dtype=torch.uint8, device="cuda")
+    st = _lib.stream_ptr()
+    _lib.call("fk_sr_gram_split", _lib.ptr(ta), _lib.ptr(tc), b, b if complex_ else n, p, n, _lib.ptr(split), nbytes,
+              st)
+    gram = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+    _lib.call("fk_sr_gram_split_accumulate", _lib.ptr(split), p, n, _lib.ptr(gram), st)
+    _lib.call("fk_sr_gram_mirror", _lib.ptr(gram), n, st)
+    got = gram.cpu().numpy()
+    err = np.abs(got - want) / scale
+    assert err.max() < 5e-5, err.max()
+    # off the diagonal: <= 3 * 2^-18 per product (lo*lo dropped, lo rounded);
+    # over >= 1000 random rows the errors average to 2e-7, over 33 to 5e-6
+    assert err[~np.eye(n, dtype=bool)].max() < (2e-6 if p >= 1000 else 1.5e-5)
+    np.testing.assert_array_equal(got, got.T)
+    # a second accumulation adds the same tile sums again
+    _lib.call("fk_sr_gram_split_accumulate", _lib.ptr(split), p, n, _lib.ptr(gram), st)
+    _lib.call("fk_sr_gram_mirror", _lib.ptr(gram), n, st)
+    np.testing.assert_allclose(gram.cpu().numpy(), 2 * got, rtol=1e-12, atol=0)
+    assert lib.fk_sr_gram_split(_lib.ptr(ta), _lib.ptr(tc), b, b if complex_ else n, p, n, _lib.ptr(split),
+                                nbytes - 1, st) == -1
+    assert b"split buffer" in lib.fk_last_error()
+
+
 def test_tensor_core_gram_rejects_unsupported_shapes(cuda):
     from flowket_gb300 import _lib
     lib = _lib.load()
@@ -96,7 +140,8 @@ def test_sr_direction_matches_parameter_space_solve(cuda, gram):
     assert np.linalg.norm(x - want) / np.linalg.norm(want) < 1e-3
 
 
-def test_vmc_with_sr_lowers_energy(cuda):
+@pytest.mark.parametrize("rows_bytes", [None, 4])
+def test_vmc_with_sr_lowers_energy(cuda, rows_bytes):
     from flowket_gb300.machines import ConvNetAutoregressive2D
     from flowket_gb300.operators import Heisenberg
     from flowket_gb300.optimization import VariationalMonteCarlo
@@ -106,11 +151,12 @@ def test_vmc_with_sr_lowers_energy(cuda):
     m = ConvNetAutoregressive2D(shape, 3, 16, weights_normalization=True, precision="fp32", seed=0)
     vmc = VariationalMonteCarlo(m, Heisenberg(hilbert_state_shape=shape, pbc=True),
                                 FastAutoregressiveSampler(m, 256, seed=3))
-    opt = ComplexValuesStochasticReconfiguration(m, lr=0.05, diag_shift=1e-3)
+    opt = ComplexValuesStochasticReconfiguration(m, lr=0.05, diag_shift=1e-3, rows_bytes=rows_bytes)
     energies = []
     for _ in range(30):
         vmc.step(opt)
         energies.append(vmc.current_energy.real)
+    assert opt.streamed == (rows_bytes is not None)
     assert np.mean(energies[-5:]) < np.mean(energies[:3]) - 1.0
 
 
@@ -175,7 +221,7 @@ def test_streamed_sr_gram_equals_gram_of_stored_rows(cuda, net, tensor_cores):
     lib = _lib.load()
     d = ctypes_ref(m.desc)
     ws = torch.empty(lib.fk_ar2d_sr_gram_workspace_bytes(d, b), dtype=torch.uint8, device="cuda")
-    min_rows = lib.fk_ar2d_sr_gram_min_rows(d, b)
+    min_rows = lib.fk_ar2d_sr_gram_min_rows(d, b, tensor_cores)
     rows = torch.empty(min_rows + 7, dtype=torch.float32, device="cuda")
     gram = torch.full((n, n), float("nan"), dtype=torch.float64, device="cuda")
     _lib.call("fk_ar2d_sr_gram", d, _lib.ptr(m.packed()), _lib.ptr(m.params), _lib.ptr(s), b, _lib.ptr(saved),
