@@ -285,6 +285,26 @@ int launch_wgrad_tc(const WgTcArgs& a, int kw, int kcol0, float* dW, float* db, 
 int launch_bias_sum(const void* G, int64_t tiles, int H, int W, int g0, int n, int64_t batch, float* part, float* db,
                     cudaStream_t s);
 
+// Per-sample weight and bias gradients of one conv with 32 input channels on
+// the tensor cores (wgrad_rows_tc_kernel): for every sample b,
+// dW_b[tap][ci][n] = sum_pix X_b[pix + tap][ci] G_b[pix][g0 + n] and
+// db_b[n] = sum_pix G_b[pix][g0 + n], written to
+// O[(o_kernel + (tap * 32 + ci) * N + n) * o_ld + o_col + b] and
+// O[(o_bias + n) * o_ld + o_col + b].
+struct WgRowsArgs {
+  const void* X;   // activations (16-bit blocked, 32 channels)
+  const void* G;   // gradients (16-bit blocked, gC channels)
+  int gC, g0, N;   // N: 16 or 32
+  int ntaps;
+  int dr[9], dc[9];
+  float* O;
+  int64_t o_kernel, o_bias, o_ld, o_col;
+  int64_t batch;
+};
+// False when the lattice is too large for the kernel's shared memory.
+bool wgrad_rows_tc_supported(int H, int W, int N);
+int launch_wgrad_rows_tc(const WgRowsArgs& a, int H, int W, int* err, cudaStream_t s);
+
 }  // namespace FK_NS
 
 #ifndef FK_TC_FP16

@@ -706,27 +706,41 @@ __global__ void wgrad_part_reduce_kernel(const float* part, int64_t tiles, int k
     dB[e - kn] = s;
 }
 
+// Where the per-sample rows of conv cd go: the [num_params][batch] array O,
+// or the sink's buffer.
+struct RowsTarget {
+  float* O;
+  int64_t o_kernel, o_bias, o_ld, o_col;
+};
+
+static int rows_target(const NetLayout& L, const ConvDesc& cd, float* O, int64_t batch, cudaStream_t s,
+                       RowSink* sink, RowsTarget* t) {
+  if (sink) {
+    int64_t r0 = 0;
+    const int st = sink_place(*sink, (int)(&cd - L.conv), &r0, s);
+    if (st != FK_OK) return st;
+    *t = RowsTarget{sink->buf, r0, r0 + (cd.p_bias - cd.p_kernel), sink->ld, sink->col};
+  } else {
+    *t = RowsTarget{O, cd.p_kernel, cd.p_bias, batch, 0};
+  }
+  return FK_OK;
+}
+
 template <typename T, typename TG = float>
 static int launch_wgrad(const NetLayout& L, WgArgs& w, const ConvDesc& cd, float* grad, float* O, int64_t batch,
                         cudaStream_t s, RowSink* sink = nullptr) {
   int64_t tiles = (batch + kTile - 1) / kTile;
   w.batch = batch;
   w.items = w.ntaps * ((w.cin + 7) / 8) * ((w.N + 7) / 8);
-  if (O && sink) {
-    int64_t r0 = 0;
-    const int st = sink_place(*sink, (int)(&cd - L.conv), &r0, s);
+  if (O) {
+    RowsTarget t;
+    const int st = rows_target(L, cd, O, batch, s, sink, &t);
     if (st != FK_OK) return st;
-    w.O = sink->buf;
-    w.o_kernel = r0;
-    w.o_bias = r0 + (cd.p_bias - cd.p_kernel);
-    w.o_ld = sink->ld;
-    w.o_col = sink->col;
-  } else if (O) {
-    w.O = O;
-    w.o_kernel = cd.p_kernel;
-    w.o_bias = cd.p_bias;
-    w.o_ld = batch;
-    w.o_col = 0;
+    w.O = t.O;
+    w.o_kernel = t.o_kernel;
+    w.o_bias = t.o_bias;
+    w.o_ld = t.o_ld;
+    w.o_col = t.o_col;
   } else {
     w.dW = grad + cd.p_kernel;
     w.dB = grad + cd.p_bias;
@@ -917,6 +931,18 @@ static int64_t tc_bwd_layout(const NetLayout& L, int64_t batch, char* base, TcBw
   return off;
 }
 
+// Per-sample weight gradients of the tensor-core adjoint's 32-channel convs on
+// the tensor cores (wgrad_rows_tc_kernel); FK_AR2D_ROWS=cuda keeps them on the
+// CUDA cores (wgrad_kernel on the same 16-bit gradients, for comparisons).
+static bool rows_on_tensor_cores() {
+  static int v = -1;
+  if (v < 0) {
+    const char* e = getenv("FK_AR2D_ROWS");
+    v = (e && strcmp(e, "cuda") == 0) ? 0 : 1;
+  }
+  return v == 1;
+}
+
 // FK_AR2D_ENGINE=rowwise also selects the CUDA-core adjoint (for comparisons).
 static bool use_tc_adjoint(const NetLayout& L) {
   static int v = -1;
@@ -975,6 +1001,39 @@ static int backward_tc(const NetLayout& L, const void* packed, const float* para
   // [g0, g0 + n) of Gt
   auto wg_rows = [&](int kind, int dr, int dc, const void* X, int cin, const void* Gt, int g0, int n,
                      const ConvDesc& cd) -> int {
+    if (cin == 32 && rows_on_tensor_cores() && wgrad_rows_tc_supported(L.H, L.W, n)) {
+      WgRowsArgs r;
+      memset(&r, 0, sizeof(r));
+      WgArgs taps;
+      memset(&taps, 0, sizeof(taps));
+      if (kind >= 0) {
+        tap_list(kind, taps);
+      } else {
+        taps.ntaps = 1;
+        taps.dr[0] = dr;
+        taps.dc[0] = dc;
+      }
+      r.X = X;
+      r.G = Gt;
+      r.gC = F;
+      r.g0 = g0;
+      r.N = n;
+      r.ntaps = taps.ntaps;
+      for (int t = 0; t < taps.ntaps; ++t) {
+        r.dr[t] = taps.dr[t];
+        r.dc[t] = taps.dc[t];
+      }
+      RowsTarget tg;
+      const int st = rows_target(L, cd, O, batch, s, sink, &tg);
+      if (st != FK_OK) return st;
+      r.O = tg.O;
+      r.o_kernel = tg.o_kernel;
+      r.o_bias = tg.o_bias;
+      r.o_ld = tg.o_ld;
+      r.o_col = tg.o_col;
+      r.batch = batch;
+      return launch_wgrad_rows_tc(r, L.H, L.W, err, s);
+    }
     WgArgs w;
     memset(&w, 0, sizeof(w));
     w.spins = spins;

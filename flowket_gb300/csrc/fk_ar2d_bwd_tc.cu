@@ -529,6 +529,238 @@ __global__ void bias_reduce_kernel(const float* part, int64_t tiles, int n, floa
   db[co] = s;
 }
 
+// ============================================================== per-sample rows
+// Per-sample weight gradients of a 32-input-channel conv as tensor-core
+// products, one sample at a time: with K = the sample's pixels (padded to a
+// multiple of 16), A = its input activations shifted by each tap (M = taps x
+// 32 channels: four taps per M = 128 tile, one more 8-row group of ones whose
+// products are the bias gradient), B = its output gradients (N = 16 or 32):
+// D_b[(tap, ci)][n] = sum_pix X_b[pix + tap][ci] G_b[pix][n]. Both operands
+// MN-major in shared memory ([8-channel group][pixel][8 channels], LBO 128 B
+// along the pixels, SBO = K * 16 B along the channels), staged from the
+// blocked layouts by 8 warps (zero outside the lattice); one thread issues
+// the K/16 MMAs of each sample into its own N columns of a TMEM buffer that
+// holds 8 samples; 4 drain warps (TMEM lane quarter = tap slot, lane = input
+// channel) write each (row, n) as 8 consecutive samples (32 bytes) of the
+// parameter-major rows. Work item = (8 samples, M tile); two 8-sample TMEM
+// buffers and two staging stages of S samples (2, or 1 on lattices whose
+// operands would not fit) overlap staging, MMAs and writes. Every wait is
+// bounded.
+namespace wgrows {
+constexpr int kStageWarps = 8, kIssuer = 8, kThreads = 32 * 13;
+constexpr int kGroupRows = 16;  // A: 16 groups of 8 rows (M = 128)
+__host__ __device__ inline int ksteps(int H, int W) { return (H * W + 15) / 16; }
+inline int stage_bytes(int S, int H, int W, int N) { return S * (kGroupRows + N / 8) * ksteps(H, W) * 16 * 16; }
+inline int samples_per_stage(int H, int W, int N) {
+  return 2 * stage_bytes(2, H, W, N) + 256 <= 200 * 1024 ? 2 : 1;
+}
+}  // namespace wgrows
+
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr)
+               : "memory");
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+template <int N>
+__global__ void __launch_bounds__(wgrows::kThreads, 1) wgrad_rows_tc_kernel(const __grid_constant__ WgRowsArgs a,
+                                                                             int H, int W, int S, int* err) {
+  using namespace wgrows;
+  using T = tc16;
+  constexpr int NG = N / 8;
+  extern __shared__ __align__(1024) uint8_t smem[];
+  const int P = H * W;
+  const int KS = ksteps(H, W), Qk = KS * 16;
+  const int stage = S * (kGroupRows + NG) * Qk * 16;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + 2 * stage);
+  uint64_t* full = bars;          // [2] staged (8 warp arrivals)
+  uint64_t* empty = bars + 2;     // [2] MMAs done with a stage (commit)
+  uint64_t* accfull = bars + 4;   // [2] 8 samples' products complete (commit)
+  uint64_t* accempty = bars + 6;  // [2] written out (4 warp arrivals)
+  uint64_t* drain = bars + 8;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 9);
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int ntiles_m = (a.ntaps + 1 + 3) / 4;  // taps and the ones slot, four per M tile
+  const int64_t groups = (a.batch + 7) / 8;
+  const int64_t items = groups * ntiles_m;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&full[i], kStageWarps);
+      mbar_init(&empty[i], 1);
+      mbar_init(&accfull[i], 1);
+      mbar_init(&accempty[i], 4);
+    }
+    mbar_init(drain, 1);
+    fence_mbar_init();
+  }
+  if (warp == kIssuer) {
+    tmem_alloc(tslot, 512);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+  bool abort = false;
+  const int subs = 8 / S;
+
+  if (warp < kStageWarps) {
+    // ---------------------------------------------------------------- staging
+    const int tid = threadIdx.x;
+    const int nch = S * (kGroupRows + NG) * Qk;
+    uint32_t gc = 0;
+    for (int64_t it = blockIdx.x; it < items && !abort; it += gridDim.x) {
+      const int64_t grp = it / ntiles_m;
+      const int mt = (int)(it % ntiles_m);
+      for (int sub = 0; sub < subs && !abort; ++sub, ++gc) {
+        const uint32_t st = gc % 2;
+        if (gc >= 2 && !mbar_wait(&empty[st], ((gc / 2) - 1) & 1, err)) {
+          abort = true;
+          break;
+        }
+        uint8_t* base = smem + st * stage;
+        // chunk c = ((region * Qk) + p) * S + s: the S samples of a (pixel,
+        // group) are adjacent in the blocked layout (one sector)
+        for (int c = tid; c < nch; c += kStageWarps * 32) {
+          const int s = c % S;
+          const int rest = c / S;
+          const int p = rest % Qk;
+          const int region = rest / Qk;
+          const int64_t b = grp * 8 + sub * S + s;
+          const int64_t tile = b / kTile;
+          const int m = (int)(b % kTile);
+          uint4 v = make_uint4(0u, 0u, 0u, 0u);
+          uint8_t* dst;
+          const int r0 = p / W, c0 = p % W;
+          if (region < kGroupRows) {
+            const int k = region >> 2, g = region & 3;
+            const int t = 4 * mt + k;
+            if (p < P && t < a.ntaps) {
+              const int r = r0 + a.dr[t], cc = c0 + a.dc[t];
+              if (r >= 0 && r < H && cc >= 0 && cc < W)
+                v = *reinterpret_cast<const uint4*>(blk<T>(a.X, tile, P, r * W + cc, 32) +
+                                                    ((int64_t)g * kTile + m) * 8);
+            } else if (p < P && t == a.ntaps && g == 0) {
+              v = make_uint4(kTcOnePair, kTcOnePair, kTcOnePair, kTcOnePair);
+            }
+            dst = base + ((int64_t)s * kGroupRows * Qk + (int64_t)region * Qk + p) * 16;
+          } else {
+            const int gn = region - kGroupRows;
+            if (p < P)
+              v = *reinterpret_cast<const uint4*>(blk<T>(a.G, tile, P, p, a.gC) +
+                                                  ((int64_t)(a.g0 / 8 + gn) * kTile + m) * 8);
+            dst = base + ((int64_t)S * kGroupRows * Qk + (int64_t)s * NG * Qk + (int64_t)gn * Qk + p) * 16;
+          }
+          *reinterpret_cast<uint4*>(dst) = v;
+        }
+        fence_proxy_async_smem();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&full[st]);
+      }
+    }
+  } else if (warp == kIssuer) {
+    // ---------------------------------------------------------------- issuer
+    const uint32_t idesc = umma_idesc_tc16_mn(128, N);
+    uint32_t gc = 0, li = 0;
+    for (int64_t it = blockIdx.x; it < items && !abort; it += gridDim.x, ++li) {
+      const uint32_t buf = li % 2;
+      if (li >= 2 && !mbar_wait(&accempty[buf], ((li / 2) - 1) & 1, err)) {
+        abort = true;
+        break;
+      }
+      tc_fence_after();
+      for (int sub = 0; sub < subs; ++sub, ++gc) {
+        const uint32_t st = gc % 2;
+        if (!mbar_wait(&full[st], (gc / 2) & 1, err)) {
+          abort = true;
+          break;
+        }
+        tc_fence_after();
+        if (lane == 0) {
+          const uint32_t base = smem_u32(smem + st * stage);
+          for (int s = 0; s < S; ++s) {
+            const uint32_t d = tmem + buf * 256 + (uint32_t)((sub * S + s) * N);
+            const uint32_t ab = base + (uint32_t)(s * kGroupRows * Qk * 16);
+            const uint32_t bb = base + (uint32_t)((S * kGroupRows + s * NG) * Qk * 16);
+            for (int ks = 0; ks < KS; ++ks)
+              umma_bf16(d, umma_sdesc(ab + ks * 256, 128, Qk * 16), umma_sdesc(bb + ks * 256, 128, Qk * 16), idesc,
+                        ks > 0 ? 1u : 0u);
+          }
+          umma_commit(&empty[st]);
+        }
+        __syncwarp();
+      }
+      if (abort) break;
+      if (lane == 0) umma_commit(&accfull[buf]);
+      __syncwarp();
+    }
+    if (lane == 0) {
+      umma_commit(drain);
+      mbar_wait(drain, 0, err);
+    }
+    __syncwarp();
+  } else {
+    // ---------------------------------------------------------------- drain
+    // warp 9..12 -> TMEM lane quarter 1, 2, 3, 0 = tap slot within the M tile
+    const int k = warp % 4;
+    const bool vec = (a.o_ld % 4) == 0 && (a.o_col % 4) == 0;
+    uint32_t li = 0;
+    for (int64_t it = blockIdx.x; it < items && !abort; it += gridDim.x, ++li) {
+      const int64_t grp = it / ntiles_m;
+      const int mt = (int)(it % ntiles_m);
+      const uint32_t buf = li % 2;
+      bool ok = mbar_wait(&accfull[buf], (li / 2) & 1, err);
+      ok = __all_sync(0xffffffffu, ok);
+      if (!ok) {
+        abort = true;
+        break;
+      }
+      tc_fence_after();
+      const int t = 4 * mt + k;
+      const int64_t b0 = grp * 8;
+      const int nb = a.batch - b0 < 8 ? (int)(a.batch - b0) : 8;
+      const uint32_t tl = tmem + buf * 256 + ((uint32_t)(k * 32) << 16);
+      if (t <= a.ntaps) {
+        for (int nc = 0; nc < NG; ++nc) {
+          float v[8][8];
+#pragma unroll
+          for (int j = 0; j < 8; ++j) tmem_ld8(tl + (uint32_t)(j * N + nc * 8), v[j]);
+          tmem_ld_wait();
+          if (t < a.ntaps || lane == 0) {
+#pragma unroll
+            for (int n = 0; n < 8; ++n) {
+              const int64_t row = t < a.ntaps ? a.o_kernel + ((int64_t)(t * 32 + lane) * N + nc * 8 + n)
+                                              : a.o_bias + nc * 8 + n;
+              float* dst = a.O + row * a.o_ld + a.o_col + b0;
+              if (vec && nb == 8) {
+                reinterpret_cast<float4*>(dst)[0] = make_float4(v[0][n], v[1][n], v[2][n], v[3][n]);
+                reinterpret_cast<float4*>(dst)[1] = make_float4(v[4][n], v[5][n], v[6][n], v[7][n]);
+              } else {
+#pragma unroll
+                for (int j = 0; j < 8; ++j)
+                  if (j < nb) dst[j] = v[j][n];
+              }
+            }
+          }
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&accempty[buf]);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == kIssuer) {
+    tc_fence_after();
+    tmem_dealloc(tmem, 512);
+  }
+}
+
 // ============================================================== launchers
 template <int F>
 static int set_smem(const void* fn, int bytes) {
@@ -584,6 +816,37 @@ int launch_wgrad_tc(const WgTcArgs& a, int kw, int kcol0, float* dW, float* db, 
   wgrad_reduce_kernel<<<(per + 255) / 256, 256, 0, s>>>(a.part, (int)grid, a.x_rows, a.ntc, a.n, kw, kcol0, dW,
                                                         a.part_bias, a.bias_jpos >= 0 ? db : nullptr);
   return check_cuda(launched(), "wgrad_reduce_kernel");
+}
+
+bool wgrad_rows_tc_supported(int H, int W, int N) {
+  return (N == 16 || N == 32) && wgrows::samples_per_stage(H, W, N) >= 1 &&
+         2 * wgrows::stage_bytes(wgrows::samples_per_stage(H, W, N), H, W, N) + 256 <= 220 * 1024;
+}
+
+int launch_wgrad_rows_tc(const WgRowsArgs& a, int H, int W, int* err, cudaStream_t s) {
+  if (!wgrad_rows_tc_supported(H, W, a.N) || a.ntaps < 1 || a.ntaps > 9) return FK_ERR_ARG;
+  static bool attr16 = false, attr32 = false;
+  const int S = wgrows::samples_per_stage(H, W, a.N);
+  const int smem = 2 * wgrows::stage_bytes(S, H, W, a.N) + 256;
+  const int64_t items = (a.batch + 7) / 8 * ((a.ntaps + 4) / 4);
+  int64_t grid = sm_count();
+  if (grid > items) grid = items;
+  if (a.N == 16) {
+    if (!attr16) {
+      int st = set_smem<32>((const void*)wgrad_rows_tc_kernel<16>, 220 * 1024);
+      if (st != FK_OK) return st;
+      attr16 = true;
+    }
+    wgrad_rows_tc_kernel<16><<<(unsigned)grid, wgrows::kThreads, smem, s>>>(a, H, W, S, err);
+  } else {
+    if (!attr32) {
+      int st = set_smem<32>((const void*)wgrad_rows_tc_kernel<32>, 220 * 1024);
+      if (st != FK_OK) return st;
+      attr32 = true;
+    }
+    wgrad_rows_tc_kernel<32><<<(unsigned)grid, wgrows::kThreads, smem, s>>>(a, H, W, S, err);
+  }
+  return check_cuda(launched(), "wgrad_rows_tc_kernel");
 }
 
 int launch_bias_sum(const void* G, int64_t tiles, int H, int W, int g0, int n, int64_t batch, float* part, float* db,

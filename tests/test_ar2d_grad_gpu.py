@@ -205,3 +205,40 @@ def test_tensor_core_per_sample_rows_match_cuda_core(cuda, tmp_path, precision):
     summed = m.backward(s, torch.as_tensor(w).cuda(), saved).cpu().numpy().astype(np.float64)
     from_rows = got.real @ w[:, 0] + got.imag @ w[:, 1]
     assert np.linalg.norm(from_rows - summed) / np.linalg.norm(summed) < 3e-2
+
+
+@pytest.mark.parametrize("precision", ["bf16", "fp16"])
+@pytest.mark.parametrize("shape,depth,b", [((5, 7), 4, 130), ((10, 10), 5, 256), ((16, 16), 3, 64)])
+def test_per_sample_weight_gradients_on_tensor_cores(cuda, tmp_path, shape, depth, b, precision):
+    """The per-sample weight and bias gradients of the tensor-core adjoint on
+    the tensor cores (wgrad_rows_tc_kernel: per sample, the tap-shifted input
+    activations times the output gradients over K = pixels) against the
+    CUDA-core per-sample kernel on the same 16-bit gradient tensors
+    (FK_AR2D_ROWS=cuda): both sum the same products in FP32, in different
+    orders. A batch that is not a multiple of 8 (130) has a partial last
+    group of samples; 16x16 stages one sample at a time."""
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = (
+        "import sys; sys.path.insert(0, %r);"
+        "import numpy as np, torch;"
+        "from flowket_gb300 import _lib;"
+        "from flowket_gb300.machines import ConvNetAutoregressive2D;"
+        "m = ConvNetAutoregressive2D(%r, %d, 32, weights_normalization=True, precision=%r, seed=9);"
+        "rng = np.random.default_rng(10);"
+        "s = torch.as_tensor(rng.choice([-1, 1], size=(%d,) + %r).astype(np.int8)).cuda();"
+        "_, _, saved = m.forward(s, mode=_lib.FK_AR2D_SAVE);"
+        "np.save(%r, m.log_derivatives(s, saved).cpu().numpy())"
+    ) % (root, shape, depth, precision, b, shape, str(tmp_path / "o.npy"))
+    env = dict(os.environ, FK_AR2D_ROWS="cuda")
+    subprocess.run([sys.executable, "-c", code], check=True, env=env)
+    ref = np.load(tmp_path / "o.npy").astype(np.complex128)
+    from flowket_gb300 import _lib
+    from flowket_gb300.machines import ConvNetAutoregressive2D
+    m = ConvNetAutoregressive2D(shape, depth, 32, weights_normalization=True, precision=precision, seed=9)
+    rng = np.random.default_rng(10)
+    s = torch.as_tensor(rng.choice([-1, 1], size=(b,) + shape).astype(np.int8)).cuda()
+    _, _, saved = m.forward(s, mode=_lib.FK_AR2D_SAVE)
+    got = m.log_derivatives(s, saved).cpu().numpy().astype(np.complex128)
+    assert got.shape == ref.shape == (m.num_params, b)
+    err = np.abs(got - ref).max(axis=0) / np.abs(ref).max(axis=0)
+    assert err.max() < 1e-5, err.max()
