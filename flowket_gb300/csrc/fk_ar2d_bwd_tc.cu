@@ -551,8 +551,10 @@ constexpr int kStageWarps = 8, kIssuer = 8, kThreads = 32 * 13;
 constexpr int kGroupRows = 16;  // A: 16 groups of 8 rows (M = 128)
 __host__ __device__ inline int ksteps(int H, int W) { return (H * W + 15) / 16; }
 inline int stage_bytes(int S, int H, int W, int N) { return S * (kGroupRows + N / 8) * ksteps(H, W) * 16 * 16; }
+// two samples per stage when their operands fit in shared memory and one
+// staging thread per (pixel, sample) remains
 inline int samples_per_stage(int H, int W, int N) {
-  return 2 * stage_bytes(2, H, W, N) + 256 <= 200 * 1024 ? 2 : 1;
+  return 2 * stage_bytes(2, H, W, N) + 256 <= 200 * 1024 && ksteps(H, W) * 32 <= kStageWarps * 32 ? 2 : 1;
 }
 }  // namespace wgrows
 
@@ -611,7 +613,6 @@ __global__ void __launch_bounds__(wgrows::kThreads, 1) wgrad_rows_tc_kernel(cons
   if (warp < kStageWarps) {
     // ---------------------------------------------------------------- staging
     const int tid = threadIdx.x;
-    const int nch = S * (kGroupRows + NG) * Qk;
     uint32_t gc = 0;
     for (int64_t it = blockIdx.x; it < items && !abort; it += gridDim.x) {
       const int64_t grp = it / ntiles_m;
@@ -623,39 +624,43 @@ __global__ void __launch_bounds__(wgrows::kThreads, 1) wgrad_rows_tc_kernel(cons
           break;
         }
         uint8_t* base = smem + st * stage;
-        // chunk c = ((region * Qk) + p) * S + s: the S samples of a (pixel,
-        // group) are adjacent in the blocked layout (one sector)
-        for (int c = tid; c < nch; c += kStageWarps * 32) {
-          const int s = c % S;
-          const int rest = c / S;
-          const int p = rest % Qk;
-          const int region = rest / Qk;
+        // thread = (pixel p, sample s) of the stage, s fastest (the S samples of
+        // a (pixel, group) are adjacent in the blocked layout); it stages that
+        // pixel's 16 A groups (taps x channel groups) and NG B groups, loads
+        // issued before the stores. No divisions inside the loops.
+        if (tid < Qk * S) {
+          const int s = tid % S;
+          const int p = tid / S;
           const int64_t b = grp * 8 + sub * S + s;
           const int64_t tile = b / kTile;
           const int m = (int)(b % kTile);
-          uint4 v = make_uint4(0u, 0u, 0u, 0u);
-          uint8_t* dst;
-          const int r0 = p / W, c0 = p % W;
-          if (region < kGroupRows) {
-            const int k = region >> 2, g = region & 3;
+          const int r0 = p / W, cq = p - (p / W) * W;
+          const bool live = p < P;
+          uint8_t* arow = base + ((int64_t)s * kGroupRows * Qk + p) * 16;
+          uint8_t* brow = base + ((int64_t)S * kGroupRows * Qk + (int64_t)s * NG * Qk + p) * 16;
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
             const int t = 4 * mt + k;
-            if (p < P && t < a.ntaps) {
-              const int r = r0 + a.dr[t], cc = c0 + a.dc[t];
-              if (r >= 0 && r < H && cc >= 0 && cc < W)
-                v = *reinterpret_cast<const uint4*>(blk<T>(a.X, tile, P, r * W + cc, 32) +
-                                                    ((int64_t)g * kTile + m) * 8);
-            } else if (p < P && t == a.ntaps && g == 0) {
-              v = make_uint4(kTcOnePair, kTcOnePair, kTcOnePair, kTcOnePair);
+            uint4 v[4];
+            const T* src = nullptr;
+            if (live && t < a.ntaps) {
+              const int r = r0 + a.dr[t], cc = cq + a.dc[t];
+              if (r >= 0 && r < H && cc >= 0 && cc < W) src = blk<T>(a.X, tile, P, r * W + cc, 32) + m * 8;
             }
-            dst = base + ((int64_t)s * kGroupRows * Qk + (int64_t)region * Qk + p) * 16;
-          } else {
-            const int gn = region - kGroupRows;
-            if (p < P)
-              v = *reinterpret_cast<const uint4*>(blk<T>(a.G, tile, P, p, a.gC) +
-                                                  ((int64_t)(a.g0 / 8 + gn) * kTile + m) * 8);
-            dst = base + ((int64_t)S * kGroupRows * Qk + (int64_t)s * NG * Qk + (int64_t)gn * Qk + p) * 16;
+#pragma unroll
+            for (int g = 0; g < 4; ++g)
+              v[g] = src ? *reinterpret_cast<const uint4*>(src + (int64_t)g * kTile * 8) : make_uint4(0u, 0u, 0u, 0u);
+            if (live && t == a.ntaps) v[0] = make_uint4(kTcOnePair, kTcOnePair, kTcOnePair, kTcOnePair);
+#pragma unroll
+            for (int g = 0; g < 4; ++g) *reinterpret_cast<uint4*>(arow + (int64_t)(4 * k + g) * Qk * 16) = v[g];
           }
-          *reinterpret_cast<uint4*>(dst) = v;
+          uint4 w[NG];
+          const T* gsrc = live ? blk<T>(a.G, tile, P, p, a.gC) + ((int64_t)(a.g0 / 8) * kTile + m) * 8 : nullptr;
+#pragma unroll
+          for (int g = 0; g < NG; ++g)
+            w[g] = gsrc ? *reinterpret_cast<const uint4*>(gsrc + (int64_t)g * kTile * 8) : make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+          for (int g = 0; g < NG; ++g) *reinterpret_cast<uint4*>(brow + (int64_t)g * Qk * 16) = w[g];
         }
         fence_proxy_async_smem();
         __syncwarp();
@@ -819,8 +824,9 @@ int launch_wgrad_tc(const WgTcArgs& a, int kw, int kcol0, float* dW, float* db, 
 }
 
 bool wgrad_rows_tc_supported(int H, int W, int N) {
-  return (N == 16 || N == 32) && wgrows::samples_per_stage(H, W, N) >= 1 &&
-         2 * wgrows::stage_bytes(wgrows::samples_per_stage(H, W, N), H, W, N) + 256 <= 220 * 1024;
+  const int S = wgrows::samples_per_stage(H, W, N);
+  return (N == 16 || N == 32) && 2 * wgrows::stage_bytes(S, H, W, N) + 256 <= 220 * 1024 &&
+         wgrows::ksteps(H, W) * 16 * S <= wgrows::kStageWarps * 32;
 }
 
 int launch_wgrad_rows_tc(const WgRowsArgs& a, int H, int W, int* err, cudaStream_t s) {
