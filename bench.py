@@ -530,6 +530,12 @@ def kernels_case(args):
     fps = flops_per_sample_forward(SHAPE, DEPTH, CHANNELS)
     record("adjoint_10x10_d10_f32", ms, flops=2.0 * fps * b, peak=peaks.get("bf16_tflops_sustained"),
            unit="TFLOP/s (bf16, measured)", samples=b, note="algorithmic FLOPs: 2x the forward's")
+    # per-sample rows (Re and Im log-derivatives) of 1024 samples: two
+    # per-sample adjoints, the weight gradients on tcgen05 (wgrad_rows_tc_kernel)
+    bo = 1024
+    ms = timed(lambda: m.log_derivatives(spins[:bo], None))
+    record("per_sample_rows_10x10_d10_f32", ms, nbytes=2 * m.num_params * bo * 4, samples=bo, params=m.num_params,
+           note="bytes: the rows written (forward and data gradients included in the time)")
     obs = Observable(Ising(h=H_FIELD, hilbert_state_shape=SHAPE, pbc=True))
     lp, _, _ = m.forward(spins)
     ms = timed(lambda: obs.local_values(m, spins, log_psi=lp, base_saved=saved))
