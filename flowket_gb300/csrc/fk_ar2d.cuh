@@ -285,16 +285,19 @@ int launch_wgrad_tc(const WgTcArgs& a, int kw, int kcol0, float* dW, float* db, 
 int launch_bias_sum(const void* G, int64_t tiles, int H, int W, int g0, int n, int64_t batch, float* part, float* db,
                     cudaStream_t s);
 
-// Per-sample weight and bias gradients of one conv with 32 input channels on
-// the tensor cores (wgrad_rows_tc_kernel): for every sample b,
+// Per-sample weight and bias gradients of one conv on the tensor cores
+// (wgrad_rows_tc_kernel): for every sample b,
 // dW_b[tap][ci][n] = sum_pix X_b[pix + tap][ci] G_b[pix][g0 + n] and
 // db_b[n] = sum_pix G_b[pix][g0 + n], written to
-// O[(o_kernel + (tap * 32 + ci) * N + n) * o_ld + o_col + b] and
-// O[(o_bias + n) * o_ld + o_col + b].
+// O[(o_kernel + (tap * cin + ci) * N + n) * o_ld + o_col + b] and
+// O[(o_bias + n) * o_ld + o_col + b]. cin = 32 with 16-bit gradients (N = 16
+// or 32), or cin = 64 with float gradients rounded to the operand format
+// (N = 32 or 64).
 struct WgRowsArgs {
-  const void* X;   // activations (16-bit blocked, 32 channels)
-  const void* G;   // gradients (16-bit blocked, gC channels)
-  int gC, g0, N;   // N: 16 or 32
+  const void* X;   // activations (16-bit blocked, cin channels)
+  const void* G;   // gradients (blocked, gC channels; float when g_float)
+  int cin, g_float;
+  int gC, g0, N;
   int ntaps;
   int dr[9], dc[9];
   float* O;

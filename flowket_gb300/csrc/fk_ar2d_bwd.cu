@@ -21,6 +21,8 @@
 // gradients are fp32 throughout.
 #include "fk_ar2d.cuh"
 
+#include <type_traits>
+
 #include <stdlib.h>
 #include <string.h>
 
@@ -706,6 +708,18 @@ __global__ void wgrad_part_reduce_kernel(const float* part, int64_t tiles, int k
     dB[e - kn] = s;
 }
 
+// Per-sample weight gradients of the tensor-core adjoint's 32-channel convs on
+// the tensor cores (wgrad_rows_tc_kernel); FK_AR2D_ROWS=cuda keeps them on the
+// CUDA cores (wgrad_kernel on the same 16-bit gradients, for comparisons).
+static bool rows_on_tensor_cores() {
+  static int v = -1;
+  if (v < 0) {
+    const char* e = getenv("FK_AR2D_ROWS");
+    v = (e && strcmp(e, "cuda") == 0) ? 0 : 1;
+  }
+  return v == 1;
+}
+
 // Where the per-sample rows of conv cd go: the [num_params][batch] array O,
 // or the sink's buffer.
 struct RowsTarget {
@@ -732,6 +746,37 @@ static int launch_wgrad(const NetLayout& L, WgArgs& w, const ConvDesc& cd, float
   int64_t tiles = (batch + kTile - 1) / kTile;
   w.batch = batch;
   w.items = w.ntaps * ((w.cin + 7) / 8) * ((w.N + 7) / 8);
+#ifndef FK_TC_FP16
+  // per-sample rows of the BF16 path's 64-channel convs (CUDA-core adjoint,
+  // float gradients): on the tensor cores, the gradients rounded to bf16
+  if (O && std::is_same<T, tc16>::value && std::is_same<TG, float>::value && w.X && w.cin == 64 &&
+      (w.N == 32 || w.N == 64) && rows_on_tensor_cores() && wgrad_rows_tc_supported(L.H, L.W, w.N)) {
+    RowsTarget tg;
+    const int st = rows_target(L, cd, O, batch, s, sink, &tg);
+    if (st != FK_OK) return st;
+    WgRowsArgs r;
+    memset(&r, 0, sizeof(r));
+    r.X = w.X;
+    r.G = w.G;
+    r.cin = 64;
+    r.g_float = 1;
+    r.gC = w.gC;
+    r.g0 = w.g0;
+    r.N = w.N;
+    r.ntaps = w.ntaps;
+    for (int t = 0; t < w.ntaps; ++t) {
+      r.dr[t] = w.dr[t];
+      r.dc[t] = w.dc[t];
+    }
+    r.O = tg.O;
+    r.o_kernel = tg.o_kernel;
+    r.o_bias = tg.o_bias;
+    r.o_ld = tg.o_ld;
+    r.o_col = tg.o_col;
+    r.batch = batch;
+    return launch_wgrad_rows_tc(r, L.H, L.W, device_error_word(), s);
+  }
+#endif
   if (O) {
     RowsTarget t;
     const int st = rows_target(L, cd, O, batch, s, sink, &t);
@@ -931,18 +976,6 @@ static int64_t tc_bwd_layout(const NetLayout& L, int64_t batch, char* base, TcBw
   return off;
 }
 
-// Per-sample weight gradients of the tensor-core adjoint's 32-channel convs on
-// the tensor cores (wgrad_rows_tc_kernel); FK_AR2D_ROWS=cuda keeps them on the
-// CUDA cores (wgrad_kernel on the same 16-bit gradients, for comparisons).
-static bool rows_on_tensor_cores() {
-  static int v = -1;
-  if (v < 0) {
-    const char* e = getenv("FK_AR2D_ROWS");
-    v = (e && strcmp(e, "cuda") == 0) ? 0 : 1;
-  }
-  return v == 1;
-}
-
 // FK_AR2D_ENGINE=rowwise also selects the CUDA-core adjoint (for comparisons).
 static bool use_tc_adjoint(const NetLayout& L) {
   static int v = -1;
@@ -1015,6 +1048,8 @@ static int backward_tc(const NetLayout& L, const void* packed, const float* para
       }
       r.X = X;
       r.G = Gt;
+      r.cin = 32;
+      r.g_float = 0;
       r.gC = F;
       r.g0 = g0;
       r.N = n;

@@ -30,6 +30,8 @@
 
 #include <string.h>
 
+#include <mutex>
+
 namespace FK_NS {
 
 template <int F>
@@ -568,12 +570,27 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
   for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-template <int N>
+// 8 gradient values of a (pixel, sample, 8-channel group) as one 16-byte
+// operand row: 16-bit gradients as they are, float gradients rounded.
+__device__ __forceinline__ uint4 grad_row(const tc16* p) { return __ldg(reinterpret_cast<const uint4*>(p)); }
+__device__ __forceinline__ uint4 grad_row(const float* p) {
+  const float4 x = __ldg(reinterpret_cast<const float4*>(p));
+  const float4 y = __ldg(reinterpret_cast<const float4*>(p) + 1);
+  return make_uint4(pack_tc16x2(x.x, x.y), pack_tc16x2(x.z, x.w), pack_tc16x2(y.x, y.y), pack_tc16x2(y.z, y.w));
+}
+
+// CIN input channels (32: four taps per M tile, 64: two), N output channels,
+// TG the gradients' type (16-bit, or float from the CUDA-core adjoint). A
+// work item is SPB = 256 / N samples (one TMEM buffer of 256 columns).
+template <int CIN, int N, typename TG>
 __global__ void __launch_bounds__(wgrows::kThreads, 1) wgrad_rows_tc_kernel(const __grid_constant__ WgRowsArgs a,
                                                                              int H, int W, int S, int* err) {
   using namespace wgrows;
   using T = tc16;
   constexpr int NG = N / 8;
+  constexpr int TPM = 128 / CIN;  // taps per M tile
+  constexpr int GPT = CIN / 8;    // 8-channel groups per tap
+  constexpr int SPB = 256 / N;    // samples per TMEM buffer (work item)
   extern __shared__ __align__(1024) uint8_t smem[];
   const int P = H * W;
   const int KS = ksteps(H, W), Qk = KS * 16;
@@ -581,13 +598,13 @@ __global__ void __launch_bounds__(wgrows::kThreads, 1) wgrad_rows_tc_kernel(cons
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + 2 * stage);
   uint64_t* full = bars;          // [2] staged (8 warp arrivals)
   uint64_t* empty = bars + 2;     // [2] MMAs done with a stage (commit)
-  uint64_t* accfull = bars + 4;   // [2] 8 samples' products complete (commit)
+  uint64_t* accfull = bars + 4;   // [2] a work item's products complete (commit)
   uint64_t* accempty = bars + 6;  // [2] written out (4 warp arrivals)
   uint64_t* drain = bars + 8;
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 9);
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  const int ntiles_m = (a.ntaps + 1 + 3) / 4;  // taps and the ones slot, four per M tile
-  const int64_t groups = (a.batch + 7) / 8;
+  const int ntiles_m = (a.ntaps + 1 + TPM - 1) / TPM;  // taps and the ones slot
+  const int64_t groups = (a.batch + SPB - 1) / SPB;
   const int64_t items = groups * ntiles_m;
   if (threadIdx.x == 0) {
     for (int i = 0; i < 2; ++i) {
@@ -608,7 +625,7 @@ __global__ void __launch_bounds__(wgrows::kThreads, 1) wgrad_rows_tc_kernel(cons
   tc_fence_after();
   const uint32_t tmem = *tslot;
   bool abort = false;
-  const int subs = 8 / S;
+  const int subs = SPB / S;
 
   if (warp < kStageWarps) {
     // ---------------------------------------------------------------- staging
@@ -626,41 +643,45 @@ __global__ void __launch_bounds__(wgrows::kThreads, 1) wgrad_rows_tc_kernel(cons
         uint8_t* base = smem + st * stage;
         // thread = (pixel p, sample s) of the stage, s fastest (the S samples of
         // a (pixel, group) are adjacent in the blocked layout); it stages that
-        // pixel's 16 A groups (taps x channel groups) and NG B groups, loads
-        // issued before the stores. No divisions inside the loops.
+        // pixel's 16 A groups (taps x channel groups) and NG B groups, every
+        // load issued before the first store.
         if (tid < Qk * S) {
           const int s = tid % S;
           const int p = tid / S;
-          const int64_t b = grp * 8 + sub * S + s;
+          const int64_t b = grp * SPB + sub * S + s;
           const int64_t tile = b / kTile;
           const int m = (int)(b % kTile);
           const int r0 = p / W, cq = p - (p / W) * W;
           const bool live = p < P;
           uint8_t* arow = base + ((int64_t)s * kGroupRows * Qk + p) * 16;
           uint8_t* brow = base + ((int64_t)S * kGroupRows * Qk + (int64_t)s * NG * Qk + p) * 16;
+          const uint4* src[TPM];
 #pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            const int t = 4 * mt + k;
-            uint4 v[4];
-            const T* src = nullptr;
+          for (int k = 0; k < TPM; ++k) {
+            const int t = TPM * mt + k;
+            src[k] = nullptr;
             if (live && t < a.ntaps) {
               const int r = r0 + a.dr[t], cc = cq + a.dc[t];
-              if (r >= 0 && r < H && cc >= 0 && cc < W) src = blk<T>(a.X, tile, P, r * W + cc, 32) + m * 8;
+              if (r >= 0 && r < H && cc >= 0 && cc < W)
+                src[k] = reinterpret_cast<const uint4*>(blk<T>(a.X, tile, P, r * W + cc, CIN) + m * 8);
             }
-#pragma unroll
-            for (int g = 0; g < 4; ++g)
-              v[g] = src ? *reinterpret_cast<const uint4*>(src + (int64_t)g * kTile * 8) : make_uint4(0u, 0u, 0u, 0u);
-            if (live && t == a.ntaps) v[0] = make_uint4(kTcOnePair, kTcOnePair, kTcOnePair, kTcOnePair);
-#pragma unroll
-            for (int g = 0; g < 4; ++g) *reinterpret_cast<uint4*>(arow + (int64_t)(4 * k + g) * Qk * 16) = v[g];
           }
-          uint4 w[NG];
-          const T* gsrc = live ? blk<T>(a.G, tile, P, p, a.gC) + ((int64_t)(a.g0 / 8) * kTile + m) * 8 : nullptr;
+          const TG* gsrc = live ? blk<TG>(a.G, tile, P, p, a.gC) + ((int64_t)(a.g0 / 8) * kTile + m) * 8 : nullptr;
+          const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
+          uint4 va[kGroupRows], vb[NG];
 #pragma unroll
-          for (int g = 0; g < NG; ++g)
-            w[g] = gsrc ? *reinterpret_cast<const uint4*>(gsrc + (int64_t)g * kTile * 8) : make_uint4(0u, 0u, 0u, 0u);
+          for (int k = 0; k < TPM; ++k)
 #pragma unroll
-          for (int g = 0; g < NG; ++g) *reinterpret_cast<uint4*>(brow + (int64_t)g * Qk * 16) = w[g];
+            for (int g = 0; g < GPT; ++g) va[GPT * k + g] = src[k] ? __ldg(src[k] + g * kTile) : zero;
+#pragma unroll
+          for (int g = 0; g < NG; ++g) vb[g] = gsrc ? grad_row(gsrc + (int64_t)g * kTile * 8) : zero;
+#pragma unroll
+          for (int k = 0; k < TPM; ++k)
+            if (live && TPM * mt + k == a.ntaps) va[GPT * k] = make_uint4(kTcOnePair, kTcOnePair, kTcOnePair, kTcOnePair);
+#pragma unroll
+          for (int i = 0; i < kGroupRows; ++i) *reinterpret_cast<uint4*>(arow + (int64_t)i * Qk * 16) = va[i];
+#pragma unroll
+          for (int g = 0; g < NG; ++g) *reinterpret_cast<uint4*>(brow + (int64_t)g * Qk * 16) = vb[g];
         }
         fence_proxy_async_smem();
         __syncwarp();
@@ -710,9 +731,13 @@ __global__ void __launch_bounds__(wgrows::kThreads, 1) wgrad_rows_tc_kernel(cons
     __syncwarp();
   } else {
     // ---------------------------------------------------------------- drain
-    // warp 9..12 -> TMEM lane quarter 1, 2, 3, 0 = tap slot within the M tile
-    const int k = warp % 4;
+    // warp 9..12 -> TMEM lane quarter 1, 2, 3, 0; M row R = quarter * 32 + lane
+    // is input channel R % CIN of tap slot R / CIN
+    const int q4 = warp % 4;
+    const int R = q4 * 32 + lane;
+    const int k = R / CIN, ci = R % CIN;
     const bool vec = (a.o_ld % 4) == 0 && (a.o_col % 4) == 0;
+    constexpr int JB = SPB < 8 ? SPB : 8;  // samples written per store group
     uint32_t li = 0;
     for (int64_t it = blockIdx.x; it < items && !abort; it += gridDim.x, ++li) {
       const int64_t grp = it / ntiles_m;
@@ -725,29 +750,35 @@ __global__ void __launch_bounds__(wgrows::kThreads, 1) wgrad_rows_tc_kernel(cons
         break;
       }
       tc_fence_after();
-      const int t = 4 * mt + k;
-      const int64_t b0 = grp * 8;
-      const int nb = a.batch - b0 < 8 ? (int)(a.batch - b0) : 8;
-      const uint32_t tl = tmem + buf * 256 + ((uint32_t)(k * 32) << 16);
+      const int t = TPM * mt + k;
+      const int64_t b0 = grp * SPB;
+      const int nb = a.batch - b0 < SPB ? (int)(a.batch - b0) : SPB;
+      const uint32_t tl = tmem + buf * 256 + ((uint32_t)(q4 * 32) << 16);
+      // slot k is warp-uniform when CIN >= 32
       if (t <= a.ntaps) {
         for (int nc = 0; nc < NG; ++nc) {
-          float v[8][8];
+          for (int j0 = 0; j0 < SPB; j0 += JB) {
+            float v[JB][8];
 #pragma unroll
-          for (int j = 0; j < 8; ++j) tmem_ld8(tl + (uint32_t)(j * N + nc * 8), v[j]);
-          tmem_ld_wait();
-          if (t < a.ntaps || lane == 0) {
+            for (int j = 0; j < JB; ++j) tmem_ld8(tl + (uint32_t)((j0 + j) * N + nc * 8), v[j]);
+            tmem_ld_wait();
+            if (t < a.ntaps || ci == 0) {
 #pragma unroll
-            for (int n = 0; n < 8; ++n) {
-              const int64_t row = t < a.ntaps ? a.o_kernel + ((int64_t)(t * 32 + lane) * N + nc * 8 + n)
-                                              : a.o_bias + nc * 8 + n;
-              float* dst = a.O + row * a.o_ld + a.o_col + b0;
-              if (vec && nb == 8) {
-                reinterpret_cast<float4*>(dst)[0] = make_float4(v[0][n], v[1][n], v[2][n], v[3][n]);
-                reinterpret_cast<float4*>(dst)[1] = make_float4(v[4][n], v[5][n], v[6][n], v[7][n]);
-              } else {
+              for (int n = 0; n < 8; ++n) {
+                const int64_t row = t < a.ntaps ? a.o_kernel + ((int64_t)(t * CIN + ci) * N + nc * 8 + n)
+                                                : a.o_bias + nc * 8 + n;
+                float* dst = a.O + row * a.o_ld + a.o_col + b0 + j0;
+                const int nj = nb - j0;
+                if (vec && nj >= JB && JB % 4 == 0) {
 #pragma unroll
-                for (int j = 0; j < 8; ++j)
-                  if (j < nb) dst[j] = v[j][n];
+                  for (int q = 0; q < JB / 4; ++q)
+                    reinterpret_cast<float4*>(dst)[q] =
+                        make_float4(v[4 * q][n], v[4 * q + 1][n], v[4 * q + 2][n], v[4 * q + 3][n]);
+                } else {
+#pragma unroll
+                  for (int j = 0; j < JB; ++j)
+                    if (j < nj) dst[j] = v[j][n];
+                }
               }
             }
           }
@@ -825,34 +856,34 @@ int launch_wgrad_tc(const WgTcArgs& a, int kw, int kcol0, float* dW, float* db, 
 
 bool wgrad_rows_tc_supported(int H, int W, int N) {
   const int S = wgrows::samples_per_stage(H, W, N);
-  return (N == 16 || N == 32) && 2 * wgrows::stage_bytes(S, H, W, N) + 256 <= 220 * 1024 &&
+  return (N == 16 || N == 32 || N == 64) && 2 * wgrows::stage_bytes(S, H, W, N) + 256 <= 220 * 1024 &&
          wgrows::ksteps(H, W) * 16 * S <= wgrows::kStageWarps * 32;
+}
+
+template <int CIN, int N, typename TG>
+static int rows_launch(const WgRowsArgs& a, int H, int W, int* err, cudaStream_t s) {
+  static std::once_flag once;
+  static int attr = FK_OK;
+  std::call_once(once, [] {
+    attr = set_smem<32>((const void*)wgrad_rows_tc_kernel<CIN, N, TG>, 220 * 1024);
+  });
+  if (attr != FK_OK) return attr;
+  const int S = wgrows::samples_per_stage(H, W, N);
+  const int smem = 2 * wgrows::stage_bytes(S, H, W, N) + 256;
+  const int64_t items = (a.batch + 256 / N - 1) / (256 / N) * ((a.ntaps + 128 / CIN) / (128 / CIN));
+  int64_t grid = sm_count();
+  if (grid > items) grid = items;
+  wgrad_rows_tc_kernel<CIN, N, TG><<<(unsigned)grid, wgrows::kThreads, smem, s>>>(a, H, W, S, err);
+  return check_cuda(launched(), "wgrad_rows_tc_kernel");
 }
 
 int launch_wgrad_rows_tc(const WgRowsArgs& a, int H, int W, int* err, cudaStream_t s) {
   if (!wgrad_rows_tc_supported(H, W, a.N) || a.ntaps < 1 || a.ntaps > 9) return FK_ERR_ARG;
-  static bool attr16 = false, attr32 = false;
-  const int S = wgrows::samples_per_stage(H, W, a.N);
-  const int smem = 2 * wgrows::stage_bytes(S, H, W, a.N) + 256;
-  const int64_t items = (a.batch + 7) / 8 * ((a.ntaps + 4) / 4);
-  int64_t grid = sm_count();
-  if (grid > items) grid = items;
-  if (a.N == 16) {
-    if (!attr16) {
-      int st = set_smem<32>((const void*)wgrad_rows_tc_kernel<16>, 220 * 1024);
-      if (st != FK_OK) return st;
-      attr16 = true;
-    }
-    wgrad_rows_tc_kernel<16><<<(unsigned)grid, wgrows::kThreads, smem, s>>>(a, H, W, S, err);
-  } else {
-    if (!attr32) {
-      int st = set_smem<32>((const void*)wgrad_rows_tc_kernel<32>, 220 * 1024);
-      if (st != FK_OK) return st;
-      attr32 = true;
-    }
-    wgrad_rows_tc_kernel<32><<<(unsigned)grid, wgrows::kThreads, smem, s>>>(a, H, W, S, err);
-  }
-  return check_cuda(launched(), "wgrad_rows_tc_kernel");
+  if (a.cin == 32 && !a.g_float && a.N == 16) return rows_launch<32, 16, tc16>(a, H, W, err, s);
+  if (a.cin == 32 && !a.g_float && a.N == 32) return rows_launch<32, 32, tc16>(a, H, W, err, s);
+  if (a.cin == 64 && a.g_float && a.N == 32) return rows_launch<64, 32, float>(a, H, W, err, s);
+  if (a.cin == 64 && a.g_float && a.N == 64) return rows_launch<64, 64, float>(a, H, W, err, s);
+  return FK_ERR_ARG;
 }
 
 int launch_bias_sum(const void* G, int64_t tiles, int H, int W, int g0, int n, int64_t batch, float* part, float* db,

@@ -242,3 +242,37 @@ def test_per_sample_weight_gradients_on_tensor_cores(cuda, tmp_path, shape, dept
     assert got.shape == ref.shape == (m.num_params, b)
     err = np.abs(got - ref).max(axis=0) / np.abs(ref).max(axis=0)
     assert err.max() < 1e-5, err.max()
+
+
+@pytest.mark.parametrize("shape,depth,b", [((6, 6), 3, 130), ((16, 16), 2, 40)])
+def test_per_sample_weight_gradients_on_tensor_cores_f64(cuda, tmp_path, shape, depth, b):
+    """64 channels (the CUDA-core adjoint of the BF16 path, float gradients):
+    the per-sample weight gradients on the tensor cores, the float gradients
+    rounded to bf16 operands, against the CUDA-core per-sample kernel on the
+    same float gradients (FK_AR2D_ROWS=cuda). max |d row| / max |row| per
+    sample, from the bf16 rounding of the gradients: measured 7.6e-4 (6x6)
+    and 5.5e-4 (16x16); bound 3e-3."""
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = (
+        "import sys; sys.path.insert(0, %r);"
+        "import numpy as np, torch;"
+        "from flowket_gb300 import _lib;"
+        "from flowket_gb300.machines import ConvNetAutoregressive2D;"
+        "m = ConvNetAutoregressive2D(%r, %d, 64, weights_normalization=True, precision='bf16', seed=11);"
+        "rng = np.random.default_rng(12);"
+        "s = torch.as_tensor(rng.choice([-1, 1], size=(%d,) + %r).astype(np.int8)).cuda();"
+        "_, _, saved = m.forward(s, mode=_lib.FK_AR2D_SAVE);"
+        "np.save(%r, m.log_derivatives(s, saved).cpu().numpy())"
+    ) % (root, shape, depth, b, shape, str(tmp_path / "o.npy"))
+    env = dict(os.environ, FK_AR2D_ROWS="cuda")
+    subprocess.run([sys.executable, "-c", code], check=True, env=env)
+    ref = np.load(tmp_path / "o.npy").astype(np.complex128)
+    from flowket_gb300 import _lib
+    from flowket_gb300.machines import ConvNetAutoregressive2D
+    m = ConvNetAutoregressive2D(shape, depth, 64, weights_normalization=True, precision="bf16", seed=11)
+    rng = np.random.default_rng(12)
+    s = torch.as_tensor(rng.choice([-1, 1], size=(b,) + shape).astype(np.int8)).cuda()
+    _, _, saved = m.forward(s, mode=_lib.FK_AR2D_SAVE)
+    got = m.log_derivatives(s, saved).cpu().numpy().astype(np.complex128)
+    err = np.abs(got - ref).max(axis=0) / np.abs(ref).max(axis=0)
+    assert err.max() < 3e-3, err.max()
