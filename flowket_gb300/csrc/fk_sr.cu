@@ -453,16 +453,40 @@ struct GramSplitArgs {
 
 __device__ __forceinline__ void gram_split_item(const GramSplitArgs& g, int64_t item, int64_t& i0, int64_t& j0,
                                                 int64_t& c0, int64_t& c1) {
-  // range-major, as gram_item: the CTAs running together share a range
+  // Range-major, as gram_item: the CTAs running together share a range. Within
+  // a range the upper-triangle tiles go in bands of kBand tile rows, column
+  // by column within a band, so that the ~152 tiles in flight span about
+  // kBand A blocks and 152 / kBand B blocks (their operands shared through
+  // L2) instead of a few tile rows with every B block.
+  constexpr int64_t kBand = 8;
   const int64_t tiles = g.items / g.splits;
-  const int64_t split = item / tiles, tile = item % tiles;
-  int64_t ti = 0, rem = tile;
-  while (ti < g.nti && rem >= g.ntj - ti / 2) {
-    rem -= g.ntj - ti / 2;
-    ++ti;
+  const int64_t split = item / tiles;
+  int64_t rem = item % tiles;
+  int64_t b0 = 0;  // first tile row of the band
+  for (; b0 < g.nti; b0 += kBand) {
+    const int64_t b1 = min(g.nti, b0 + kBand);
+    int64_t cnt = 0;
+    for (int64_t ti = b0; ti < b1; ++ti) cnt += g.ntj - ti / 2;
+    if (rem < cnt) break;
+    rem -= cnt;
   }
-  i0 = ti * gram_tc::kM;
-  j0 = (ti / 2 + rem) * gram_tc::kN;
+  const int64_t b1 = min(g.nti, b0 + kBand);
+  // column tj holds the band's rows ti < 2 tj + 2 (tj >= ti / 2)
+  int64_t tj = b0 / 2;
+  for (;;) {
+    const int64_t c = min(b1, 2 * tj + 2) - b0;
+    if (c == b1 - b0) break;  // full columns from here on
+    if (rem < c) break;
+    rem -= c;
+    ++tj;
+  }
+  const int64_t full = b1 - b0;
+  if (min(b1, 2 * tj + 2) - b0 == full) {
+    tj += rem / full;
+    rem %= full;
+  }
+  i0 = (b0 + rem) * gram_tc::kM;
+  j0 = tj * gram_tc::kN;
   c0 = split * g.kper;
   c1 = min(g.kchunks, c0 + g.kper);
 }

@@ -64,14 +64,16 @@ def test_tensor_core_gram_matches_fp64(cuda, p, b, complex_):
 
 
 @pytest.mark.parametrize("p,b,complex_", [(3000, 96, True), (4133, 200, True), (70_000, 512, True),
-                                         (1000, 45, True), (64, 8, True), (33, 300, False), (9000, 1030, False)])
+                                         (1000, 45, True), (64, 8, True), (33, 300, False), (9000, 1030, False),
+                                         (300, 4100, True)])
 def test_split_tensor_core_gram_matches_fp64(cuda, p, b, complex_):
     """fk_sr_gram_split (bf16 hi + lo written once in the blocked operand
     layout) + fk_sr_gram_split_accumulate (bulk-copied operands, the same
     split-BF16 products) + fk_sr_gram_mirror against the FP64 Gram of the
     same FP32 rows, with fk_sr_gram_tc's bounds; column counts that are not
-    multiples of 8, 128 or 256 and row counts that are not multiples of 32.
-    Each call adds into the Gram: a second call doubles it."""
+    multiples of 8, 128 or 256 and row counts that are not multiples of 32;
+    8,200 columns: 65 x 33 tiles in bands of 8 tile rows, the last one
+    partial. Each call adds into the Gram: a second call doubles it."""
     from flowket_gb300 import _lib
     rng = np.random.default_rng(p + 3 * b)
     a = rng.normal(size=(p, b)).astype(np.float32)
