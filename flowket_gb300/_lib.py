@@ -69,6 +69,7 @@ _SIGNATURES = {
     "fk_sr_gram_split_bytes": (c_i64, [c_i64, c_i64]),
     "fk_sr_gram_split": (c_i32, [c_p, c_p, c_i64, c_i64, c_i64, c_i64, c_p, c_i64, c_p]),
     "fk_sr_gram_split_accumulate": (c_i32, [c_p, c_i64, c_i64, c_p, c_p]),
+    "fk_sr_center_split": (c_i32, [c_p, c_p, c_i64, c_i64, c_i64, c_i64, c_i32, c_p, c_i64, c_p]),
     "fk_sr_solve_workspace_bytes": (c_i64, [c_i64]),
     "fk_sr_solve": (c_i32, [c_p, c_i64, c_f64, c_f64, c_p, c_f64, c_i32, c_p, c_p, c_p, c_i64, c_p]),
     "fk_sr_solve_noalloc": (c_i32, [c_p, c_i64, c_f64, c_f64, c_p, c_f64, c_i32, c_p, c_p, c_p]),

@@ -522,12 +522,14 @@ static int sink_flush(RowSink& k, cudaStream_t s) {
     delete a;
     if (nw > 0) FK_CUDA(launched());
   }
-  int st = fk_center_columns(k.buf, k.used * k.groups, k.ld / k.groups, nullptr, s);
-  if (st == FK_OK && k.tensor_cores) {
-    st = fk_sr_gram_split(k.buf, nullptr, k.ld, k.ld, k.used, k.ld, k.split, k.split_bytes, s);
+  int st;
+  if (k.tensor_cores) {
+    // the two passes' column groups [0, B) and [B, 2B) centred and split in one pass
+    st = fk_sr_center_split(k.buf, k.buf + k.ld / 2, k.ld, k.ld / 2, k.used, k.ld, 0, k.split, k.split_bytes, s);
     if (st == FK_OK) st = fk_sr_gram_split_accumulate(k.split, k.used, k.ld, k.gram, s);
-  } else if (st == FK_OK) {
-    st = fk_sr_gram_accumulate(k.buf, k.used, k.ld, k.gram, 0, s);
+  } else {
+    st = fk_center_columns(k.buf, k.used * k.groups, k.ld / k.groups, nullptr, s);
+    if (st == FK_OK) st = fk_sr_gram_accumulate(k.buf, k.used, k.ld, k.gram, 0, s);
   }
   for (int i = 0; i < k.n; ++i) k.at[k.conv[i]] = -1;
   k.used = 0;

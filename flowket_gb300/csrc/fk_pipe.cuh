@@ -256,10 +256,7 @@ __device__ void pipe_issuer(const PipeGeom& g, const PipeItems& items, uint8_t* 
   const uint32_t idesc3 = umma_idesc_tc16(128, 3 * F);
   const uint64_t a0 = umma_sdesc(smem_u32(ring), 2048, 128);
   const uint64_t w0 = umma_sdesc(smem_u32(wsm), 3 * F * 16, 128);
-  constexpr uint32_t kBlk16 = C::kBlk >> 4;           // one ring block
-  constexpr uint32_t kRow16 = C::kWRow >> 4;          // one kernel row of the scatter operand
-  constexpr uint32_t kKs16 = (2 * 2048) >> 4;         // one K=16 step of A
-  constexpr uint32_t kKsW16 = (2 * 3 * F * 16) >> 4;  // one K=16 step of B
+  constexpr uint32_t kBlk16 = C::kBlk >> 4;  // one ring block
   const int W = g.W, o0 = g.o0;
   uint32_t cs = 0;     // ring slot of the current column
   uint32_t gbase = 0;  // global index of output column 0 of the current item

@@ -437,6 +437,71 @@ __global__ void split_kernel(const float* __restrict__ a, const float* __restric
   lo[idx] = ul;
 }
 
+// Centring and split in one pass (center_split_kernel): one CTA per block of
+// 32 rows. Each row is centred within its two column groups, [0, bsz) from a
+// and [bsz, n) from b (the per-row compensated mean of center_kernel, the
+// same arithmetic), optionally written back in place, and split into the
+// blocked hi / lo operands: the rows are read from DRAM once (the second
+// pass over the CTA's 32 rows hits L2).
+__global__ void __launch_bounds__(256) center_split_kernel(float* __restrict__ a, float* __restrict__ b, int64_t ld,
+                                                           int64_t bsz, int64_t rows, int64_t n, int64_t groups,
+                                                           int write_back, uint4* __restrict__ hi,
+                                                           uint4* __restrict__ lo) {
+  __shared__ float mean_sm[32][2];
+  const int64_t kc = blockIdx.x;
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  for (int rr = 0; rr < 4; ++rr) {
+    const int r = warp * 4 + rr;
+    const int64_t p = kc * 32 + r;
+    for (int h = 0; h < 2; ++h) {
+      const int64_t c_lo = h == 0 ? 0 : bsz;
+      const int64_t c_hi = h == 0 ? (bsz < n ? bsz : n) : n;
+      float mu = 0.f;
+      if (p < rows && c_hi > c_lo) {
+        const float* src = h == 0 ? a + p * ld : b + p * ld;
+        const int64_t len = c_hi - c_lo;
+        Kahan k;
+        for (int64_t j = lane; j < len; j += 32) k.add(src[j]);
+        float sum = k.s - k.c;
+        for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        mu = sum / (float)len;
+      }
+      if (lane == 0) mean_sm[r][h] = mu;
+    }
+  }
+  __syncthreads();
+  // 64 columns per pass: thread = (row r, 8-column group gq); the 8 threads
+  // of a row read 256 contiguous bytes of it
+  const int r = threadIdx.x / 8, gq = threadIdx.x % 8;
+  const int64_t p = kc * 32 + r;
+  for (int64_t c0 = 0; c0 < groups * 8; c0 += 64) {
+    const int64_t c = c0 + 8 * gq;
+    float v[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int64_t col = c + e;
+      float x = 0.f;
+      if (p < rows && col < n) {
+        float* q = col < bsz ? a + p * ld + col : b + p * ld + (col - bsz);
+        x = *q - mean_sm[r][col < bsz ? 0 : 1];
+        if (write_back) *q = x;
+      }
+      v[e] = x;
+    }
+    float hv[8], lv[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      hv[e] = __bfloat162float(__float2bfloat16_rn(v[e]));
+      lv[e] = v[e] - hv[e];
+    }
+    const int64_t idx = ((kc * groups + c / 8) * 32 + r);
+    hi[idx] = make_uint4(pack_bf16x2(hv[0], hv[1]), pack_bf16x2(hv[2], hv[3]), pack_bf16x2(hv[4], hv[5]),
+                         pack_bf16x2(hv[6], hv[7]));
+    lo[idx] = make_uint4(pack_bf16x2(lv[0], lv[1]), pack_bf16x2(lv[2], lv[3]), pack_bf16x2(lv[4], lv[5]),
+                         pack_bf16x2(lv[6], lv[7]));
+  }
+}
+
 struct GramSplitArgs {
   const uint8_t* hi;
   const uint8_t* lo;
@@ -1009,6 +1074,24 @@ int fk_sr_gram_split(const float* a, const float* b, int64_t ld, int64_t bsz, in
                (long long)split_bytes_given, (long long)split_bytes(rows, n));
   if (rows == 0) return FK_OK;
   return split_run(a, b ? b : a, ld, bsz, rows, n, split, static_cast<cudaStream_t>(stream));
+}
+
+int fk_sr_center_split(float* a, float* b, int64_t ld, int64_t bsz, int64_t rows, int64_t n, int32_t write_back,
+                       void* split, int64_t split_bytes_given, void* stream) {
+  FK_CHECK_ARG(a && split && rows >= 0 && n > 0 && bsz > 0 && bsz <= n && (b || bsz == n) && ld >= bsz &&
+                   ld >= n - bsz,
+               "fk_sr_center_split: bad arguments");
+  FK_CHECK_ARG(((uintptr_t)split % 16) == 0, "fk_sr_center_split: split must be 16-byte aligned");
+  FK_CHECK_ARG(split_bytes_given >= split_bytes(rows, n), "fk_sr_center_split: split buffer %lld < %lld bytes",
+               (long long)split_bytes_given, (long long)split_bytes(rows, n));
+  if (rows == 0) return FK_OK;
+  const int64_t groups = split_cols_pad(n) / 8;
+  const int64_t kchunks = split_rows_pad(rows) / 32;
+  uint4* hi = static_cast<uint4*>(split);
+  uint4* lo = hi + kchunks * groups * 32;
+  center_split_kernel<<<(unsigned)kchunks, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      a, b ? b : a, ld, bsz, rows, n, groups, write_back, hi, lo);
+  return check_cuda(launched(), "center_split_kernel");
 }
 
 int fk_sr_gram_split_accumulate(const void* split, int64_t rows, int64_t n, double* gram, void* stream) {

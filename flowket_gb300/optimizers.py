@@ -125,17 +125,21 @@ class ComplexValuesStochasticReconfiguration:
         tc = getattr(self.machine, "precision", "fp32") in ("bf16", "fp16")
         return "fk_sr_gram_tc" if tc else "fk_sr_gram"
 
-    def _gram(self, o_re, o_im, p, b, gram, st):
-        """gram = Y^T Y, Y = [o_re | o_im] (p x 2b): on the tensor cores from
-        operands split into bf16 hi + lo once (fk_sr_gram_split, then
-        fk_sr_gram_split_accumulate), or on the CUDA cores (fk_sr_gram)."""
+    def _center_gram(self, o_re, o_im, p, b, gram, st):
+        """Centres the rows of o_re and o_im (p x b each) in place and builds
+        gram = Y^T Y, Y = [o_re | o_im] (p x 2b): on the tensor cores from
+        operands split into bf16 hi + lo once, centring and split in one pass
+        (fk_sr_center_split, then fk_sr_gram_split_accumulate), or on the CUDA
+        cores (fk_center_columns, fk_sr_gram)."""
         n = 2 * b
         if self._gram_entry(b) == "fk_sr_gram":
+            _lib.call("fk_center_columns", _lib.ptr(o_re), p, b, None, st)
+            _lib.call("fk_center_columns", _lib.ptr(o_im), p, b, None, st)
             _lib.call("fk_sr_gram", _lib.ptr(o_re), _lib.ptr(o_im), p, b, _lib.ptr(gram), n * n, st)
             return
         nbytes = _lib.load().fk_sr_gram_split_bytes(p, n)
         split = torch.empty(nbytes, dtype=torch.uint8, device=gram.device)
-        _lib.call("fk_sr_gram_split", _lib.ptr(o_re), _lib.ptr(o_im), b, b, p, n, _lib.ptr(split), nbytes, st)
+        _lib.call("fk_sr_center_split", _lib.ptr(o_re), _lib.ptr(o_im), b, b, p, n, 1, _lib.ptr(split), nbytes, st)
         gram.zero_()
         _lib.call("fk_sr_gram_split_accumulate", _lib.ptr(split), p, n, _lib.ptr(gram), st)
         _lib.call("fk_sr_gram_mirror", _lib.ptr(gram), n, st)
@@ -153,11 +157,9 @@ class ComplexValuesStochasticReconfiguration:
         o_re, o_im = m.log_derivatives_split(spins)
         p = o_re.shape[0]
         st = _lib.stream_ptr()
-        _lib.call("fk_center_columns", _lib.ptr(o_re), p, b, None, st)
-        _lib.call("fk_center_columns", _lib.ptr(o_im), p, b, None, st)
         n = 2 * b
         bf = self._buffers(n, m.device)
-        self._gram(o_re, o_im, p, b, bf["gram"], st)
+        self._center_gram(o_re, o_im, p, b, bf["gram"], st)
         _lib.call("fk_sr_hermitian_embed", _lib.ptr(bf["gram"]), b, st)
         bf["rhs"][:b] = local[:, 0] - local[:, 0].mean()
         bf["rhs"][b:] = local[:, 1] - local[:, 1].mean()
@@ -188,11 +190,9 @@ class ComplexValuesStochasticReconfiguration:
         o_im = m.backward(spins, ones, saved, per_sample=True)
         p = m.num_params
         st = _lib.stream_ptr()
-        _lib.call("fk_center_columns", _lib.ptr(o_re), p, b, None, st)
-        _lib.call("fk_center_columns", _lib.ptr(o_im), p, b, None, st)
         n = 2 * b
         bf = self._buffers(n, m.device)
-        self._gram(o_re, o_im, p, b, bf["gram"], st)
+        self._center_gram(o_re, o_im, p, b, bf["gram"], st)
         bf["rhs"][:b] = local[:, 0] - local[:, 0].mean()
         bf["rhs"][b:] = local[:, 1] - local[:, 1].mean()
         _lib.call("fk_sr_solve", _lib.ptr(bf["gram"]), n, 1.0 / b, self.diag_shift, _lib.ptr(bf["rhs"]), self.tol,

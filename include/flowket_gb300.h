@@ -308,6 +308,12 @@ int64_t fk_sr_gram_split_bytes(int64_t rows, int64_t n);
 int fk_sr_gram_split(const float* a, const float* b, int64_t ld, int64_t bsz, int64_t rows, int64_t n, void* split,
                      int64_t split_bytes, void* stream);
 int fk_sr_gram_split_accumulate(const void* split, int64_t rows, int64_t n, double* gram, void* stream);
+/* fk_center_columns and fk_sr_gram_split in one pass over the rows: every
+ * row of Y (columns [0, bsz) from a, [bsz, n) from b, row stride ld) centred
+ * within those two column groups with fk_center_columns' arithmetic,
+ * written back in place when write_back != 0, and split into `split`. */
+int fk_sr_center_split(float* a, float* b, int64_t ld, int64_t bsz, int64_t rows, int64_t n, int32_t write_back,
+                       void* split, int64_t split_bytes, void* stream);
 /* FP64 conjugate gradients on (scale * gram + shift I) x = rhs, stopping at
  * ||r|| <= tol ||rhs|| or max_iter (linear_equations.py:34-137); stats (device,
  * optional) = {iterations, ||r||^2, tol^2 ||rhs||^2}. No host synchronisation. */

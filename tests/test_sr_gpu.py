@@ -109,6 +109,36 @@ def test_split_tensor_core_gram_matches_fp64(cuda, p, b, complex_):
     assert b"split buffer" in lib.fk_last_error()
 
 
+@pytest.mark.parametrize("p,b", [(1000, 96), (77, 45), (300, 1030)])
+def test_center_split_equals_center_then_split(cuda, p, b):
+    """fk_sr_center_split (centring of each row within [0, b) and [b, 2b),
+    written back, and the split in one pass) gives bitwise the rows of
+    fk_center_columns on each half and the split operands of
+    fk_sr_gram_split on them; without write-back the rows stay as they were."""
+    from flowket_gb300 import _lib
+    rng = np.random.default_rng(p + b)
+    a = torch.as_tensor(rng.normal(1.0, 2.0, size=(p, b)).astype(np.float32)).cuda()
+    c = torch.as_tensor(rng.normal(-0.5, 1.0, size=(p, b)).astype(np.float32)).cuda()
+    lib = _lib.load()
+    n = 2 * b
+    nbytes = lib.fk_sr_gram_split_bytes(p, n)
+    st = _lib.stream_ptr()
+    a1, c1 = a.clone(), c.clone()
+    split1 = torch.zeros(nbytes, dtype=torch.uint8, device="cuda")
+    _lib.call("fk_sr_center_split", _lib.ptr(a1), _lib.ptr(c1), b, b, p, n, 1, _lib.ptr(split1), nbytes, st)
+    a2, c2 = a.clone(), c.clone()
+    _lib.call("fk_center_columns", _lib.ptr(a2), p, b, None, st)
+    _lib.call("fk_center_columns", _lib.ptr(c2), p, b, None, st)
+    split2 = torch.zeros(nbytes, dtype=torch.uint8, device="cuda")
+    _lib.call("fk_sr_gram_split", _lib.ptr(a2), _lib.ptr(c2), b, b, p, n, _lib.ptr(split2), nbytes, st)
+    assert torch.equal(a1, a2) and torch.equal(c1, c2)
+    assert torch.equal(split1, split2)
+    a3, c3 = a.clone(), c.clone()
+    split3 = torch.zeros(nbytes, dtype=torch.uint8, device="cuda")
+    _lib.call("fk_sr_center_split", _lib.ptr(a3), _lib.ptr(c3), b, b, p, n, 0, _lib.ptr(split3), nbytes, st)
+    assert torch.equal(a3, a) and torch.equal(c3, c) and torch.equal(split3, split2)
+
+
 def test_tensor_core_gram_rejects_unsupported_shapes(cuda):
     from flowket_gb300 import _lib
     lib = _lib.load()
