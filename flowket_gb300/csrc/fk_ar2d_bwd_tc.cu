@@ -465,25 +465,40 @@ __global__ void __launch_bounds__(kWgThreads, 1) wgrad_tc_kernel(const __grid_co
 
 // Sums the per-CTA partials in CTA order into the raw kernel gradient
 // dW[((i*kw + j)*cin + ci)*n + co] (i = kernel row, j = kernel column).
-__global__ void wgrad_reduce_kernel(const float* part, int parts, int x_rows, int ntc, int n, int kw, int kcol0,
-                                    float* dW, const float* part_bias, float* db) {
+// Sums the per-CTA partials in a fixed order: block = 32 elements x 8 lanes
+// of partials; lane group pg sums partials pg, pg + 8, ...; the 8 sums are
+// then added in order pg = 0..7.
+__global__ void __launch_bounds__(256) wgrad_reduce_kernel(const float* part, int parts, int x_rows, int ntc, int n,
+                                                           int kw, int kcol0, float* dW, const float* part_bias,
+                                                           float* db) {
+  __shared__ float acc[8][33];
   const int per = x_rows * 32 * ntc * n;
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= per) {
-    if (db && e < per + n) {
-      float s = 0.f;
-      for (int b = 0; b < parts; ++b) s += part_bias[(int64_t)b * n + (e - per)];
-      db[e - per] = s;
-    }
+  const int eg = threadIdx.x % 32, pg = threadIdx.x / 32;
+  const int e = blockIdx.x * 32 + eg;
+  const bool bias = e >= per;
+  float s = 0.f;
+  if (!bias) {
+#pragma unroll 4
+    for (int b = pg; b < parts; b += 8) s += part[(int64_t)b * per + e];
+  } else if (db && e < per + n) {
+#pragma unroll 4
+    for (int b = pg; b < parts; b += 8) s += part_bias[(int64_t)b * n + (e - per)];
+  }
+  acc[pg][eg] = s;
+  __syncthreads();
+  if (pg != 0) return;
+  float t = 0.f;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) t += acc[q][eg];
+  if (bias) {
+    if (db && e < per + n) db[e - per] = t;
     return;
   }
-  float s = 0.f;
-  for (int b = 0; b < parts; ++b) s += part[(int64_t)b * per + e];
   const int row = e / (ntc * n), col = e % (ntc * n);
   const int i = row / 32, ci = row % 32;
   const int jpos = col / n, co = col % n;
   const int j = kcol0 + (ntc - 1 - jpos);
-  dW[((int64_t)(i * kw + j) * 32 + ci) * n + co] = s;
+  dW[((int64_t)(i * kw + j) * 32 + ci) * n + co] = t;
 }
 
 // Bias gradient, step 1: per tile (one CTA, thread = sample) the sum over
@@ -849,8 +864,8 @@ int launch_wgrad_tc(const WgTcArgs& a, int kw, int kcol0, float* dW, float* db, 
   wgrad_tc_kernel<32><<<(unsigned)grid, kWgThreads, WgCfg<32>::kSmem, s>>>(a, H, W, items, err);
   FK_CUDA(launched());
   const int per = a.x_rows * 32 * a.ntc * a.n + (a.bias_jpos >= 0 ? a.n : 0);
-  wgrad_reduce_kernel<<<(per + 255) / 256, 256, 0, s>>>(a.part, (int)grid, a.x_rows, a.ntc, a.n, kw, kcol0, dW,
-                                                        a.part_bias, a.bias_jpos >= 0 ? db : nullptr);
+  wgrad_reduce_kernel<<<(per + 31) / 32, 256, 0, s>>>(a.part, (int)grid, a.x_rows, a.ntc, a.n, kw, kcol0, dW,
+                                                      a.part_bias, a.bias_jpos >= 0 ? db : nullptr);
   return check_cuda(launched(), "wgrad_reduce_kernel");
 }
 
