@@ -71,3 +71,29 @@ def test_bad_arguments_are_rejected_without_launch(built):
     assert st == -1 and b"NULL" in lib.fk_last_error()
     st = lib.fk_adam_step(None, None, None, None, 4, 0, 1e-3, 0.9, 0.999, 1e-7, None)
     assert st == -1
+
+
+def test_sr_gram_entry_points_check_arguments_without_launch(built):
+    """The block-by-block and split-operand Gram entry points and the
+    streamed SR Gram reject bad arguments on the host, before any launch,
+    and their size queries answer without a GPU."""
+    import ctypes
+    from flowket_gb300 import _lib
+    lib = _lib.load()
+    # split operands: rows padded to 32, columns to 256, bf16 hi + lo
+    assert lib.fk_sr_gram_split_bytes(100, 300) == 2 * 128 * 512 * 2
+    assert lib.fk_sr_gram_split_bytes(0, 8) == 0
+    assert lib.fk_sr_gram_split_bytes(-1, 8) == -1
+    assert lib.fk_sr_gram_split(None, None, 8, 8, 4, 8, None, 0, None) == -1
+    assert lib.fk_sr_center_split(None, None, 8, 8, 4, 16, 1, None, 0, None) == -1
+    assert lib.fk_sr_gram_split_accumulate(None, 4, 8, None, None) == -1
+    assert lib.fk_sr_gram_accumulate(None, 4, 8, None, 0, None) == -1
+    assert lib.fk_sr_gram_mirror(None, 8, None) == -1
+    d = _lib.Ar2dDesc(4, 4, 3, 16, 1, _lib.PRECISIONS["bf16"], 0)
+    assert lib.fk_ar2d_sr_gram_workspace_bytes(ctypes.byref(d), 64) > 0
+    cc = lib.fk_ar2d_sr_gram_min_rows(ctypes.byref(d), 64, 0)
+    tc = lib.fk_ar2d_sr_gram_min_rows(ctypes.byref(d), 64, 1)
+    assert 0 < cc < tc
+    assert lib.fk_ar2d_sr_gram(ctypes.byref(d), None, None, None, 64, None, 0, None, 0, None, 0, None, 1,
+                               None) == -1
+    assert b"NULL" in lib.fk_last_error()
