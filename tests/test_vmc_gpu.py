@@ -84,6 +84,30 @@ def test_causal_reuse_equals_full_forward(cuda, precision, which):
     assert torch.equal(e_full, e_reuse)
 
 
+@pytest.mark.parametrize("precision,which,shape,depth,f", [("bf16", 0, (10, 10), 4, 32), ("fp16", 1, (6, 7), 3, 32),
+                                                         ("bf16", 1, (6, 6), 3, 64), ("fp32", 0, (6, 6), 3, 32),
+                                                         ("bf16", 2, (4, 4), 5, 16)])
+def test_causal_reuse_equals_full_forward_engines(cuda, precision, which, shape, depth, f):
+    """The causal-reuse forward (every op from the first flipped row rk, the
+    rows above and the rows the first evaluated row's taps read gathered from
+    the base activations) gives bitwise the full forward on every engine:
+    pipelined (F = 32), per-pixel (F = 64) and FP32. (The V stream of row r
+    depends on the spins of row r: its taps include row r, and the shift
+    that makes the network autoregressive comes after it, when row r's V
+    output feeds Cat at row r + 1; so the V ops of row rk are evaluated too.)"""
+    from flowket_gb300.machines import ConvNetAutoregressive2D
+    from flowket_gb300.observables import Observable
+    from flowket_gb300.samplers import FastAutoregressiveSampler
+    m = ConvNetAutoregressive2D(shape, depth, f, weights_normalization=True, precision=precision, seed=4)
+    op = _ops(shape)[which][0]
+    spins, lp, saved = FastAutoregressiveSampler(m, 200, seed=9).sample()
+    obs = Observable(op, evaluation_batch_size=1024)
+    _, _, bf, rows = obs.connections(spins)
+    full = m.forward(bf["configs"][:rows])[0]
+    reuse = m.forward_connections(bf["configs"], bf["owner"], bf["cflips"], rows, saved, 200, chunk=1024)
+    assert torch.equal(full, reuse[:rows])
+
+
 def test_exact_variational_matches_oracle_and_finite_differences(cuda):
     """ExactVariational (exact_variational.py:96-155) on 3x3 Heisenberg PBC:
     the energy, variance and probabilities equal the oracle's closed form over
