@@ -31,6 +31,11 @@ struct FwdCfg {
   static constexpr int kBias = 64 * 4;              // main (F) + chained (<= 32) biases
   static constexpr int kMaxW = 16;                  // head partials [W][128] float2
   static constexpr int kSmemBase = C::kRing + C::kW + kCW + C::kCA + kBias + C::kBars;
+  // TMEM: a ring of kNS accumulator slots of F columns, then the kNB chained
+  // accumulators (32 columns each) -- a deeper ring than the adjoint's, whose
+  // chained accumulators take 2F columns each
+  static constexpr int kNS = (512 - C::kNB * 32) / F;
+  static constexpr uint32_t kChainCol = (uint32_t)(kNS * F);
   static int head_bytes(int w) { return w * kTile * 8; }
 };
 
@@ -47,7 +52,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) op_pipe_kernel(const __grid_c
   constexpr int F2 = F / 2;
   constexpr int NC2 = F2 < 16 ? 16 : F2;
   constexpr int NB = C::kNB;
-  constexpr int NS = C::kNS;
+  constexpr int NS = FC::kNS;
   constexpr int NR = C::kNcol;
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t* ring = smem;
@@ -125,9 +130,9 @@ __global__ void __launch_bounds__(kPipeThreads, 1) op_pipe_kernel(const __grid_c
                        WeightCopy{cwsm, a.chain.w, has_chain ? chain_bytes : 0u}, WeightCopy{nullptr, nullptr, 0u},
                        err, abort);
   } else if (warp == 1) {
-    pipe_issuer<F>(geom, items, ring, wsm, tmem, empty, accf, &drain[0], err, abort);
+    pipe_issuer<F, NS>(geom, items, ring, wsm, tmem, empty, accf, &drain[0], err, abort);
   } else if (warp == 2) {
-    pipe_waiter<F>(geom, items, full, wbar, acce, err, abort);
+    pipe_waiter<F, NS>(geom, items, full, wbar, acce, err, abort);
   } else if (warp == 3) {
     // ------------------------------------------------------------------ chain issuer
     // The chained 1x1 MMA of each output, on the epilogue's staged bf16
@@ -145,7 +150,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) op_pipe_kernel(const __grid_c
           tc_fence_after();
 #pragma unroll
           for (int ks = 0; ks < F / 16; ++ks)
-            umma_bf16(tmem + C::kChainCol + b * 32, ca0 + ((b * (kTile * F * 2) + ks * 2 * 2048) >> 4),
+            umma_bf16(tmem + FC::kChainCol + b * 32, ca0 + ((b * (kTile * F * 2) + ks * 2 * 2048) >> 4),
                       cw0 + ((ks * 2 * cnp * 16) >> 4), idesc_c, ks > 0 ? 1u : 0u);
           umma_commit(&cf[b]);
         }
@@ -178,9 +183,9 @@ __global__ void __launch_bounds__(kPipeThreads, 1) op_pipe_kernel(const __grid_c
       tc_fence_after();
       float out[32];
       if (kind == kConvC)
-        tread<16>(tl, C::kChainCol + b * 32, out);
+        tread<16>(tl, FC::kChainCol + b * 32, out);
       else
-        tread<NC2>(tl, C::kChainCol + b * 32, out);
+        tread<NC2>(tl, FC::kChainCol + b * 32, out);
       tc_fence_before();
       const int pix = pr * W + pc;
       if (kind == kConvV) {
@@ -379,6 +384,8 @@ bool pipe_supported(int F, int W) { return (F == 16 || F == 32) && W >= 2 && W <
 
 static_assert(FwdCfg<32>::kSmemBase + 16 * kTile * 8 <= 227 * 1024, "pipelined engine exceeds shared memory");
 static_assert(FwdCfg<16>::kSmemBase + 16 * kTile * 8 <= 227 * 1024, "pipelined engine exceeds shared memory");
-static_assert(3 * 32 <= 256 && PipeCfg<16>::kNS * 16 <= 256, "TMEM layout");
+static_assert(FwdCfg<32>::kChainCol + PipeCfg<32>::kNB * 32 <= 512 &&
+                  FwdCfg<16>::kChainCol + PipeCfg<16>::kNB * 32 <= 512 && FwdCfg<32>::kNS >= 6,
+              "TMEM layout");
 
 }  // namespace FK_NS

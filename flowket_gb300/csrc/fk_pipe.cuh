@@ -157,12 +157,11 @@ __device__ void pipe_producer(const PipeGeom& g, const PipeItems& items, const v
 constexpr int kColsPerStep = 2;
 
 // Waiter (whole warp).
-template <int F>
+template <int F, int NS = PipeCfg<F>::kNS>
 __device__ void pipe_waiter(const PipeGeom& g, const PipeItems& items, uint64_t* full, uint64_t* wbar,
                             uint64_t* acce, int* err, bool& abort) {
   using C = PipeCfg<F>;
   constexpr int NR = C::kNcol;
-  constexpr int NS = C::kNS;
   static_assert(NR >= 2 * kColsPerStep && NS >= 3 + kColsPerStep + 1, "ring or TMEM slots too few for a step");
   pwait(wbar, 0, err, abort);
   uint32_t gx = 0, gbase = 0;
@@ -243,13 +242,12 @@ __device__ __forceinline__ void issue_rev_partial(uint64_t a_col, uint64_t b_liv
 
 // Issuer (whole warp; lane 0 issues). `w0` is the descriptor of kernel row 0
 // of the scatter operand ([F/8][3F][8] per kernel row).
-template <int F>
+template <int F, int NS = PipeCfg<F>::kNS>
 __device__ void pipe_issuer(const PipeGeom& g, const PipeItems& items, uint8_t* ring, uint8_t* wsm,
                             uint32_t tmem, uint64_t* empty, uint64_t* accf, uint64_t* drain, int* err,
                             bool& abort) {
   using C = PipeCfg<F>;
   constexpr int NR = C::kNcol;
-  constexpr int NS = C::kNS;
   const int lane = threadIdx.x % 32;
   const uint32_t idesc1 = umma_idesc_tc16(128, F);
   const uint32_t idesc2 = umma_idesc_tc16(128, 2 * F);
