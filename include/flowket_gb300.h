@@ -177,13 +177,13 @@ int fk_ar2d_backward(const fk_ar2d_desc* desc, const void* packed, const float* 
  * rows of fk_ar2d_backward with seeds (1, 0) and (0, 1). Both per-sample
  * adjoints run together over the one set of activations in `saved`; each
  * conv's rows go, as they are produced, to a row buffer of rows_floats
- * floats (at least fk_ar2d_sr_gram_min_rows with the same tensor_cores);
- * when the next step's convs do
- * not fit, and at the end, the buffered rows get the weight-norm chain rule,
- * are centred (fk_center_columns) and Y^T Y of the buffer is added into gram
- * (tensor_cores = 0: fk_sr_gram_accumulate on the CUDA cores; 1: the split
- * BF16 tensor-core Gram, fk_sr_gram_split + fk_sr_gram_split_accumulate, its
- * split operands kept in the same buffer after the rows). */
+ * floats (at least fk_ar2d_sr_gram_min_rows with the same tensor_cores).
+ * When the next step's convs do not fit, and at the end, the buffered rows
+ * get the weight-norm chain rule and Y^T Y of the buffer is added into gram:
+ * tensor_cores = 0: centred (fk_center_columns) and fk_sr_gram_accumulate on
+ * the CUDA cores; 1: centred and split in one pass (fk_sr_center_split, the
+ * split operands kept in the same buffer after the rows) and
+ * fk_sr_gram_split_accumulate on the tensor cores. */
 int64_t fk_ar2d_sr_gram_workspace_bytes(const fk_ar2d_desc* desc, int64_t batch);
 int64_t fk_ar2d_sr_gram_min_rows(const fk_ar2d_desc* desc, int64_t batch, int32_t tensor_cores);
 int fk_ar2d_sr_gram(const fk_ar2d_desc* desc, const void* packed, const float* params, const int8_t* spins,
@@ -296,8 +296,10 @@ int fk_sr_gram_accumulate(const float* y, int64_t rows, int64_t n, double* gram,
                           void* stream);
 /* Copies the upper triangle of gram (n x n) into the lower one. */
 int fk_sr_gram_mirror(double* gram, int64_t n, void* stream);
-/* The tensor-core Gram in two stages, for Grams that read each value many
- * times (n / 128 + n / 256 tiles per value): fk_sr_gram_split writes Y (rows
+/* The tensor-core Gram (the S matrix of
+ * optimizers/stochastic_reconfiguration/optimizer.py:94-114 in sample space)
+ * in two stages, for Grams that read each value many times (n / 128 +
+ * n / 256 tiles per value): fk_sr_gram_split writes Y (rows
  * x n, column c from a[p * ld + c] when c < bsz, else b[p * ld + c - bsz];
  * b = NULL: all from a) once as bf16 hi + lo in the blocked operand layout
  * (fk_sr_gram_split_bytes(rows, n) bytes, 16-byte aligned), and
